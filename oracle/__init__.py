@@ -1,0 +1,227 @@
+"""CPU oracle for the PIC-cycle hot path -- TEST INFRASTRUCTURE ONLY.
+
+The oracle is a plain C++ restatement (``pic_oracle.hpp``) of PIConGPU's
+reference algorithms for the electromagnetic PIC step: Yee field solver
+(fields/MaxwellSolver/FDTD/FDTDBase.kernel), form-factor gather
+(algorithms/FieldToParticleInterpolation.hpp), Boris push
+(particles/pusher/particlePusherBoris.hpp), moveParticle
+(particles/MoveParticle.hpp), Esirkepov deposition
+(fields/currentDeposition/Esirkepov/Esirkepov.hpp) and the energy and charge
+conservation diagnostics.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may load it, and only as the checker.
+
+Data conventions (shared with the CUDA library's host exchange format):
+
+* fields: float32 arrays of shape ``(3, nz, ny, nx)``, no guard cells, periodic;
+* particles: dict with ``pos`` (3, n) float32 in-cell positions in [0, 1),
+  ``mom`` (3, n) float32 macro-weighted momenta, ``w`` (n,) float32 weightings,
+  ``sc`` (n,) int32 supercell index, ``lcell`` (n,) uint16 cell index inside
+  the supercell and optionally ``id`` (n,) uint32.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+
+class OrcGrid(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("nx", "ny", "nz", "sx", "sy", "sz")] + [
+        (n, ctypes.c_float) for n in ("dx", "dy", "dz", "dt", "c", "eps0")
+    ]
+
+
+class OrcSpecies(ctypes.Structure):
+    _fields_ = [
+        ("charge", ctypes.c_float),
+        ("mass", ctypes.c_float),
+        ("shape", ctypes.c_int),
+        ("pusher", ctypes.c_int),
+        ("current", ctypes.c_int),
+    ]
+
+
+class OrcField(ctypes.Structure):
+    _fields_ = [("c", ctypes.c_void_p * 3)]
+
+
+class OrcParticles(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_uint64),
+        ("pos", ctypes.c_void_p * 3),
+        ("mom", ctypes.c_void_p * 3),
+        ("w", ctypes.c_void_p),
+        ("sc", ctypes.c_void_p),
+        ("lcell", ctypes.c_void_p),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library with its Makefile (g++, OpenMP)."""
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.POINTER
+        vp = ctypes.c_void_p
+        L.orc_shape_value.restype = ctypes.c_float
+        L.orc_shape_value.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float]
+        L.orc_shape_ca_array.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_int, vp]
+        L.orc_shape_os_array.argtypes = [ctypes.c_int, ctypes.c_float, vp]
+        L.orc_move_particle.restype = ctypes.c_int
+        L.orc_move_particle.argtypes = [P(OrcGrid), vp, vp, vp]
+        L.orc_gather.argtypes = [P(OrcGrid), ctypes.c_int, P(OrcField), ctypes.c_int, vp, vp, vp]
+        L.orc_yee_b_half.argtypes = [P(OrcGrid), P(OrcField), P(OrcField)]
+        L.orc_yee_e.argtypes = [P(OrcGrid), P(OrcField), P(OrcField)]
+        L.orc_add_current.argtypes = [P(OrcGrid), P(OrcField), P(OrcField)]
+        L.orc_push.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), P(OrcField), P(OrcField)]
+        L.orc_deposit.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), P(OrcField), ctypes.c_int]
+        L.orc_esirkepov_one.argtypes = [P(OrcGrid), ctypes.c_int, vp, vp, vp, ctypes.c_float, P(OrcField)]
+        L.orc_step.argtypes = [
+            P(OrcGrid),
+            ctypes.c_int,
+            P(OrcSpecies),
+            P(OrcParticles),
+            P(OrcField),
+            P(OrcField),
+            P(OrcField),
+            ctypes.c_int,
+        ]
+        L.orc_charge_density.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), vp]
+        L.orc_charge_residual.restype = ctypes.c_double
+        L.orc_charge_residual.argtypes = [P(OrcGrid), P(OrcField), vp, vp]
+        L.orc_kinetic_energy.restype = ctypes.c_double
+        L.orc_kinetic_energy.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles)]
+        L.orc_field_energy.argtypes = [P(OrcGrid), P(OrcField), P(OrcField), vp]
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+# ----------------------------------------------------------------- helpers
+def _ptr(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"], "arrays handed to the oracle must be C-contiguous"
+    return a.ctypes.data
+
+
+def grid(g) -> OrcGrid:
+    """Build the ctypes grid from any object/dict with nx..eps0 attributes."""
+    get = (lambda k: g[k]) if isinstance(g, dict) else (lambda k: getattr(g, k))
+    return OrcGrid(*[int(get(k)) for k in ("nx", "ny", "nz", "sx", "sy", "sz")],
+                   *[float(get(k)) for k in ("dx", "dy", "dz", "dt", "c", "eps0")])
+
+
+def species(s) -> OrcSpecies:
+    get = (lambda k: s[k]) if isinstance(s, dict) else (lambda k: getattr(s, k))
+    return OrcSpecies(float(get("charge")), float(get("mass")), int(get("shape")),
+                      int(get("pusher")), int(get("current")))
+
+
+def field(F: np.ndarray) -> OrcField:
+    assert F.dtype == np.float32 and F.shape[0] == 3 and F.flags["C_CONTIGUOUS"]
+    f = OrcField()
+    for d in range(3):
+        f.c[d] = F[d].ctypes.data
+    return f
+
+
+def particles(p: dict) -> OrcParticles:
+    for k, dt in (("pos", np.float32), ("mom", np.float32), ("w", np.float32), ("sc", np.int32),
+                  ("lcell", np.uint16)):
+        assert p[k].dtype == dt and p[k].flags["C_CONTIGUOUS"], k
+    o = OrcParticles()
+    o.n = p["w"].shape[0]
+    for d in range(3):
+        o.pos[d] = p["pos"][d].ctypes.data
+        o.mom[d] = p["mom"][d].ctypes.data
+    o.w = _ptr(p["w"])
+    o.sc = _ptr(p["sc"])
+    o.lcell = _ptr(p["lcell"])
+    return o
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def yee_b_half(g, E, B):
+    lib().orc_yee_b_half(grid(g), field(E), field(B))
+
+
+def yee_e(g, B, E):
+    lib().orc_yee_e(grid(g), field(B), field(E))
+
+
+def add_current(g, J, E):
+    lib().orc_add_current(grid(g), field(J), field(E))
+
+
+def push(g, s, p, E, B):
+    lib().orc_push(grid(g), species(s), particles(p), field(E), field(B))
+
+
+def deposit(g, s, p, J, threads: int = 1):
+    lib().orc_deposit(grid(g), species(s), particles(p), field(J), int(threads))
+
+
+def esirkepov_one(g, shape, cell, pos, vel, charge, J):
+    cell = np.ascontiguousarray(cell, dtype=np.int32)
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    vel = np.ascontiguousarray(vel, dtype=np.float32)
+    lib().orc_esirkepov_one(grid(g), int(shape), _ptr(cell), _ptr(pos), _ptr(vel), float(charge), field(J))
+
+
+def step(g, species_list, plist, E, B, J, threads: int = 1):
+    n = len(species_list)
+    S = (OrcSpecies * n)(*[species(s) for s in species_list])
+    P = (OrcParticles * n)(*[particles(p) for p in plist])
+    lib().orc_step(grid(g), n, S, P, field(E), field(B), field(J), int(threads))
+
+
+def gather(g, shape, F, is_b, cell, pos):
+    cell = np.ascontiguousarray(cell, dtype=np.int32)
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    out = np.zeros(3, np.float32)
+    lib().orc_gather(grid(g), int(shape), field(F), int(bool(is_b)), _ptr(cell), _ptr(pos), _ptr(out))
+    return out
+
+
+def charge_density(g, s, p, rho):
+    lib().orc_charge_density(grid(g), species(s), particles(p), _ptr(rho))
+
+
+def charge_residual(g, E, rho):
+    out = np.zeros_like(rho)
+    m = lib().orc_charge_residual(grid(g), field(E), _ptr(rho), _ptr(out))
+    return m, out
+
+
+def kinetic_energy(g, s, p) -> float:
+    return lib().orc_kinetic_energy(grid(g), species(s), particles(p))
+
+
+def field_energy(g, E, B):
+    out = np.zeros(2, np.float64)
+    lib().orc_field_energy(grid(g), field(E), field(B), _ptr(out))
+    return out
+
+
+def move_particle(g, pos, lcell):
+    pos = np.array(pos, dtype=np.float32)
+    lc = np.array([lcell], dtype=np.uint16)
+    d = np.zeros(3, np.int32)
+    mm = lib().orc_move_particle(grid(g), _ptr(pos), _ptr(lc), _ptr(d))
+    return pos, int(lc[0]), int(mm), d

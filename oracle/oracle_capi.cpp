@@ -1,0 +1,215 @@
+// C entry points of the CPU oracle (test infrastructure only; see pic_oracle.hpp).
+// Loaded by tests/ and by bench.py's CPU-baseline leg through ctypes.
+#ifdef _OPENMP
+#    include <omp.h>
+#endif
+#include "pic_oracle.hpp"
+
+#include <cstdint>
+
+extern "C"
+{
+    struct orc_grid
+    {
+        int nx, ny, nz, sx, sy, sz;
+        float dx, dy, dz, dt, c, eps0;
+    };
+    struct orc_species
+    {
+        float charge, mass;
+        int shape, pusher, current;
+    };
+    struct orc_field
+    {
+        float* c[3];
+    };
+    struct orc_particles
+    {
+        uint64_t n;
+        float* pos[3];
+        float* mom[3];
+        float* w;
+        int32_t* sc;
+        uint16_t* lcell;
+    };
+}
+
+namespace
+{
+    orc::Grid toGrid(orc_grid const* g)
+    {
+        return orc::Grid{g->nx, g->ny, g->nz, g->sx, g->sy, g->sz, g->dx, g->dy, g->dz, g->dt, g->c, g->eps0};
+    }
+    orc::SpeciesParam toSp(orc_species const* s)
+    {
+        return orc::SpeciesParam{s->charge, s->mass, s->shape, s->pusher, s->current};
+    }
+    orc::Field3<float> toF(orc_field const* f)
+    {
+        return orc::Field3<float>{{f->c[0], f->c[1], f->c[2]}};
+    }
+    orc::Particles<float> toP(orc_particles const* p)
+    {
+        orc::Particles<float> r;
+        r.n = p->n;
+        for(int d = 0; d < 3; ++d)
+        {
+            r.pos[d] = p->pos[d];
+            r.mom[d] = p->mom[d];
+        }
+        r.w = p->w;
+        r.sc = p->sc;
+        r.lcell = p->lcell;
+        return r;
+    }
+} // namespace
+
+extern "C"
+{
+    int orc_abi_version() { return 1; }
+
+    void orc_set_threads(int n)
+    {
+#ifdef _OPENMP
+        omp_set_num_threads(n > 0 ? n : 1);
+#else
+        (void) n;
+#endif
+    }
+
+    int orc_max_threads()
+    {
+#ifdef _OPENMP
+        return omp_get_max_threads();
+#else
+        return 1;
+#endif
+    }
+
+    // piecewise assignment functions: onSupport=0 -> ChargeAssignment, 1 -> ChargeAssignmentOnSupport
+    float orc_shape_value(int shape, int onSupport, float x)
+    {
+        return onSupport ? orc::ShapeFn<float>::os(shape, x) : orc::ShapeFn<float>::ca(shape, x);
+    }
+
+    // ChargeAssignment::shapeArray(pos, isOutOfRange): support+1 values
+    void orc_shape_ca_array(int shape, float pos, int isOutOfRange, float* out)
+    {
+        orc::ShapeFn<float>::caArray(shape, pos, isOutOfRange != 0, out);
+    }
+
+    // ChargeAssignmentOnSupport::shapeArray(x): support values
+    void orc_shape_os_array(int shape, float x, float* out)
+    {
+        float v[6] = {0, 0, 0, 0, 0, 0};
+        orc::ShapeFn<float>::baseArray(shape, x, v);
+        for(int i = 0; i < orc::support(shape); ++i)
+            out[i] = v[i];
+    }
+
+    int orc_move_particle(orc_grid const* g, float* pos, uint16_t* lcell, int* dir)
+    {
+        orc::Grid G = toGrid(g);
+        return orc::moveParticle(G, pos, *lcell, dir);
+    }
+
+    void orc_gather(
+        orc_grid const* g,
+        int shape,
+        orc_field const* F,
+        int isB,
+        int const* cell,
+        float const* pos,
+        float* out)
+    {
+        orc::Grid G = toGrid(g);
+        orc::gather(G, shape, toF(F), isB ? orc::kPosB : orc::kPosE, cell, pos, out);
+    }
+
+    void orc_yee_b_half(orc_grid const* g, orc_field const* E, orc_field* B)
+    {
+        auto Bf = toF(B);
+        orc::yeeBHalf(toGrid(g), toF(E), Bf);
+    }
+
+    void orc_yee_e(orc_grid const* g, orc_field const* B, orc_field* E)
+    {
+        auto Ef = toF(E);
+        orc::yeeE(toGrid(g), toF(B), Ef);
+    }
+
+    void orc_add_current(orc_grid const* g, orc_field const* J, orc_field* E)
+    {
+        auto Ef = toF(E);
+        orc::addCurrent(toGrid(g), toF(J), Ef);
+    }
+
+    void orc_push(orc_grid const* g, orc_species const* s, orc_particles* p, orc_field const* E, orc_field const* B)
+    {
+        auto P = toP(p);
+        orc::push(toGrid(g), toSp(s), P, toF(E), toF(B));
+    }
+
+    void orc_deposit(orc_grid const* g, orc_species const* s, orc_particles const* p, orc_field* J, int nthreads)
+    {
+        auto Jf = toF(J);
+        orc::depositThreaded(toGrid(g), toSp(s), toP(p), Jf, nthreads);
+    }
+
+    // Single-particle Esirkepov deposit at a given global cell / in-cell position / velocity.
+    void orc_esirkepov_one(
+        orc_grid const* g,
+        int shape,
+        int const* cell,
+        float const* pos,
+        float const* vel,
+        float charge,
+        orc_field* J)
+    {
+        orc::Grid G = toGrid(g);
+        auto Jf = toF(J);
+        orc::JAccess<float> acc{&G, &Jf};
+        orc::esirkepov(G, shape, cell, pos, vel, charge, acc);
+    }
+
+    void orc_step(
+        orc_grid const* g,
+        int nspecies,
+        orc_species const* s,
+        orc_particles* p,
+        orc_field* E,
+        orc_field* B,
+        orc_field* J,
+        int depositThreads)
+    {
+        std::vector<orc::SpeciesParam> sp(nspecies);
+        std::vector<orc::Particles<float>> P(nspecies);
+        for(int i = 0; i < nspecies; ++i)
+        {
+            sp[i] = toSp(&s[i]);
+            P[i] = toP(&p[i]);
+        }
+        auto Ef = toF(E), Bf = toF(B), Jf = toF(J);
+        orc::step(toGrid(g), nspecies, sp.data(), P.data(), Ef, Bf, Jf, depositThreads);
+    }
+
+    void orc_charge_density(orc_grid const* g, orc_species const* s, orc_particles const* p, float* rho)
+    {
+        orc::chargeDensity(toGrid(g), toSp(s), toP(p), rho);
+    }
+
+    double orc_charge_residual(orc_grid const* g, orc_field const* E, float const* rho, float* out)
+    {
+        return orc::chargeResidual(toGrid(g), toF(E), rho, out);
+    }
+
+    double orc_kinetic_energy(orc_grid const* g, orc_species const* s, orc_particles const* p)
+    {
+        return orc::kineticEnergy(toGrid(g), toSp(s), toP(p));
+    }
+
+    void orc_field_energy(orc_grid const* g, orc_field const* E, orc_field const* B, double* out)
+    {
+        orc::fieldEnergy(toGrid(g), toF(E), toF(B), out);
+    }
+}
