@@ -1,0 +1,376 @@
+"""Throughput of the PIC cycle in particle-steps/s on GB300 (one JSON line).
+
+Workload (default ``two_stream_256``): 256^3 periodic cells, electrons in two
+slabs along y drifting at +-0.2c along x (u_th = 0.005) over a proton
+background at the same positions, 16 macro particles per cell per species
+(5.4e8 particles), TSC shape, Boris pusher, Esirkepov deposition, Yee solver,
+FP32, omega_p dt = 0.1.  A step is one Simulation::runOneStep over all
+particles.  ``thermal_32`` is the 32^3 CIC electron-proton thermal plasma.
+
+* value: particle-steps/s with everything resident in HBM, timed with CUDA
+  events on the launching stream (max over ranks); the particle arrays
+  (21 GB) are far larger than L2, so no flush is needed between steps.
+* roofline: the fused push kernel; achieved = algorithmic bytes per launch /
+  mean launch time from events recorded around each launch.
+* e2e: the same metric through the C-ABI from pinned host buffers: upload of
+  both species, K steps each followed by the FP64 energy read-back, download
+  of both species.
+* cpu_baseline: the CPU oracle (C++, OpenMP, all host threads) on a bounded
+  sample of the same workload (64^3 cells, same ppc/shape/solvers).
+* --impl reference: that CPU implementation alone, as the reference arm.
+Multi-GPU (torchrun): independent replicas, one per GPU (the path is a
+single periodic box; it has no exchange step to shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "two_stream_256": dict(n=(256, 256, 256), ppc=16, shape="TSC", u_th=0.005, drift=0.2, split=True,
+                           sample_n=(64, 64, 64)),
+    "thermal_32": dict(n=(32, 32, 32), ppc=4, shape="CIC", u_th=0.01, drift=0.0, split=False,
+                       sample_n=(32, 32, 32)),
+    # the two-stream workload on 64^3 cells (8.4e6 particles, 270 MB of particle arrays): profiling case
+    "two_stream_64": dict(n=(64, 64, 64), ppc=16, shape="TSC", u_th=0.005, drift=0.2, split=True,
+                          sample_n=(64, 64, 64)),
+}
+DT = float(np.float32(0.99 / np.sqrt(3.0)))
+MASS_P = 1836.0
+# algorithmic bytes: particle read x,u,w,cell (30 B) + write x,u (24 B); per cell and step the
+# gather reads E,B (24 B), J is written (12 B), the Yee updates read E,B,J (36 B) and write E,B (24 B)
+B_PARTICLE = 54.0
+B_CELL = 96.0
+B_PUSH_CELL = 36.0  # per push launch: E,B tile read + J write
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def density():
+    wp = 0.1 / DT  # omega_p dt = 0.1 with q = m = eps0 = 1
+    return wp * wp
+
+
+def drift_u(beta):
+    return beta / np.sqrt(1.0 - beta * beta) if beta else 0.0
+
+
+# ---------------------------------------------------------------------- CPU sample (oracle)
+def numpy_plasma(n, ppc, u_th, drift, split, mass, seed, pos_seed, sc=(8, 8, 4)):
+    nx, ny, nz = n
+    ncell = nx * ny * nz
+    cells = np.repeat(np.arange(ncell, dtype=np.int64), ppc)
+    cx, cy, cz = cells % nx, (cells // nx) % ny, cells // (nx * ny)
+    nsx, nsy = nx // sc[0], ny // sc[1]
+    scidx = (cx // sc[0]) + nsx * ((cy // sc[1]) + nsy * (cz // sc[2]))
+    lc = (cx % sc[0]) + sc[0] * ((cy % sc[1]) + sc[1] * (cz % sc[2]))
+    pos = np.random.default_rng(pos_seed).random((3, cells.size), dtype=np.float32)
+    rng = np.random.default_rng(seed)
+    u = rng.standard_normal((3, cells.size), dtype=np.float32) * np.float32(u_th)
+    ud = drift_u(drift)
+    if ud:
+        u[0] += np.where(cy < ny // 2, ud, -ud).astype(np.float32) if split else np.float32(ud)
+    w = np.float32(density() / ppc)
+    mom = (u * np.float32(mass * w)).astype(np.float32)
+    return dict(pos=np.ascontiguousarray(pos), mom=np.ascontiguousarray(mom), w=np.full(cells.size, w, np.float32),
+                sc=scidx.astype(np.int32), lcell=lc.astype(np.uint16))
+
+
+def cpu_sample_rate(wl, steps, warmup, budget_s=20.0):
+    """Oracle particle-steps/s on the bounded sample, all host threads."""
+    import oracle
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    n = wl["sample_n"]
+    g = dict(nx=n[0], ny=n[1], nz=n[2], sx=8, sy=8, sz=4, dx=1.0, dy=1.0, dz=1.0, dt=DT, c=1.0, eps0=1.0)
+    shape = {"CIC": 1, "TSC": 2, "PQS": 3}[wl["shape"]]
+    pe = numpy_plasma(n, wl["ppc"], wl["u_th"], wl["drift"], wl["split"], 1.0, 11, 7)
+    pi = numpy_plasma(n, wl["ppc"], wl["u_th"] / np.sqrt(MASS_P), 0.0, False, MASS_P, 12, 7)
+    se = dict(charge=-1.0, mass=1.0, shape=shape, pusher=0, current=1)
+    si = dict(charge=1.0, mass=MASS_P, shape=shape, pusher=0, current=1)
+    shp = (3, n[2], n[1], n[0])
+    E, B, J = (np.zeros(shp, np.float32) for _ in range(3))
+    npart = pe["w"].size + pi["w"].size
+    for _ in range(max(warmup, 1)):
+        oracle.step(g, [se, si], [pe, pi], E, B, J, threads)
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        oracle.step(g, [se, si], [pe, pi], E, B, J, threads)
+        done += 1
+        if time.perf_counter() - t0 > budget_s and done >= 1:
+            break
+    dt = time.perf_counter() - t0
+    sample = (f"{n[0]}x{n[1]}x{n[2]} cells, 2x{wl['ppc']} ppc ({npart} particles), {wl['shape']}, {done} steps "
+              f"of the oracle step (push, Yee, Esirkepov, J add) on {threads} threads")
+    return npart * done / dt, threads, sample
+
+
+# ---------------------------------------------------------------------- clocks
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "100", "-i",
+                 str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = [r.split(", ") for r in out.strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------- GPU arm
+def build_sim(pg, wl, device):
+    g = pg.Grid(*wl["n"], dt=DT, supercell=(8, 8, 4), device=device)
+    sim = pg.Simulation(g)
+    sim.add_species(pg.Species("e", -1.0, 1.0, pusher="Boris", shape=wl["shape"], current="Esirkepov"))
+    sim.add_species(pg.Species("i", 1.0, MASS_P, pusher="Boris", shape=wl["shape"], current="Esirkepov"))
+    return sim
+
+
+def init_plasma(sim, wl):
+    n = density()
+    ud = drift_u(wl["drift"])
+    if wl["split"]:
+        sim.init_plasma("e", wl["ppc"], n, wl["u_th"], drift_lo=(ud, 0, 0), drift_hi=(-ud, 0, 0), split_axis=1,
+                        split_cell=wl["n"][1] // 2, seed=1, position_seed=7)
+    else:
+        sim.init_plasma("e", wl["ppc"], n, wl["u_th"], drift_lo=(ud, 0, 0), seed=1, position_seed=7)
+    sim.init_plasma("i", wl["ppc"], n, wl["u_th"] / np.sqrt(MASS_P), seed=2, position_seed=7)
+
+
+def pinned_like(torch, p):
+    out = {}
+    for k, v in p.items():
+        t = torch.empty(v.shape, dtype=getattr(torch, str(v.dtype)) if str(v.dtype) != "uint16" else torch.int16,
+                        pin_memory=True)
+        a = t.numpy()
+        if str(v.dtype) == "uint16":
+            a = a.view(np.uint16)
+        a[...] = v
+        out[k] = (a, t)
+    return {k: a for k, (a, _) in out.items()}, [t for _, t in out.values()]
+
+
+def run_gpu(args, wl, rank, world, local_rank):
+    import torch
+
+    import picongpu_gb300 as pg
+
+    torch.cuda.set_device(local_rank)
+    stream = torch.cuda.Stream()
+    sim = build_sim(pg, wl, local_rank)
+    sim.set_stream(stream.cuda_stream)
+    init_plasma(sim, wl)
+    npart = sim.particle_count("e") + sim.particle_count("i")
+    ncell = wl["n"][0] * wl["n"][1] * wl["n"][2]
+    for _ in range(args.warmup):
+        sim.step()
+    sim.profile(True)
+    launches0 = sim.launch_count()
+    dist = world > 1
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sim.step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = sim.launch_count() - launches0
+    kt = sim.kernel_times()
+    sim.profile(False)
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local_rank}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * npart * args.steps / (ms / 1e3)
+
+    # roofline of the fused push kernel (dominant kernel)
+    push_ms, push_n = kt["push"]
+    push_bytes = args.steps * (B_PARTICLE * npart + 2 * B_PUSH_CELL * ncell)
+    peak, peak_kind = peaks()
+    achieved = push_bytes / (push_ms / 1e3) / 1e9 if push_ms > 0 else None
+    traffic = push_traffic(npart / 2, ncell)
+    roof = {"kernel": "kPush (gather+Boris+move+Esirkepov+migration, per species)", "bound": "hbm",
+            "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
+            "traffic": traffic, "algorithmic_bytes_per_launch": (B_PARTICLE * npart + 2 * B_PUSH_CELL * ncell) / 2,
+            "mean_launch_ms": push_ms / max(push_n, 1),
+            "step_frac_of_peak": round(value / world * (B_PARTICLE + B_CELL / (2 * wl["ppc"])) / (peak * 1e9), 4),
+            "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]}}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, wl, sim, pg, torch, local_rank, world)
+    sim.close()
+    return dict(value=value, ms=ms, npart=npart, ncell=ncell, roof=roof, clocks=clk, launches=launches, e2e=e2e)
+
+
+def push_traffic(n_per_launch, ncell):
+    """DRAM bytes per push launch from the committed ncu summary (bytes per particle), scaled; else None."""
+    p = os.path.join(ROOT, "profiles", "push_tsc_two_stream.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_particle:"):
+            return float(line.split(":")[1]) * n_per_launch
+    return None
+
+
+def run_e2e(args, wl, sim, pg, torch, local_rank, world):
+    """Same metric through the C-ABI from pinned host memory (upload, K steps + energies, download)."""
+    host = {}
+    keep = []
+    for name in ("e", "i"):
+        p = sim.get_particles(name)
+        host[name], ts = pinned_like(torch, p)
+        keep += ts
+    E0 = sim.get_field("E")
+    B0 = sim.get_field("B")
+    sim2 = build_sim(pg, wl, local_rank)
+    npart = sum(host[n]["w"].size for n in host)
+    h2d = sum(a.nbytes for n in host for a in host[n].values()) + E0.nbytes + B0.nbytes
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim2.set_field("E", E0)
+    sim2.set_field("B", B0)
+    for name in ("e", "i"):
+        sim2.set_particles(name, host[name])
+    for _ in range(args.steps):
+        sim2.step()
+        sim2.energies()
+    d2h = 0
+    for name in ("e", "i"):
+        out = sim2.get_particles(name, out=host[name])
+        d2h += sum(a.nbytes for a in out.values())
+    t1 = time.perf_counter()
+    dt = t1 - t0
+    if world > 1:
+        t = torch.tensor([dt], device=f"cuda:{local_rank}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt = float(t.item())
+    d2h += args.steps * 8 * (2 + 2)
+    sim2.close()
+    del keep
+    return {"value": world * npart * args.steps / dt, "unit": "particle-steps/s",
+            "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
+            "wall_s": round(dt, 4)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="two_stream_256", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    n = wl["n"]
+    config = {"workload": f"{args.workload}: {n[0]}x{n[1]}x{n[2]} cells, 2 species x {wl['ppc']} ppc, "
+                          f"{wl['shape']}, Boris, Esirkepov, Yee, fp32",
+              "cells": list(n), "ppc_per_species": wl["ppc"], "species": ["e (q=-1, m=1)", "i (q=+1, m=1836)"],
+              "shape": wl["shape"], "supercell": [8, 8, 4], "dt": DT, "omega_p_dt": 0.1,
+              "l2": "inputs larger than L2 (particle SoA of both species streamed every step)",
+              "parallelism": f"replicas x{args.gpus}"}
+    metric = "particle-steps/s"
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        val, cores, sample = cpu_sample_rate(wl, args.steps, args.warmup, budget_s=60.0)
+        print(json.dumps({"impl": "reference", "metric": metric, "value": val, "unit": metric, "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                          "cpu_baseline": {"value": val, "unit": metric, "cores": cores, "kind": "port",
+                                           "sample": sample},
+                          "e2e": {"value": val, "unit": metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl", device_id=torch.device(f"cuda:{local_rank}"))
+    r = run_gpu(args, wl, rank, world, local_rank)
+    if rank != 0:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        val, cores, sample = cpu_sample_rate(wl, 10, 1, budget_s=20.0)
+        cpu = {"value": val, "unit": metric, "cores": cores, "kind": "port", "sample": sample}
+    line = {"metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded device init)", "config": config,
+            "particles": r["npart"], "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"],
+            "clocks": r["clocks"], "gpu_launches": r["launches"]}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,268 @@
+/* picgb.h -- C-ABI of the GB300-native PIC cycle (Yee + Boris/gather + Esirkepov
+ * + supercell bookkeeping).
+ *
+ * Plain C types only: opaque handles, pointers and sizes.  Every call returns
+ * an int status (PICGB_OK = 0); no C++ exception crosses this boundary.  The
+ * text of the last error of the calling thread is available from
+ * picgb_last_error().  One host thread drives one simulation handle, which
+ * enqueues all its work on one CUDA stream (the reference's single host
+ * thread over its event-system queues, pmacc/eventSystem/queues/QueueController.hpp:42-81).
+ *
+ * Units are the caller's: the library takes cell sizes, dt, c and eps0 as
+ * given (the reference converts SI to its own units in unitless/simulation.unitless).
+ *
+ * Reference interfaces replaced (paths inside the PIConGPU source tree):
+ *   picgb_create / picgb_destroy        Simulation::init / MappingDesc setup (simulation/control/Simulation.hpp:320-418)
+ *   picgb_add_species                   VectorAllSpecies + speciesDefinition.param flags (param/speciesDefinition.param:49-92)
+ *   picgb_get_buffer / picgb_share      DataConnector::get / share (pmacc/dataManagement/DataConnector.hpp:48-136)
+ *   picgb_step                          Simulation::runOneStep (simulation/control/Simulation.hpp:522-542)
+ *   picgb_stage_*                       the stages inside runOneStep (see each declaration)
+ *   picgb_energies                      EnergyFields / EnergyParticles plugins (plugins/EnergyFields.x.cpp:183-261,
+ *                                       plugins/EnergyParticles.x.cpp:58-160)
+ *   picgb_charge_residual               ChargeConservation plugin (plugins/ChargeConservation.tpp:181-260)
+ */
+#ifndef PICGB_H
+#define PICGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C"
+{
+#endif
+
+#define PICGB_ABI_VERSION 1
+
+    /* ------------------------------------------------------------ status codes */
+    enum picgb_status
+    {
+        PICGB_OK = 0,
+        PICGB_ERR_INVALID = 1, /* bad argument or configuration (e.g. CFL violated, Yee.hpp:57-63) */
+        PICGB_ERR_CUDA = 2, /* a CUDA runtime call failed; see picgb_last_error() */
+        PICGB_ERR_OVERFLOW = 3, /* a supercell ran out of particle slots (the reference traps on heap
+                                   exhaustion, pmacc/particles/memory/boxes/ParticlesBox.hpp:97-122) */
+        PICGB_ERR_NOT_FOUND = 4, /* unknown DataConnector id (DataConnector.hpp:113-114 throws) */
+        PICGB_ERR_DUPLICATE = 5, /* id already registered (DataConnector::share throws) */
+        PICGB_ERR_TIMEOUT = 6, /* a bounded device wait gave up */
+        PICGB_ERR_UNSUPPORTED = 7, /* policy combination without a kernel */
+        PICGB_ERR_LOST = 8 /* particles were dropped: overflow beyond the spill buffer */
+    };
+
+    /* ------------------------------------------------------------ policies
+     * The .param type policies (param/species.param:49-90, param/fieldSolver.param:57)
+     * as run-time enums; each combination maps to a compile-time-specialised kernel. */
+    enum picgb_pusher
+    {
+        PICGB_PUSHER_BORIS = 0, /* particles/pusher/particlePusherBoris.hpp */
+        PICGB_PUSHER_FREE = 1, /* particles/pusher/particlePusherFree.hpp */
+        PICGB_PUSHER_NONE = 2 /* species without the particlePusher<> flag: not pushed (immobile) */
+    };
+    enum picgb_shape
+    {
+        PICGB_SHAPE_NGP = 0, /* oracle only */
+        PICGB_SHAPE_CIC = 1,
+        PICGB_SHAPE_TSC = 2,
+        PICGB_SHAPE_PQS = 3,
+        PICGB_SHAPE_PCS = 4 /* oracle only */
+    };
+    enum picgb_current
+    {
+        PICGB_CURRENT_NONE = 0, /* species without the current<> flag */
+        PICGB_CURRENT_ESIRKEPOV = 1 /* fields/currentDeposition/Esirkepov/Esirkepov.hpp */
+    };
+    enum picgb_field_solver
+    {
+        PICGB_SOLVER_YEE = 0 /* fields/MaxwellSolver/Yee/Yee.def */
+    };
+    enum picgb_supercell
+    {
+        PICGB_SUPERCELL_8x8x4 = 0, /* param/memory.param:51 default */
+        PICGB_SUPERCELL_4x4x4 = 1,
+        PICGB_SUPERCELL_8x8x8 = 2
+    };
+
+    typedef struct picgb_grid_config
+    {
+        int32_t nx, ny, nz; /* cells of the periodic box; multiples of the supercell size */
+        int32_t supercell; /* enum picgb_supercell */
+        float dx, dy, dz; /* cell edge lengths */
+        float dt; /* time step; c^2 dt^2 sum(1/d^2) <= 1 is enforced */
+        float c; /* speed of light */
+        float eps0; /* vacuum permittivity (mu0 = 1/(eps0 c^2)) */
+        int32_t field_solver; /* enum picgb_field_solver */
+        int32_t fuse_deposit; /* 1: deposit J inside the push kernel (default); 0: separate deposit stage */
+        int32_t device; /* CUDA device ordinal */
+    } picgb_grid_config;
+
+    typedef struct picgb_species_config
+    {
+        const char* name; /* DataConnector id, e.g. "e", "i" (FrameType::getName()) */
+        float charge; /* charge of one real particle (chargeRatio * base charge) */
+        float mass; /* mass of one real particle (massRatio * base mass) */
+        int32_t pusher; /* enum picgb_pusher */
+        int32_t shape; /* enum picgb_shape */
+        int32_t current; /* enum picgb_current */
+        uint32_t capacity; /* particle slots per supercell; 0 = 1.25 x the largest initial count */
+        int32_t with_ids; /* keep a per-particle uint32 id through the migration */
+    } picgb_species_config;
+
+    /* Host exchange format of one species: n particles as SoA arrays.
+     * pos = in-cell position in [0,1), mom = macro-weighted momentum, w = weighting,
+     * sc = supercell linear index (x fastest), lcell = cell inside the supercell
+     * (x fastest), id optional (NULL). */
+    typedef struct picgb_particles
+    {
+        uint64_t n;
+        float* pos[3];
+        float* mom[3];
+        float* w;
+        int32_t* sc;
+        uint16_t* lcell;
+        uint32_t* id;
+    } picgb_particles;
+
+    /* Device buffer descriptor handed out by the registry (the DataBox a plugin reads). */
+    enum picgb_buffer_kind
+    {
+        PICGB_BUFFER_FIELD = 0, /* ptr[0..ncomp) = component arrays, dims = cells, guard = 0 (periodic wrap) */
+        PICGB_BUFFER_SPECIES = 1, /* ptr = px,py,pz,ux,uy,uz,w,lcell,id,count; capacity slots per supercell */
+        PICGB_BUFFER_OPAQUE = 2 /* non-array simulation data (e.g. "FieldSolverFDTD") */
+    };
+    typedef struct picgb_buffer_desc
+    {
+        int32_t kind; /* enum picgb_buffer_kind */
+        int32_t ncomp; /* number of valid entries in ptr */
+        void* ptr[10]; /* device pointers */
+        int64_t dims[3]; /* cells (fields) or supercells (species) per axis */
+        int64_t stride[3]; /* element strides of x, y, z */
+        int32_t guard[3]; /* guard cells per side: 0, periodic neighbours by wrap */
+        int32_t elem_bytes; /* bytes per element of ptr[0] */
+        uint32_t capacity; /* species: slots per supercell */
+        int32_t layout; /* 0 = SoA per component, x fastest */
+    } picgb_buffer_desc;
+
+    typedef struct picgb_sim picgb_sim;
+
+    /* ------------------------------------------------------------ lifetime */
+    int picgb_abi_version(void);
+    const char* picgb_last_error(void);
+
+    /* Simulation::init (simulation/control/Simulation.hpp:320-418): fields E, B, J
+     * (FieldE/B/J, names "E","B","J") zeroed and registered; "FieldTmp0" and
+     * "FieldSolverFDTD" registered. */
+    int picgb_create(const picgb_grid_config* cfg, picgb_sim** out);
+    int picgb_destroy(picgb_sim* sim);
+
+    /* CreateSpecies (Simulation.hpp:385-386) with the species' flags
+     * (param/speciesDefinition.param:49-92); registers the species under cfg->name. */
+    int picgb_add_species(picgb_sim* sim, const picgb_species_config* cfg, int32_t* index);
+
+    /* Particle initialisation from host arrays (replaces the InitPipeline of
+     * param/speciesInitialization.param): copies in and sorts into supercells. */
+    int picgb_species_set(picgb_sim* sim, int32_t species, const picgb_particles* host);
+    int picgb_species_count(picgb_sim* sim, int32_t species, uint64_t* n);
+
+    /* Seeded plasma on the device (startPosition::Random + manipulators Temperature/Drift,
+     * particles/startPosition/RandomImpl.hpp, particles/manipulators/unary/Temperature.hpp:61-108):
+     * ppc particles per cell at uniform random in-cell positions, momenta
+     * u = drift + u_th * N(0,1) per component (u = gamma*beta, macro momentum = u m w c),
+     * weighting w = density * cell volume / ppc.  Species given the same
+     * position_seed get identical positions (a quasi-neutral start). */
+    typedef struct picgb_plasma_init
+    {
+        uint32_t ppc;
+        float density;
+        float u_th;
+        float drift_lo[3]; /* mean u where cell[split_axis] < split_cell (everywhere if split_axis < 0) */
+        float drift_hi[3]; /* mean u where cell[split_axis] >= split_cell */
+        int32_t split_axis;
+        int32_t split_cell;
+        uint64_t seed;
+        uint64_t position_seed;
+    } picgb_plasma_init;
+    int picgb_species_init_plasma(picgb_sim* sim, int32_t species, const picgb_plasma_init* init);
+    /* Copies all particles out (supercell order; order inside a supercell is not defined). */
+    int picgb_species_get(picgb_sim* sim, int32_t species, picgb_particles* host);
+
+    /* Whole-field copies (host arrays of nx*ny*nz floats per component, x fastest);
+     * name is "E", "B", "J" or "FieldTmp0" (one component). */
+    int picgb_field_set(picgb_sim* sim, const char* name, const float* const* host);
+    int picgb_field_get(picgb_sim* sim, const char* name, float* const* host);
+
+    /* ------------------------------------------------------------ DataConnector */
+    /* DataConnector::get (DataConnector.hpp:109-114): PICGB_ERR_NOT_FOUND on an unknown id. */
+    int picgb_get_buffer(picgb_sim* sim, const char* name, picgb_buffer_desc* out);
+    /* DataConnector::share: registers caller-owned device data; PICGB_ERR_DUPLICATE on an existing id. */
+    int picgb_share(picgb_sim* sim, const char* name, const picgb_buffer_desc* desc);
+    /* DataConnector::unshare */
+    int picgb_unshare(picgb_sim* sim, const char* name);
+    /* Number of registered ids and the i-th id (for listing). */
+    int picgb_registry_size(picgb_sim* sim, int32_t* n);
+    int picgb_registry_name(picgb_sim* sim, int32_t i, char* buf, size_t len);
+
+    /* ------------------------------------------------------------ the PIC step */
+    /* Simulation::runOneStep (Simulation.hpp:522-542): CurrentReset, ParticlePush (+shift),
+     * update_beforeCurrent, CurrentDeposition, AddCurrent, update_afterCurrent. */
+    int picgb_step(picgb_sim* sim, uint32_t step);
+    /* runs n steps starting at step index `step` */
+    int picgb_run(picgb_sim* sim, uint32_t step, uint32_t n);
+
+    /* Stages (for callers that interleave their own work):
+     * CurrentReset (simulation/stage/CurrentReset.hpp:45-51): J = 0 */
+    int picgb_stage_current_reset(picgb_sim* sim);
+    /* ParticlePush (simulation/stage/ParticlePush.x.cpp:141): gather + push + move of all species
+     * with a pusher, then the supercell migration.  With fuse_deposit the current of species with
+     * current<> is deposited in the same kernel (J complete after this stage). */
+    int picgb_stage_push(picgb_sim* sim, uint32_t step);
+    /* fieldSolver.update_beforeCurrent (FDTD.hpp:69; FDTDBase.hpp:97-121): B half step, E step */
+    int picgb_stage_field_before(picgb_sim* sim, uint32_t step);
+    /* CurrentDeposition (simulation/stage/CurrentDeposition.x.cpp:105); no-op with fuse_deposit */
+    int picgb_stage_deposit(picgb_sim* sim, uint32_t step);
+    /* CurrentInterpolationAndAdditionToEMF (stage/CurrentInterpolationAndAdditionToEMF.hpp:99-148):
+     * E += -(dt/eps0) J, currentInterpolation::None */
+    int picgb_stage_add_current(picgb_sim* sim);
+    /* fieldSolver.update_afterCurrent (FDTD.hpp:95; FDTDBase.hpp:151-183): B half step */
+    int picgb_stage_field_after(picgb_sim* sim, uint32_t step);
+
+    /* ------------------------------------------------------------ diagnostics */
+    /* out[0] = field energy of E, out[1] = of B, out[2 + s] = kinetic energy of species s;
+     * FP64 sums (EnergyFields.x.cpp:211-225, EnergyParticles.x.cpp:58-160, KinEnergy.hpp:43-66).
+     * Synchronises the stream.  len = entries available in out. */
+    int picgb_energies(picgb_sim* sim, double* out, size_t len);
+    /* Charge conservation (ChargeConservation.tpp:181-260): deposits rho of all species with a
+     * current into "FieldTmp0", returns max|eps0 div E - rho| and max|rho|.  Synchronises. */
+    int picgb_charge_residual(picgb_sim* sim, double* max_residual, double* max_rho);
+
+    /* ------------------------------------------------------------ execution control */
+    /* Enqueue on a caller's CUDA stream (cudaStream_t passed as void*); NULL = own stream. */
+    int picgb_set_stream(picgb_sim* sim, void* stream);
+    int picgb_synchronize(picgb_sim* sim);
+    /* Device-side kernel launches issued by this handle since creation (own kernels only). */
+    int picgb_launch_count(picgb_sim* sim, uint64_t* n);
+    /* Status word written by the kernels (bits: 1 overflow, 2 lost, 4 bad cell, 8 timeout); reading
+     * synchronises, reset clears it. */
+    int picgb_device_status(picgb_sim* sim, uint32_t* bits, int32_t reset);
+
+    /* Per-kernel timing with CUDA events recorded around each launch on the launching stream
+     * (the reference's TimeIntervall step timer, pmacc/simulationControl/SimulationHelper.cpp:143-170,
+     * at kernel granularity).  Enabling resets the counters. */
+    enum picgb_kernel_class
+    {
+        PICGB_KERNEL_PUSH = 0, /* fused gather/push/move(/deposit)/migration */
+        PICGB_KERNEL_COMPACT = 1, /* hole compaction after the migration */
+        PICGB_KERNEL_YEE_B = 2, /* B half step */
+        PICGB_KERNEL_YEE_E = 3, /* E step (+ J) */
+        PICGB_KERNEL_DEPOSIT = 4, /* separate deposit (fuse_deposit = 0) */
+        PICGB_KERNEL_ADD_CURRENT = 5, /* separate J add (fuse_deposit = 0) */
+        PICGB_KERNEL_CLASSES = 6
+    };
+    int picgb_profile_enable(picgb_sim* sim, int32_t on);
+    /* Total device milliseconds and launch count of one kernel class; synchronises. */
+    int picgb_profile_read(picgb_sim* sim, int32_t kernel_class, double* total_ms, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PICGB_H */

@@ -1,0 +1,218 @@
+// Yee FDTD field kernels and field diagnostics.
+//
+// Fields are SoA [component][z][y][x] without guard cells; the periodic
+// neighbour is reached by index wrap, which replaces the reference's guard
+// exchange of E and B (MaxwellSolver/FDTD/FDTDBase.hpp:111,168,181).
+#include "picgb_device.cuh"
+#include "picgb_internal.hpp"
+
+namespace picgb
+{
+    constexpr int kFieldBX = 128;
+
+    // B -= curl(E) * 0.5 * dt with forward differences
+    // (FDTDBase.kernel:92-121 UpdateBHalfFunctor, differentiation/ForwardDerivative.hpp:45-63, Curl.hpp:84-89).
+    __global__ void __launch_bounds__(kFieldBX) kYeeBHalf(float const* __restrict__ E, float* __restrict__ B, GridParams g)
+    {
+        int const x = blockIdx.x * blockDim.x + threadIdx.x;
+        int const y = blockIdx.y, z = blockIdx.z;
+        if(x >= g.nx)
+            return;
+        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+        size_t const row = size_t(g.nx) * (size_t(y) + size_t(g.ny) * z);
+        size_t const i = row + x;
+        size_t const ix = row + (x + 1 == g.nx ? 0 : x + 1);
+        size_t const iy = size_t(g.nx) * (size_t(y + 1 == g.ny ? 0 : y + 1) + size_t(g.ny) * z) + x;
+        size_t const iz = size_t(g.nx) * (size_t(y) + size_t(g.ny) * (z + 1 == g.nz ? 0 : z + 1)) + x;
+        float const* Ex = E;
+        float const* Ey = E + nc;
+        float const* Ez = E + 2 * nc;
+        float const ex = __ldg(Ex + i), ey = __ldg(Ey + i), ez = __ldg(Ez + i);
+        float const dFdx_y = fdv(fs(__ldg(Ey + ix), ey), g.dx);
+        float const dFdx_z = fdv(fs(__ldg(Ez + ix), ez), g.dx);
+        float const dFdy_x = fdv(fs(__ldg(Ex + iy), ex), g.dy);
+        float const dFdy_z = fdv(fs(__ldg(Ez + iy), ez), g.dy);
+        float const dFdz_x = fdv(fs(__ldg(Ex + iz), ex), g.dz);
+        float const dFdz_y = fdv(fs(__ldg(Ey + iz), ey), g.dz);
+        float const c0 = fs(dFdy_z, dFdz_y), c1 = fs(dFdz_x, dFdx_z), c2 = fs(dFdx_y, dFdy_x);
+        B[i] = fs(B[i], fm(fm(c0, 0.5f), g.dt));
+        B[nc + i] = fs(B[nc + i], fm(fm(c1, 0.5f), g.dt));
+        B[2 * nc + i] = fs(B[2 * nc + i], fm(fm(c2, 0.5f), g.dt));
+    }
+
+    // E += curl(B) * c^2 * dt with backward differences (FDTDBase.kernel:51-81 UpdateEFunctor,
+    // BackwardDerivative.hpp:45-63); optionally followed by E += coeff * J
+    // (currentInterpolation/None.hpp:60-65) as a separate rounding step.
+    __global__ void __launch_bounds__(kFieldBX)
+        kYeeE(float const* __restrict__ B, float* __restrict__ E, float const* __restrict__ J, float coeff, GridParams g)
+    {
+        int const x = blockIdx.x * blockDim.x + threadIdx.x;
+        int const y = blockIdx.y, z = blockIdx.z;
+        if(x >= g.nx)
+            return;
+        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+        size_t const row = size_t(g.nx) * (size_t(y) + size_t(g.ny) * z);
+        size_t const i = row + x;
+        size_t const ix = row + (x == 0 ? g.nx - 1 : x - 1);
+        size_t const iy = size_t(g.nx) * (size_t(y == 0 ? g.ny - 1 : y - 1) + size_t(g.ny) * z) + x;
+        size_t const iz = size_t(g.nx) * (size_t(y) + size_t(g.ny) * (z == 0 ? g.nz - 1 : z - 1)) + x;
+        float const* Bx = B;
+        float const* By = B + nc;
+        float const* Bz = B + 2 * nc;
+        float const bx = __ldg(Bx + i), by = __ldg(By + i), bz = __ldg(Bz + i);
+        float const dFdx_y = fdv(fs(by, __ldg(By + ix)), g.dx);
+        float const dFdx_z = fdv(fs(bz, __ldg(Bz + ix)), g.dx);
+        float const dFdy_x = fdv(fs(bx, __ldg(Bx + iy)), g.dy);
+        float const dFdy_z = fdv(fs(bz, __ldg(Bz + iy)), g.dy);
+        float const dFdz_x = fdv(fs(bx, __ldg(Bx + iz)), g.dz);
+        float const dFdz_y = fdv(fs(by, __ldg(By + iz)), g.dz);
+        float const c2 = fm(g.c, g.c);
+        float const cu[3] = {fs(dFdy_z, dFdz_y), fs(dFdz_x, dFdx_z), fs(dFdx_y, dFdy_x)};
+#pragma unroll
+        for(int d = 0; d < 3; ++d)
+        {
+            size_t const k = d * nc + i;
+            float e = fa(E[k], fm(fm(cu[d], c2), g.dt));
+            if(J)
+                e = fa(e, fm(coeff, __ldg(J + k)));
+            E[k] = e;
+        }
+    }
+
+    __global__ void kAddCurrent(float* __restrict__ E, float const* __restrict__ J, float coeff, size_t n)
+    {
+        for(size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+            E[i] = fa(E[i], fm(coeff, J[i]));
+    }
+
+    cudaError_t launchYeeBHalf(float const* E, float* B, GridParams const& g, cudaStream_t stream)
+    {
+        dim3 grid((g.nx + kFieldBX - 1) / kFieldBX, g.ny, g.nz);
+        kYeeBHalf<<<grid, kFieldBX, 0, stream>>>(E, B, g);
+        return cudaGetLastError();
+    }
+
+    cudaError_t launchYeeE(float const* B, float* E, float const* J, float coeff, GridParams const& g, cudaStream_t stream)
+    {
+        dim3 grid((g.nx + kFieldBX - 1) / kFieldBX, g.ny, g.nz);
+        kYeeE<<<grid, kFieldBX, 0, stream>>>(B, E, J, coeff, g);
+        return cudaGetLastError();
+    }
+
+    cudaError_t launchAddCurrent(float* E, float const* J, float coeff, size_t ncell, cudaStream_t stream)
+    {
+        size_t const n = 3 * ncell;
+        int const blocks = int(std::min<size_t>((n + 255) / 256, 152 * 32));
+        kAddCurrent<<<blocks, 256, 0, stream>>>(E, J, coeff, n);
+        return cudaGetLastError();
+    }
+
+    // ------------------------------------------------------------ diagnostics
+    __device__ __forceinline__ double warpSumD(double v)
+    {
+#pragma unroll
+        for(int o = 16; o > 0; o >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, o);
+        return v;
+    }
+
+    // sum over cells of F_c^2 (square in float, cast to FP64, summed in FP64:
+    // plugins/EnergyFields.x.cpp:240-261 squareComponentWise + cast64Bit)
+    __global__ void kFieldEnergy(float const* __restrict__ F, size_t nc, double* out3)
+    {
+        __shared__ double ws[3][32];
+        double acc[3] = {0.0, 0.0, 0.0};
+        for(size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < nc; i += size_t(gridDim.x) * blockDim.x)
+        {
+#pragma unroll
+            for(int d = 0; d < 3; ++d)
+            {
+                float const v = F[d * nc + i];
+                acc[d] += double(fm(v, v));
+            }
+        }
+        int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for(int d = 0; d < 3; ++d)
+        {
+            double const s = warpSumD(acc[d]);
+            if(lane == 0)
+                ws[d][warp] = s;
+        }
+        __syncthreads();
+        if(warp == 0)
+        {
+#pragma unroll
+            for(int d = 0; d < 3; ++d)
+            {
+                double v = lane < int(blockDim.x >> 5) ? ws[d][lane] : 0.0;
+                v = warpSumD(v);
+                if(lane == 0 && v != 0.0)
+                    atomicAdd(out3 + d, v);
+            }
+        }
+    }
+
+    cudaError_t launchFieldEnergy(float const* F, size_t ncell, double* out3, cudaStream_t stream)
+    {
+        int const blocks = int(std::min<size_t>((ncell + 255) / 256, 152 * 8));
+        kFieldEnergy<<<blocks, 256, 0, stream>>>(F, ncell, out3);
+        return cudaGetLastError();
+    }
+
+    // |eps0 * div E - rho| (plugins/ChargeConservation.tpp:121-135, 211-240) and its max;
+    // max|rho| alongside.  Non-negative floats order like their bit patterns.
+    __global__ void kChargeResidual(
+        float const* __restrict__ E,
+        float const* __restrict__ rho,
+        GridParams g,
+        float* __restrict__ out,
+        unsigned* maxBits,
+        unsigned* maxRhoBits)
+    {
+        int const x = blockIdx.x * blockDim.x + threadIdx.x;
+        int const y = blockIdx.y, z = blockIdx.z;
+        float r = 0.0f, ar = 0.0f;
+        if(x < g.nx)
+        {
+            size_t const nc = size_t(g.nx) * g.ny * g.nz;
+            size_t const row = size_t(g.nx) * (size_t(y) + size_t(g.ny) * z);
+            size_t const i = row + x;
+            size_t const ix = row + (x == 0 ? g.nx - 1 : x - 1);
+            size_t const iy = size_t(g.nx) * (size_t(y == 0 ? g.ny - 1 : y - 1) + size_t(g.ny) * z) + x;
+            size_t const iz = size_t(g.nx) * (size_t(y) + size_t(g.ny) * (z == 0 ? g.nz - 1 : z - 1)) + x;
+            float const rw = fdv(1.0f, g.dx), rh = fdv(1.0f, g.dy), rd = fdv(1.0f, g.dz);
+            float const div = fa(fa(fm(fs(E[i], E[ix]), rw), fm(fs(E[nc + i], E[nc + iy]), rh)),
+                                 fm(fs(E[2 * nc + i], E[2 * nc + iz]), rd));
+            r = fabsf(fs(fm(div, g.eps0), rho[i]));
+            ar = fabsf(rho[i]);
+            if(out)
+                out[i] = r;
+        }
+#pragma unroll
+        for(int o = 16; o > 0; o >>= 1)
+        {
+            r = fmaxf(r, __shfl_down_sync(0xffffffffu, r, o));
+            ar = fmaxf(ar, __shfl_down_sync(0xffffffffu, ar, o));
+        }
+        if((threadIdx.x & 31) == 0)
+        {
+            atomicMax(maxBits, __float_as_uint(r));
+            atomicMax(maxRhoBits, __float_as_uint(ar));
+        }
+    }
+
+    cudaError_t launchChargeResidual(
+        float const* E,
+        float const* rho,
+        GridParams const& g,
+        float* out,
+        unsigned* maxBits,
+        unsigned* maxRhoBits,
+        cudaStream_t stream)
+    {
+        dim3 grid((g.nx + kFieldBX - 1) / kFieldBX, g.ny, g.nz);
+        kChargeResidual<<<grid, kFieldBX, 0, stream>>>(E, rho, g, out, maxBits, maxRhoBits);
+        return cudaGetLastError();
+    }
+} // namespace picgb

@@ -1,0 +1,503 @@
+// Particle bookkeeping kernels: shape dispatch of the push/deposit launchers,
+// hole compaction after the migration (the reference's KernelFillGaps,
+// pmacc/particles/ParticlesBase.kernel:183-359), upload scatter into the
+// supercell layout, download gather, and the FP64 kinetic-energy reduction
+// (plugins/EnergyParticles.x.cpp:58-160).
+#include "picgb_device.cuh"
+#include "picgb_internal.hpp"
+
+namespace picgb
+{
+#define PICGB_DECL_SHAPE(NAME)                                                                                        \
+    cudaError_t launchPush##NAME(                                                                                     \
+        int,                                                                                                          \
+        SpeciesDev const&,                                                                                            \
+        float const*,                                                                                                 \
+        float const*,                                                                                                 \
+        float*,                                                                                                       \
+        GridParams const&,                                                                                            \
+        PushParams const&,                                                                                            \
+        unsigned*,                                                                                                    \
+        cudaStream_t);                                                                                                \
+    cudaError_t launchDeposit##NAME(                                                                                  \
+        int,                                                                                                          \
+        SpeciesDev const&,                                                                                            \
+        float*,                                                                                                       \
+        GridParams const&,                                                                                            \
+        PushParams const&,                                                                                            \
+        unsigned*,                                                                                                    \
+        cudaStream_t);                                                                                                \
+    cudaError_t launchChargeDensity##NAME(int, SpeciesDev const&, float*, GridParams const&, float, float, cudaStream_t);
+    PICGB_DECL_SHAPE(CIC)
+    PICGB_DECL_SHAPE(TSC)
+    PICGB_DECL_SHAPE(PQS)
+
+    cudaError_t launchPush(
+        int shape,
+        int scId,
+        SpeciesDev const& sp,
+        float const* E,
+        float const* B,
+        float* J,
+        GridParams const& g,
+        PushParams const& pp,
+        unsigned* status,
+        cudaStream_t stream)
+    {
+        switch(shape)
+        {
+        case 1:
+            return launchPushCIC(scId, sp, E, B, J, g, pp, status, stream);
+        case 2:
+            return launchPushTSC(scId, sp, E, B, J, g, pp, status, stream);
+        case 3:
+            return launchPushPQS(scId, sp, E, B, J, g, pp, status, stream);
+        }
+        return cudaErrorInvalidValue;
+    }
+
+    cudaError_t launchDeposit(
+        int shape,
+        int scId,
+        SpeciesDev const& sp,
+        float* J,
+        GridParams const& g,
+        PushParams const& pp,
+        unsigned* status,
+        cudaStream_t stream)
+    {
+        switch(shape)
+        {
+        case 1:
+            return launchDepositCIC(scId, sp, J, g, pp, status, stream);
+        case 2:
+            return launchDepositTSC(scId, sp, J, g, pp, status, stream);
+        case 3:
+            return launchDepositPQS(scId, sp, J, g, pp, status, stream);
+        }
+        return cudaErrorInvalidValue;
+    }
+
+    cudaError_t launchChargeDensity(
+        int shape,
+        int scId,
+        SpeciesDev const& sp,
+        float* rho,
+        GridParams const& g,
+        float charge,
+        float cellVolume,
+        cudaStream_t stream)
+    {
+        switch(shape)
+        {
+        case 1:
+            return launchChargeDensityCIC(scId, sp, rho, g, charge, cellVolume, stream);
+        case 2:
+            return launchChargeDensityTSC(scId, sp, rho, g, charge, cellVolume, stream);
+        case 3:
+            return launchChargeDensityPQS(scId, sp, rho, g, charge, cellVolume, stream);
+        }
+        return cudaErrorInvalidValue;
+    }
+
+    // ------------------------------------------------------------ block scan
+    // In-place exclusive scan of n <= 32 * 32 * items entries in shared memory by
+    // one block of blockDim.x (multiple of 32, <= 1024) threads; returns the total.
+    __device__ uint32_t blockExclusiveScan(uint32_t* a, int n, uint32_t* warpSums)
+    {
+        int const T = blockDim.x;
+        int const per = (n + T - 1) / T;
+        int const b = threadIdx.x * per;
+        int const e = min(n, b + per);
+        uint32_t local = 0;
+        for(int i = b; i < e; ++i)
+            local += a[i];
+        // inclusive warp scan of the per-thread totals
+        uint32_t v = local;
+        int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for(int o = 1; o < 32; o <<= 1)
+        {
+            uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+            if(lane >= o)
+                v += t;
+        }
+        if(lane == 31)
+            warpSums[warp] = v;
+        __syncthreads();
+        if(warp == 0)
+        {
+            int const nw = T >> 5;
+            uint32_t s = lane < nw ? warpSums[lane] : 0u;
+#pragma unroll
+            for(int o = 1; o < 32; o <<= 1)
+            {
+                uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
+                if(lane >= o)
+                    s += t;
+            }
+            if(lane < nw)
+                warpSums[lane] = s;
+        }
+        __syncthreads();
+        uint32_t offset = (v - local) + (warp > 0 ? warpSums[warp - 1] : 0u);
+        uint32_t const total = warpSums[(T >> 5) - 1];
+        for(int i = b; i < e; ++i)
+        {
+            uint32_t const x = a[i];
+            a[i] = offset;
+            offset += x;
+        }
+        __syncthreads();
+        return total;
+    }
+
+    __device__ __forceinline__ uint32_t maskBelow(int w, uint32_t limit)
+    {
+        // bits j of word w with 32 * w + j < limit
+        int64_t const r = int64_t(limit) - 32 * int64_t(w);
+        if(r <= 0)
+            return 0u;
+        if(r >= 32)
+            return 0xffffffffu;
+        return (1u << r) - 1u;
+    }
+
+    __device__ __forceinline__ void copyParticle(SpeciesDev const& sp, size_t dst, size_t src)
+    {
+        sp.px[dst] = sp.px[src];
+        sp.py[dst] = sp.py[src];
+        sp.pz[dst] = sp.pz[src];
+        sp.ux[dst] = sp.ux[src];
+        sp.uy[dst] = sp.uy[src];
+        sp.uz[dst] = sp.uz[src];
+        sp.w[dst] = sp.w[src];
+        sp.lcell[dst] = sp.lcell[src];
+        if(sp.id)
+            sp.id[dst] = sp.id[src];
+    }
+
+    // Fill the slots vacated by leaving particles with the last valid particles
+    // of the supercell so that slots [0, count) are dense again.
+    __global__ void __launch_bounds__(256) kCompact(SpeciesDev sp)
+    {
+        extern __shared__ uint32_t csm[];
+        __shared__ uint32_t warpSums[32];
+        int const sc = blockIdx.x;
+        uint32_t const tail = sp.tail[sc];
+        uint32_t const n = tail < sp.cap ? tail : sp.cap;
+        uint32_t const h = sp.nhole[sc];
+        if(h == 0)
+        {
+            if(threadIdx.x == 0)
+            {
+                sp.count[sc] = n;
+                sp.tail[sc] = n;
+            }
+            return;
+        }
+        uint32_t const newc = n - h;
+        int const W = int((n + 31) / 32);
+        uint32_t* bm = csm;
+        uint32_t* dpre = csm + W;
+        uint32_t* spre = csm + 2 * W;
+        for(int i = threadIdx.x; i < W; i += blockDim.x)
+            bm[i] = 0u;
+        __syncthreads();
+        size_t const base = size_t(sc) * sp.cap;
+        for(uint32_t i = threadIdx.x; i < h; i += blockDim.x)
+        {
+            uint32_t const s = sp.holes[base + i];
+            atomicOr(bm + (s >> 5), 1u << (s & 31));
+        }
+        __syncthreads();
+        for(int w = threadIdx.x; w < W; w += blockDim.x)
+        {
+            uint32_t const lo = maskBelow(w, newc);
+            uint32_t const hi = maskBelow(w, n) & ~lo;
+            dpre[w] = __popc(bm[w] & lo);
+            spre[w] = __popc(~bm[w] & hi);
+        }
+        __syncthreads();
+        blockExclusiveScan(dpre, W, warpSums);
+        blockExclusiveScan(spre, W, warpSums);
+        for(int w = threadIdx.x; w < W; w += blockDim.x)
+        {
+            uint32_t m = bm[w] & maskBelow(w, newc);
+            uint32_t r = dpre[w];
+            while(m)
+            {
+                int const b = __ffs(m) - 1;
+                m &= m - 1u;
+                // source word: last ws with spre[ws] <= r
+                int lo = 0, hi = W - 1;
+                while(lo < hi)
+                {
+                    int const mid = (lo + hi + 1) >> 1;
+                    if(spre[mid] <= r)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                int const ws = lo;
+                uint32_t sm = ~bm[ws] & (maskBelow(ws, n) & ~maskBelow(ws, newc));
+                for(uint32_t q = r - spre[ws]; q > 0; --q)
+                    sm &= sm - 1u;
+                int const sb = __ffs(sm) - 1;
+                if(sb < 0)
+                    break; // unreachable for consistent ranks; never index with it
+                copyParticle(sp, base + 32u * w + b, base + 32u * ws + sb);
+                ++r;
+            }
+        }
+        __syncthreads();
+        if(threadIdx.x == 0)
+        {
+            sp.count[sc] = newc;
+            sp.tail[sc] = newc;
+            sp.nhole[sc] = 0u;
+        }
+    }
+
+    cudaError_t launchCompact(SpeciesDev const& sp, int nsc, cudaStream_t stream)
+    {
+        size_t const smem = sizeof(uint32_t) * 3 * ((sp.cap + 31) / 32);
+        if(smem > 48 * 1024)
+        {
+            cudaError_t e = cudaFuncSetAttribute(kCompact, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if(e != cudaSuccess)
+                return e;
+        }
+        kCompact<<<nsc, 256, smem, stream>>>(sp);
+        return cudaGetLastError();
+    }
+
+    // ------------------------------------------------------------ upload
+    // Occupancy per supercell; also validates the input: supercell and cell
+    // indices in range and in-cell positions in [0, 1) (the kernels assume a
+    // particle moves at most one cell per step from a valid in-cell position).
+    __global__ void kHistogram(
+        uint64_t n,
+        int32_t const* __restrict__ sc,
+        uint16_t const* __restrict__ lcell,
+        float const* __restrict__ px,
+        float const* __restrict__ py,
+        float const* __restrict__ pz,
+        uint32_t* count,
+        int nsc,
+        int vol,
+        unsigned* status)
+    {
+        for(uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+        {
+            int const s = sc[i];
+            bool bad = s < 0 || s >= nsc || int(lcell[i]) >= vol;
+            if(px)
+            {
+                float const x = px[i], y = py[i], z = pz[i];
+                bad |= !(x >= 0.0f && x < 1.0f && y >= 0.0f && y < 1.0f && z >= 0.0f && z < 1.0f);
+            }
+            if(bad)
+            {
+                atomicOr(status, ST_BAD_CELL);
+                continue;
+            }
+            atomicAdd(count + s, 1u);
+        }
+    }
+
+    cudaError_t launchHistogram(
+        int scId,
+        uint64_t n,
+        int32_t const* sc,
+        uint16_t const* lcell,
+        float const* const* pos,
+        uint32_t* count,
+        int nsc,
+        unsigned* status,
+        cudaStream_t stream)
+    {
+        int const vol = scId == 0 ? 256 : (scId == 1 ? 64 : 512);
+        if(n == 0)
+            return cudaSuccess;
+        int const blocks = int(std::min<uint64_t>((n + 255) / 256, 152 * 64));
+        float const* px = pos ? pos[0] : nullptr;
+        float const* py = pos ? pos[1] : nullptr;
+        float const* pz = pos ? pos[2] : nullptr;
+        kHistogram<<<blocks, 256, 0, stream>>>(n, sc, lcell, px, py, pz, count, nsc, vol, status);
+        return cudaGetLastError();
+    }
+
+    struct Attr7
+    {
+        float const* a[7];
+    };
+
+    __global__ void kScatter(
+        uint64_t n,
+        Attr7 attr,
+        int32_t const* __restrict__ sc,
+        uint16_t const* __restrict__ lcell,
+        uint32_t const* __restrict__ id,
+        SpeciesDev sp,
+        unsigned* status)
+    {
+        for(uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+        {
+            int const s = sc[i];
+            uint32_t const slot = atomicAdd(sp.count + s, 1u);
+            if(slot >= sp.cap)
+            {
+                atomicOr(status, ST_LOST);
+                continue;
+            }
+            size_t const d = size_t(s) * sp.cap + slot;
+            sp.px[d] = attr.a[0][i];
+            sp.py[d] = attr.a[1][i];
+            sp.pz[d] = attr.a[2][i];
+            sp.ux[d] = attr.a[3][i];
+            sp.uy[d] = attr.a[4][i];
+            sp.uz[d] = attr.a[5][i];
+            sp.w[d] = attr.a[6][i];
+            sp.lcell[d] = lcell[i];
+            if(sp.id)
+                sp.id[d] = id ? id[i] : uint32_t(i);
+        }
+    }
+
+    cudaError_t launchScatter(
+        uint64_t n,
+        float const* const* attr,
+        int32_t const* sc,
+        uint16_t const* lcell,
+        uint32_t const* id,
+        SpeciesDev const& sp,
+        unsigned* status,
+        cudaStream_t stream)
+    {
+        if(n == 0)
+            return cudaSuccess;
+        Attr7 a;
+        for(int i = 0; i < 7; ++i)
+            a.a[i] = attr[i];
+        int const blocks = int(std::min<uint64_t>((n + 255) / 256, 152 * 64));
+        kScatter<<<blocks, 256, 0, stream>>>(n, a, sc, lcell, id, sp, status);
+        return cudaGetLastError();
+    }
+
+    // ------------------------------------------------------------ download
+    struct OutAttr
+    {
+        float* a[7];
+    };
+
+    __global__ void kGatherOut(
+        SpeciesDev sp,
+        uint64_t const* __restrict__ offsets,
+        OutAttr out,
+        int32_t* __restrict__ osc,
+        uint16_t* __restrict__ olc,
+        uint32_t* __restrict__ oid)
+    {
+        int const sc = blockIdx.x;
+        uint32_t const n = sp.count[sc];
+        size_t const base = size_t(sc) * sp.cap;
+        uint64_t const o = offsets[sc];
+        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        {
+            size_t const s = base + k;
+            uint64_t const d = o + k;
+            out.a[0][d] = sp.px[s];
+            out.a[1][d] = sp.py[s];
+            out.a[2][d] = sp.pz[s];
+            out.a[3][d] = sp.ux[s];
+            out.a[4][d] = sp.uy[s];
+            out.a[5][d] = sp.uz[s];
+            out.a[6][d] = sp.w[s];
+            osc[d] = sc;
+            olc[d] = sp.lcell[s];
+            if(oid)
+                oid[d] = sp.id ? sp.id[s] : 0u;
+        }
+    }
+
+    cudaError_t launchGatherOut(
+        SpeciesDev const& sp,
+        int nsc,
+        uint64_t const* offsets,
+        float* const* attr,
+        int32_t* sc,
+        uint16_t* lcell,
+        uint32_t* id,
+        cudaStream_t stream)
+    {
+        OutAttr o;
+        for(int i = 0; i < 7; ++i)
+            o.a[i] = attr[i];
+        kGatherOut<<<nsc, 256, 0, stream>>>(sp, offsets, o, sc, lcell, id);
+        return cudaGetLastError();
+    }
+
+    // ------------------------------------------------------------ energies
+    __device__ __forceinline__ double blockSumD(double v)
+    {
+        __shared__ double ws[32];
+#pragma unroll
+        for(int o = 16; o > 0; o >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, o);
+        int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if(lane == 0)
+            ws[warp] = v;
+        __syncthreads();
+        double r = 0.0;
+        if(warp == 0)
+        {
+            r = lane < int(blockDim.x >> 5) ? ws[lane] : 0.0;
+#pragma unroll
+            for(int o = 16; o > 0; o >>= 1)
+                r += __shfl_down_sync(0xffffffffu, r, o);
+        }
+        __syncthreads();
+        return r;
+    }
+
+    // KinEnergy (algorithms/KinEnergy.hpp:43-66) per macro particle in float,
+    // summed in FP64.
+    __global__ void kKineticEnergy(SpeciesDev sp, float mass0, float c, double* out)
+    {
+        int const sc = blockIdx.x;
+        uint32_t const n = sp.count[sc];
+        size_t const base = size_t(sc) * sp.cap;
+        float const c2 = fm(c, c);
+        double acc = 0.0;
+        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        {
+            size_t const s = base + k;
+            float const m = fm(mass0, sp.w[s]);
+            float const ux = sp.ux[s], uy = sp.uy[s], uz = sp.uz[s];
+            float const mom2 = l2n2(ux, uy, uz);
+            float e;
+            if(m == 0.0f)
+                e = fm(c, fsq(mom2));
+            else
+            {
+                float const r = fdv(1.0f, fm(fm(m, m), c2));
+                float const gamma = fsq(fa(1.0f, fm(mom2, r)));
+                if(gamma < 1.005f)
+                    e = fdv(mom2, fm(2.0f, m));
+                else
+                    e = fm(fm(fs(gamma, 1.0f), m), c2);
+            }
+            acc += double(e);
+        }
+        double const s = blockSumD(acc);
+        if(threadIdx.x == 0 && s != 0.0)
+            atomicAdd(out, s);
+    }
+
+    cudaError_t launchKineticEnergy(SpeciesDev const& sp, int nsc, float mass, float c, double* out, cudaStream_t stream)
+    {
+        kKineticEnergy<<<nsc, 256, 0, stream>>>(sp, mass, c, out);
+        return cudaGetLastError();
+    }
+} // namespace picgb

@@ -1,0 +1,1177 @@
+// Host runtime behind the C-ABI of include/picgb.h: the simulation handle,
+// the DataConnector-style registry, species upload/download, the stage
+// sequence of one PIC step and the diagnostics.
+#include "picgb.h"
+#include "picgb_device.cuh"
+#include "picgb_init.hpp"
+#include "picgb_internal.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+using namespace picgb;
+
+namespace
+{
+    thread_local std::string g_lastError;
+
+    int fail(int code, char const* fmt, ...)
+    {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        std::vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        g_lastError = buf;
+        return code;
+    }
+
+#define CUDA_TRY(expr)                                                                                                \
+    do                                                                                                                \
+    {                                                                                                                 \
+        cudaError_t e_ = (expr);                                                                                      \
+        if(e_ != cudaSuccess)                                                                                         \
+            return fail(PICGB_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__);   \
+    } while(0)
+
+    template<typename T>
+    cudaError_t dalloc(T*& p, size_t n)
+    {
+        p = nullptr;
+        if(n == 0)
+            return cudaSuccess;
+        return cudaMalloc(reinterpret_cast<void**>(&p), n * sizeof(T));
+    }
+
+    template<typename T>
+    void dfree(T*& p)
+    {
+        if(p)
+            cudaFree(p);
+        p = nullptr;
+    }
+
+    int scSize(int id, int* s)
+    {
+        static int const tab[3][3] = {{8, 8, 4}, {4, 4, 4}, {8, 8, 8}};
+        if(id < 0 || id > 2)
+            return 0;
+        s[0] = tab[id][0];
+        s[1] = tab[id][1];
+        s[2] = tab[id][2];
+        return 1;
+    }
+
+    struct Species
+    {
+        std::string name;
+        picgb_species_config cfg{};
+        SpeciesDev dev{};
+        int nsc = 0;
+        bool allocated = false;
+
+        void freeAll()
+        {
+            dfree(dev.px);
+            dfree(dev.py);
+            dfree(dev.pz);
+            dfree(dev.ux);
+            dfree(dev.uy);
+            dfree(dev.uz);
+            dfree(dev.w);
+            dfree(dev.lcell);
+            dfree(dev.id);
+            dfree(dev.count);
+            dfree(dev.tail);
+            dfree(dev.nhole);
+            dfree(dev.holes);
+            dfree(dev.sp_attr);
+            dfree(dev.sp_sc);
+            dfree(dev.sp_lcell);
+            dfree(dev.sp_id);
+            dfree(dev.sp_count);
+            allocated = false;
+        }
+    };
+
+    // Registry entry (pmacc/dataManagement/DataConnector.hpp:48-136): either an
+    // internal buffer (field or species, resolved at lookup so relayouts are
+    // seen) or caller-shared device data.
+    struct Entry
+    {
+        enum Kind
+        {
+            FieldE,
+            FieldB,
+            FieldJ,
+            FieldTmp,
+            SpeciesBuf,
+            Opaque,
+            External
+        } kind;
+        int index = 0;
+        picgb_buffer_desc desc{};
+    };
+} // namespace
+
+struct picgb_sim
+{
+    picgb_grid_config cfg{};
+    GridParams g{};
+    int sc[3] = {8, 8, 4};
+    int nsc = 0;
+    size_t ncell = 0;
+    float* E = nullptr;
+    float* B = nullptr;
+    float* J = nullptr;
+    float* rho = nullptr;
+    unsigned* status = nullptr; // device status word
+    unsigned* hostStatus = nullptr; // pinned
+    double* energy = nullptr; // device accumulators
+    unsigned* maxBits = nullptr; // device: residual max, rho max
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    uint64_t launches = 0;
+    std::vector<std::unique_ptr<Species>> species;
+    std::map<std::string, Entry> registry;
+    // per-kernel event timing (picgb_profile_enable)
+    bool prof = false;
+    struct Pending
+    {
+        int cls;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> eventPool;
+    double profMs[PICGB_KERNEL_CLASSES] = {};
+    uint64_t profN[PICGB_KERNEL_CLASSES] = {};
+
+    float coeffJ() const { return -(1.0f / cfg.eps0) * cfg.dt; } // FDTD.hpp:84
+    float cellVolume() const
+    {
+        float v = cfg.dx * cfg.dy;
+        v = v * cfg.dz;
+        return v;
+    }
+    PushParams pushParams(Species const& s, bool deposit) const
+    {
+        PushParams p{};
+        p.charge = s.cfg.charge;
+        p.mass = s.cfg.mass;
+        p.dt = cfg.dt;
+        p.c2 = cfg.c * cfg.c;
+        p.rc2 = 1.0f / (cfg.c * cfg.c);
+        float const vdt = cellVolume() * cfg.dt;
+        p.invVdt = 1.0f / vdt;
+        p.pusher = s.cfg.pusher;
+        p.deposit = deposit ? 1 : 0;
+        return p;
+    }
+};
+
+namespace
+{
+    int checkSim(picgb_sim* s)
+    {
+        if(!s)
+            return fail(PICGB_ERR_INVALID, "null simulation handle");
+        return PICGB_OK;
+    }
+
+    int checkSpecies(picgb_sim* s, int32_t i)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(i < 0 || i >= int32_t(s->species.size()))
+            return fail(PICGB_ERR_INVALID, "species index %d out of range", int(i));
+        return PICGB_OK;
+    }
+
+    cudaError_t takeEvent(picgb_sim* s, cudaEvent_t* e)
+    {
+        if(!s->eventPool.empty())
+        {
+            *e = s->eventPool.back();
+            s->eventPool.pop_back();
+            return cudaSuccess;
+        }
+        return cudaEventCreate(e);
+    }
+
+    // Launch one kernel through `launch`, bracketed by events when profiling is on.
+    template<typename F>
+    cudaError_t timedLaunch(picgb_sim* s, int cls, F&& launch)
+    {
+        ++s->launches;
+        if(!s->prof)
+            return launch();
+        picgb_sim::Pending p{cls, nullptr, nullptr};
+        cudaError_t e = takeEvent(s, &p.a);
+        if(e == cudaSuccess)
+            e = takeEvent(s, &p.b);
+        if(e == cudaSuccess)
+            e = cudaEventRecord(p.a, s->stream);
+        if(e != cudaSuccess)
+            return e;
+        e = launch();
+        if(e != cudaSuccess)
+            return e;
+        e = cudaEventRecord(p.b, s->stream);
+        s->pending.push_back(p);
+        return e;
+    }
+
+    // Accumulate the completed event pairs (call after a stream synchronisation).
+    cudaError_t profFlush(picgb_sim* s)
+    {
+        for(auto& p : s->pending)
+        {
+            float ms = 0.0f;
+            cudaError_t e = cudaEventElapsedTime(&ms, p.a, p.b);
+            if(e != cudaSuccess)
+                return e;
+            s->profMs[p.cls] += ms;
+            s->profN[p.cls] += 1;
+            s->eventPool.push_back(p.a);
+            s->eventPool.push_back(p.b);
+        }
+        s->pending.clear();
+        return cudaSuccess;
+    }
+
+    void fieldDesc(picgb_sim const* s, float* base, int ncomp, picgb_buffer_desc* d)
+    {
+        std::memset(d, 0, sizeof(*d));
+        d->kind = PICGB_BUFFER_FIELD;
+        d->ncomp = ncomp;
+        for(int c = 0; c < ncomp; ++c)
+            d->ptr[c] = base + c * s->ncell;
+        d->dims[0] = s->cfg.nx;
+        d->dims[1] = s->cfg.ny;
+        d->dims[2] = s->cfg.nz;
+        d->stride[0] = 1;
+        d->stride[1] = s->cfg.nx;
+        d->stride[2] = int64_t(s->cfg.nx) * s->cfg.ny;
+        d->elem_bytes = 4;
+        d->layout = 0;
+    }
+
+    void speciesDesc(picgb_sim const* s, Species const& sp, picgb_buffer_desc* d)
+    {
+        std::memset(d, 0, sizeof(*d));
+        d->kind = PICGB_BUFFER_SPECIES;
+        d->ncomp = 10;
+        void* p[10] = {sp.dev.px, sp.dev.py, sp.dev.pz, sp.dev.ux, sp.dev.uy, sp.dev.uz, sp.dev.w, sp.dev.lcell,
+                       sp.dev.id, sp.dev.count};
+        for(int i = 0; i < 10; ++i)
+            d->ptr[i] = p[i];
+        d->dims[0] = s->g.nscx;
+        d->dims[1] = s->g.nscy;
+        d->dims[2] = s->g.nscz;
+        d->stride[0] = 1;
+        d->stride[1] = s->g.nscx;
+        d->stride[2] = int64_t(s->g.nscx) * s->g.nscy;
+        d->elem_bytes = 4;
+        d->capacity = sp.dev.cap;
+        d->layout = 0;
+    }
+
+    int addEntry(picgb_sim* s, std::string const& name, Entry e)
+    {
+        if(s->registry.count(name))
+            return fail(PICGB_ERR_DUPLICATE, "DataConnector: id '%s' is already registered", name.c_str());
+        s->registry.emplace(name, e);
+        return PICGB_OK;
+    }
+
+    // Allocate the supercell-major storage of a species with `cap` slots per supercell.
+    int allocSpecies(picgb_sim* s, Species& sp, uint32_t cap)
+    {
+        sp.freeAll();
+        size_t const n = size_t(s->nsc) * cap;
+        SpeciesDev& d = sp.dev;
+        d.cap = cap;
+        CUDA_TRY(dalloc(d.px, n));
+        CUDA_TRY(dalloc(d.py, n));
+        CUDA_TRY(dalloc(d.pz, n));
+        CUDA_TRY(dalloc(d.ux, n));
+        CUDA_TRY(dalloc(d.uy, n));
+        CUDA_TRY(dalloc(d.uz, n));
+        CUDA_TRY(dalloc(d.w, n));
+        CUDA_TRY(dalloc(d.lcell, n));
+        if(sp.cfg.with_ids)
+            CUDA_TRY(dalloc(d.id, n));
+        CUDA_TRY(dalloc(d.count, size_t(s->nsc)));
+        CUDA_TRY(dalloc(d.tail, size_t(s->nsc)));
+        CUDA_TRY(dalloc(d.nhole, size_t(s->nsc)));
+        CUDA_TRY(dalloc(d.holes, n));
+        // spill buffer: 1/64 of the slots, at least 4096
+        d.spill_cap = uint32_t(std::max<size_t>(4096, n / 64));
+        CUDA_TRY(dalloc(d.sp_attr, size_t(7) * d.spill_cap));
+        CUDA_TRY(dalloc(d.sp_sc, size_t(d.spill_cap)));
+        CUDA_TRY(dalloc(d.sp_lcell, size_t(d.spill_cap)));
+        CUDA_TRY(dalloc(d.sp_id, size_t(d.spill_cap)));
+        CUDA_TRY(dalloc(d.sp_count, 1));
+        CUDA_TRY(cudaMemsetAsync(d.count, 0, sizeof(uint32_t) * s->nsc, s->stream));
+        CUDA_TRY(cudaMemsetAsync(d.tail, 0, sizeof(uint32_t) * s->nsc, s->stream));
+        CUDA_TRY(cudaMemsetAsync(d.nhole, 0, sizeof(uint32_t) * s->nsc, s->stream));
+        CUDA_TRY(cudaMemsetAsync(d.sp_count, 0, sizeof(uint32_t), s->stream));
+        sp.nsc = s->nsc;
+        sp.allocated = true;
+        return PICGB_OK;
+    }
+
+    // Contiguous device copy of particles in the host exchange format.
+    struct Staging
+    {
+        float* a[7] = {};
+        int32_t* sc = nullptr;
+        uint16_t* lcell = nullptr;
+        uint32_t* id = nullptr;
+        uint64_t n = 0;
+
+        cudaError_t alloc(uint64_t count, bool ids)
+        {
+            n = count;
+            for(auto& p : a)
+                if(cudaError_t e = dalloc(p, count))
+                    return e;
+            if(cudaError_t e = dalloc(sc, count))
+                return e;
+            if(cudaError_t e = dalloc(lcell, count))
+                return e;
+            if(ids)
+                if(cudaError_t e = dalloc(id, count))
+                    return e;
+            return cudaSuccess;
+        }
+        ~Staging()
+        {
+            for(auto& p : a)
+                dfree(p);
+            dfree(sc);
+            dfree(lcell);
+            dfree(id);
+        }
+    };
+
+    int readStatus(picgb_sim* s, unsigned* bits, bool reset)
+    {
+        CUDA_TRY(cudaMemcpyAsync(s->hostStatus, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        *bits = *s->hostStatus;
+        if(reset && *bits)
+            CUDA_TRY(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->stream));
+        return PICGB_OK;
+    }
+
+    // Grow the per-supercell capacity and re-insert the particles parked in the
+    // spill buffer (the reference would abort on an exhausted frame heap).
+    int relayout(picgb_sim* s, Species& sp, double growth)
+    {
+        std::vector<uint32_t> cnt(s->nsc);
+        uint32_t spill = 0;
+        CUDA_TRY(cudaMemcpyAsync(cnt.data(), sp.dev.count, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(&spill, sp.dev.sp_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        spill = std::min(spill, sp.dev.spill_cap);
+        std::vector<uint64_t> off(s->nsc);
+        uint64_t total = 0;
+        for(int i = 0; i < s->nsc; ++i)
+        {
+            off[i] = total;
+            total += cnt[i];
+        }
+        Staging st;
+        CUDA_TRY(st.alloc(total + spill, sp.cfg.with_ids != 0));
+        uint64_t* doff = nullptr;
+        CUDA_TRY(dalloc(doff, size_t(s->nsc)));
+        CUDA_TRY(cudaMemcpyAsync(doff, off.data(), sizeof(uint64_t) * s->nsc, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, st.a, st.sc, st.lcell, st.id, s->stream));
+        ++s->launches;
+        size_t const C = sp.dev.spill_cap;
+        for(int k = 0; k < 7; ++k)
+            CUDA_TRY(cudaMemcpyAsync(
+                st.a[k] + total,
+                sp.dev.sp_attr + k * C,
+                sizeof(float) * spill,
+                cudaMemcpyDeviceToDevice,
+                s->stream));
+        CUDA_TRY(cudaMemcpyAsync(st.sc + total, sp.dev.sp_sc, sizeof(int32_t) * spill, cudaMemcpyDeviceToDevice, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(
+            st.lcell + total,
+            sp.dev.sp_lcell,
+            sizeof(uint16_t) * spill,
+            cudaMemcpyDeviceToDevice,
+            s->stream));
+        if(st.id)
+            CUDA_TRY(
+                cudaMemcpyAsync(st.id + total, sp.dev.sp_id, sizeof(uint32_t) * spill, cudaMemcpyDeviceToDevice, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        dfree(doff);
+        // histogram of the new occupancy
+        uint32_t* hcount = nullptr;
+        CUDA_TRY(dalloc(hcount, size_t(s->nsc)));
+        CUDA_TRY(cudaMemsetAsync(hcount, 0, sizeof(uint32_t) * s->nsc, s->stream));
+        CUDA_TRY(launchHistogram(
+            s->cfg.supercell,
+            total + spill,
+            st.sc,
+            st.lcell,
+            nullptr,
+            hcount,
+            s->nsc,
+            s->status,
+            s->stream));
+        ++s->launches;
+        CUDA_TRY(cudaMemcpyAsync(cnt.data(), hcount, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        dfree(hcount);
+        uint32_t mx = *std::max_element(cnt.begin(), cnt.end());
+        uint64_t want = std::max<uint64_t>(uint64_t(std::ceil(mx * growth)), sp.dev.cap + 32);
+        want = (want + 31) / 32 * 32;
+        if(want > 65504)
+            return fail(PICGB_ERR_OVERFLOW, "species '%s': %u particles in one supercell exceed the slot limit",
+                        sp.name.c_str(), mx);
+        if(int r = allocSpecies(s, sp, uint32_t(want)))
+            return r;
+        float const* attr[7] = {st.a[0], st.a[1], st.a[2], st.a[3], st.a[4], st.a[5], st.a[6]};
+        CUDA_TRY(launchScatter(total + spill, attr, st.sc, st.lcell, st.id, sp.dev, s->status, s->stream));
+        ++s->launches;
+        CUDA_TRY(cudaMemcpyAsync(sp.dev.tail, sp.dev.count, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToDevice, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return PICGB_OK;
+    }
+
+    // After a step: a set overflow bit means arrivals were parked in the spill
+    // buffer; they are re-inserted with a larger capacity before anything else runs.
+    int afterStep(picgb_sim* s)
+    {
+        unsigned bits = 0;
+        if(int r = readStatus(s, &bits, false))
+            return r;
+        CUDA_TRY(profFlush(s));
+        if(bits & ST_LOST)
+            return fail(PICGB_ERR_LOST, "particles were lost: the spill buffer overflowed");
+        if(bits & ST_OVERFLOW)
+        {
+            for(auto& sp : s->species)
+            {
+                uint32_t spill = 0;
+                CUDA_TRY(cudaMemcpy(&spill, sp->dev.sp_count, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+                if(spill)
+                    if(int r = relayout(s, *sp, 1.25))
+                        return r;
+            }
+            CUDA_TRY(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->stream));
+        }
+        return PICGB_OK;
+    }
+
+    bool hasCurrent(Species const& sp) { return sp.cfg.current == PICGB_CURRENT_ESIRKEPOV; }
+} // namespace
+
+extern "C"
+{
+    int picgb_abi_version(void) { return PICGB_ABI_VERSION; }
+
+    const char* picgb_last_error(void) { return g_lastError.c_str(); }
+
+    int picgb_create(const picgb_grid_config* cfg, picgb_sim** out)
+    {
+        if(!cfg || !out)
+            return fail(PICGB_ERR_INVALID, "null argument");
+        *out = nullptr;
+        int sc[3];
+        if(!scSize(cfg->supercell, sc))
+            return fail(PICGB_ERR_INVALID, "unknown supercell id %d", int(cfg->supercell));
+        if(cfg->nx <= 0 || cfg->ny <= 0 || cfg->nz <= 0 || cfg->nx % sc[0] || cfg->ny % sc[1] || cfg->nz % sc[2])
+            return fail(PICGB_ERR_INVALID, "grid %dx%dx%d is not a positive multiple of the supercell %dx%dx%d",
+                        int(cfg->nx), int(cfg->ny), int(cfg->nz), sc[0], sc[1], sc[2]);
+        if(cfg->field_solver != PICGB_SOLVER_YEE)
+            return fail(PICGB_ERR_UNSUPPORTED, "field solver %d is not available", int(cfg->field_solver));
+        if(!(cfg->dx > 0 && cfg->dy > 0 && cfg->dz > 0 && cfg->dt > 0 && cfg->c > 0 && cfg->eps0 > 0))
+            return fail(PICGB_ERR_INVALID, "cell sizes, dt, c and eps0 must be positive");
+        // Courant-Friedrichs-Lewy condition of the Yee solver (MaxwellSolver/Yee/Yee.hpp:57-63)
+        double const cfl = double(cfg->c) * cfg->c * double(cfg->dt) * cfg->dt
+            * (1.0 / (double(cfg->dx) * cfg->dx) + 1.0 / (double(cfg->dy) * cfg->dy) + 1.0 / (double(cfg->dz) * cfg->dz));
+        if(cfl > 1.0)
+            return fail(PICGB_ERR_INVALID, "Courant-Friedrichs-Lewy condition violated: c^2 dt^2 sum 1/d^2 = %g > 1", cfl);
+        int ndev = 0;
+        CUDA_TRY(cudaGetDeviceCount(&ndev));
+        if(cfg->device < 0 || cfg->device >= ndev)
+            return fail(PICGB_ERR_INVALID, "CUDA device %d not present (%d devices)", int(cfg->device), ndev);
+        CUDA_TRY(cudaSetDevice(cfg->device));
+
+        auto s = std::make_unique<picgb_sim>();
+        s->cfg = *cfg;
+        std::copy(sc, sc + 3, s->sc);
+        s->g.nx = cfg->nx;
+        s->g.ny = cfg->ny;
+        s->g.nz = cfg->nz;
+        s->g.nscx = cfg->nx / sc[0];
+        s->g.nscy = cfg->ny / sc[1];
+        s->g.nscz = cfg->nz / sc[2];
+        s->g.dx = cfg->dx;
+        s->g.dy = cfg->dy;
+        s->g.dz = cfg->dz;
+        s->g.dt = cfg->dt;
+        s->g.c = cfg->c;
+        s->g.eps0 = cfg->eps0;
+        s->nsc = s->g.nscx * s->g.nscy * s->g.nscz;
+        s->ncell = size_t(cfg->nx) * cfg->ny * cfg->nz;
+        CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        s->ownStream = true;
+        CUDA_TRY(dalloc(s->E, 3 * s->ncell));
+        CUDA_TRY(dalloc(s->B, 3 * s->ncell));
+        CUDA_TRY(dalloc(s->J, 3 * s->ncell));
+        CUDA_TRY(dalloc(s->rho, s->ncell));
+        CUDA_TRY(dalloc(s->status, 1));
+        CUDA_TRY(dalloc(s->energy, 64));
+        CUDA_TRY(dalloc(s->maxBits, 2));
+        CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&s->hostStatus), sizeof(unsigned)));
+        CUDA_TRY(cudaMemsetAsync(s->E, 0, sizeof(float) * 3 * s->ncell, s->stream));
+        CUDA_TRY(cudaMemsetAsync(s->B, 0, sizeof(float) * 3 * s->ncell, s->stream));
+        CUDA_TRY(cudaMemsetAsync(s->J, 0, sizeof(float) * 3 * s->ncell, s->stream));
+        CUDA_TRY(cudaMemsetAsync(s->rho, 0, sizeof(float) * s->ncell, s->stream));
+        CUDA_TRY(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        // DataConnector registrations of Simulation::init (Simulation.hpp:324-339, 740-753)
+        addEntry(s.get(), "E", Entry{Entry::FieldE});
+        addEntry(s.get(), "B", Entry{Entry::FieldB});
+        addEntry(s.get(), "J", Entry{Entry::FieldJ});
+        addEntry(s.get(), "FieldTmp0", Entry{Entry::FieldTmp});
+        addEntry(s.get(), "FieldSolverFDTD", Entry{Entry::Opaque});
+        addEntry(s.get(), "CurrentInterpolationAndAdditionToEMF", Entry{Entry::Opaque});
+        *out = s.release();
+        return PICGB_OK;
+    }
+
+    int picgb_destroy(picgb_sim* s)
+    {
+        if(!s)
+            return PICGB_OK;
+        cudaSetDevice(s->cfg.device);
+        if(s->stream)
+            cudaStreamSynchronize(s->stream);
+        for(auto& sp : s->species)
+            sp->freeAll();
+        dfree(s->E);
+        dfree(s->B);
+        dfree(s->J);
+        dfree(s->rho);
+        dfree(s->status);
+        dfree(s->energy);
+        dfree(s->maxBits);
+        if(s->hostStatus)
+            cudaFreeHost(s->hostStatus);
+        profFlush(s);
+        for(auto e : s->eventPool)
+            cudaEventDestroy(e);
+        if(s->ownStream && s->stream)
+            cudaStreamDestroy(s->stream);
+        delete s;
+        return PICGB_OK;
+    }
+
+    int picgb_add_species(picgb_sim* s, const picgb_species_config* cfg, int32_t* index)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(!cfg || !cfg->name || !cfg->name[0])
+            return fail(PICGB_ERR_INVALID, "species needs a name");
+        if(cfg->pusher < 0 || cfg->pusher > 2)
+            return fail(PICGB_ERR_INVALID, "unknown pusher %d", int(cfg->pusher));
+        if(cfg->shape < PICGB_SHAPE_CIC || cfg->shape > PICGB_SHAPE_PQS)
+            return fail(PICGB_ERR_UNSUPPORTED, "shape %d has no CUDA kernel (CIC, TSC, PQS are available)",
+                        int(cfg->shape));
+        if(cfg->current < 0 || cfg->current > 1)
+            return fail(PICGB_ERR_INVALID, "unknown current solver %d", int(cfg->current));
+        if(!(cfg->mass > 0.0f))
+            return fail(PICGB_ERR_INVALID, "species mass must be positive");
+        if(cfg->capacity > 65504)
+            return fail(PICGB_ERR_INVALID, "capacity %u exceeds 65504 slots per supercell", cfg->capacity);
+        auto sp = std::make_unique<Species>();
+        sp->name = cfg->name;
+        sp->cfg = *cfg;
+        sp->cfg.name = nullptr;
+        Entry e{Entry::SpeciesBuf};
+        e.index = int(s->species.size());
+        if(int r = addEntry(s, sp->name, e))
+            return r;
+        s->species.push_back(std::move(sp));
+        if(index)
+            *index = e.index;
+        return PICGB_OK;
+    }
+
+    int picgb_species_set(picgb_sim* s, int32_t si, const picgb_particles* h)
+    {
+        if(int r = checkSpecies(s, si))
+            return r;
+        if(!h)
+            return fail(PICGB_ERR_INVALID, "null particle descriptor");
+        Species& sp = *s->species[si];
+        uint64_t const n = h->n;
+        if(n && (!h->pos[0] || !h->pos[1] || !h->pos[2] || !h->mom[0] || !h->mom[1] || !h->mom[2] || !h->w || !h->sc
+                 || !h->lcell))
+            return fail(PICGB_ERR_INVALID, "particle arrays must not be null");
+        CUDA_TRY(cudaSetDevice(s->cfg.device));
+        Staging st;
+        CUDA_TRY(st.alloc(n, sp.cfg.with_ids != 0 && h->id));
+        float const* src[7] = {h->pos[0], h->pos[1], h->pos[2], h->mom[0], h->mom[1], h->mom[2], h->w};
+        for(int k = 0; k < 7; ++k)
+            CUDA_TRY(cudaMemcpyAsync(st.a[k], src[k], sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(st.sc, h->sc, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(st.lcell, h->lcell, sizeof(uint16_t) * n, cudaMemcpyHostToDevice, s->stream));
+        if(st.id)
+            CUDA_TRY(cudaMemcpyAsync(st.id, h->id, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s->stream));
+        uint32_t* hcount = nullptr;
+        CUDA_TRY(dalloc(hcount, size_t(s->nsc)));
+        CUDA_TRY(cudaMemsetAsync(hcount, 0, sizeof(uint32_t) * s->nsc, s->stream));
+        CUDA_TRY(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->stream));
+        float const* pos3[3] = {st.a[0], st.a[1], st.a[2]};
+        CUDA_TRY(launchHistogram(s->cfg.supercell, n, st.sc, st.lcell, pos3, hcount, s->nsc, s->status, s->stream));
+        ++s->launches;
+        std::vector<uint32_t> cnt(s->nsc);
+        CUDA_TRY(cudaMemcpyAsync(cnt.data(), hcount, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToHost, s->stream));
+        unsigned bits = 0;
+        if(int r = readStatus(s, &bits, true))
+        {
+            dfree(hcount);
+            return r;
+        }
+        dfree(hcount);
+        if(bits & ST_BAD_CELL)
+            return fail(PICGB_ERR_INVALID, "species '%s': a particle has an out-of-range supercell, cell index or in-cell position",
+                        sp.name.c_str());
+        uint32_t const mx = cnt.empty() ? 0u : *std::max_element(cnt.begin(), cnt.end());
+        uint32_t cap = sp.cfg.capacity;
+        if(cap == 0)
+            cap = uint32_t(std::max<uint64_t>(32, uint64_t(std::ceil(1.25 * mx))));
+        cap = (cap + 31) / 32 * 32;
+        if(cap > 65504)
+            return fail(PICGB_ERR_OVERFLOW, "species '%s': %u particles per supercell exceed the slot limit",
+                        sp.name.c_str(), mx);
+        if(mx > cap)
+            return fail(PICGB_ERR_OVERFLOW, "species '%s': a supercell holds %u particles, capacity is %u",
+                        sp.name.c_str(), mx, cap);
+        if(!sp.allocated || sp.dev.cap != cap)
+        {
+            if(int r = allocSpecies(s, sp, cap))
+                return r;
+        }
+        else
+        {
+            CUDA_TRY(cudaMemsetAsync(sp.dev.count, 0, sizeof(uint32_t) * s->nsc, s->stream));
+            CUDA_TRY(cudaMemsetAsync(sp.dev.nhole, 0, sizeof(uint32_t) * s->nsc, s->stream));
+            CUDA_TRY(cudaMemsetAsync(sp.dev.sp_count, 0, sizeof(uint32_t), s->stream));
+        }
+        float const* attr[7] = {st.a[0], st.a[1], st.a[2], st.a[3], st.a[4], st.a[5], st.a[6]};
+        CUDA_TRY(launchScatter(n, attr, st.sc, st.lcell, st.id, sp.dev, s->status, s->stream));
+        ++s->launches;
+        CUDA_TRY(cudaMemcpyAsync(sp.dev.tail, sp.dev.count, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToDevice, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return PICGB_OK;
+    }
+
+    int picgb_species_init_plasma(picgb_sim* s, int32_t si, const picgb_plasma_init* init)
+    {
+        if(int r = checkSpecies(s, si))
+            return r;
+        if(!init || init->ppc == 0)
+            return fail(PICGB_ERR_INVALID, "plasma init needs ppc > 0");
+        if(init->split_axis > 2 || !(init->u_th >= 0.0f) || !(init->density >= 0.0f))
+            return fail(PICGB_ERR_INVALID, "invalid plasma init parameters");
+        Species& sp = *s->species[si];
+        CUDA_TRY(cudaSetDevice(s->cfg.device));
+        uint64_t const perSc = uint64_t(init->ppc) * s->sc[0] * s->sc[1] * s->sc[2];
+        uint64_t cap = sp.cfg.capacity ? sp.cfg.capacity : uint64_t(std::ceil(1.25 * perSc));
+        cap = (std::max<uint64_t>(cap, 32) + 31) / 32 * 32;
+        if(cap < perSc || cap > 65504)
+            return fail(PICGB_ERR_OVERFLOW, "species '%s': %llu particles per supercell do not fit %llu slots (max 65504)",
+                        sp.name.c_str(), (unsigned long long) perSc, (unsigned long long) cap);
+        if(!sp.allocated || sp.dev.cap != cap)
+        {
+            if(int r = allocSpecies(s, sp, uint32_t(cap)))
+                return r;
+        }
+        InitParams ip{};
+        ip.ppc = init->ppc;
+        ip.weight = init->density * s->cellVolume() / float(init->ppc);
+        ip.mass = sp.cfg.mass;
+        ip.c = s->cfg.c;
+        ip.u_th = init->u_th;
+        for(int d = 0; d < 3; ++d)
+        {
+            ip.drift_lo[d] = init->drift_lo[d];
+            ip.drift_hi[d] = init->drift_hi[d];
+        }
+        ip.split_axis = init->split_axis;
+        ip.split_cell = init->split_cell;
+        ip.seed = init->seed;
+        ip.position_seed = init->position_seed;
+        CUDA_TRY(cudaMemsetAsync(sp.dev.sp_count, 0, sizeof(uint32_t), s->stream));
+        CUDA_TRY(launchInitPlasma(sp.dev, s->g, ip, s->sc, s->stream));
+        ++s->launches;
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return PICGB_OK;
+    }
+
+    int picgb_species_count(picgb_sim* s, int32_t si, uint64_t* n)
+    {
+        if(int r = checkSpecies(s, si))
+            return r;
+        Species& sp = *s->species[si];
+        *n = 0;
+        if(!sp.allocated)
+            return PICGB_OK;
+        std::vector<uint32_t> cnt(s->nsc);
+        CUDA_TRY(cudaMemcpyAsync(cnt.data(), sp.dev.count, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        uint64_t t = 0;
+        for(auto c : cnt)
+            t += c;
+        *n = t;
+        return PICGB_OK;
+    }
+
+    int picgb_species_get(picgb_sim* s, int32_t si, picgb_particles* h)
+    {
+        if(int r = checkSpecies(s, si))
+            return r;
+        Species& sp = *s->species[si];
+        if(!sp.allocated)
+        {
+            h->n = 0;
+            return PICGB_OK;
+        }
+        std::vector<uint32_t> cnt(s->nsc);
+        CUDA_TRY(cudaMemcpyAsync(cnt.data(), sp.dev.count, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        std::vector<uint64_t> off(s->nsc);
+        uint64_t total = 0;
+        for(int i = 0; i < s->nsc; ++i)
+        {
+            off[i] = total;
+            total += cnt[i];
+        }
+        if(h->n < total)
+            return fail(PICGB_ERR_INVALID, "host arrays hold %llu particles, %llu needed",
+                        (unsigned long long) h->n, (unsigned long long) total);
+        Staging st;
+        CUDA_TRY(st.alloc(total, h->id != nullptr));
+        uint64_t* doff = nullptr;
+        CUDA_TRY(dalloc(doff, size_t(s->nsc)));
+        CUDA_TRY(cudaMemcpyAsync(doff, off.data(), sizeof(uint64_t) * s->nsc, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, st.a, st.sc, st.lcell, st.id, s->stream));
+        ++s->launches;
+        float* dst[7] = {h->pos[0], h->pos[1], h->pos[2], h->mom[0], h->mom[1], h->mom[2], h->w};
+        for(int k = 0; k < 7; ++k)
+            CUDA_TRY(cudaMemcpyAsync(dst[k], st.a[k], sizeof(float) * total, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(h->sc, st.sc, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(h->lcell, st.lcell, sizeof(uint16_t) * total, cudaMemcpyDeviceToHost, s->stream));
+        if(h->id)
+            CUDA_TRY(cudaMemcpyAsync(h->id, st.id, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        dfree(doff);
+        h->n = total;
+        return PICGB_OK;
+    }
+
+    static int fieldPtr(picgb_sim* s, const char* name, float** p, int* ncomp)
+    {
+        if(!name)
+            return fail(PICGB_ERR_INVALID, "null field name");
+        std::string const n(name);
+        if(n == "E")
+            *p = s->E, *ncomp = 3;
+        else if(n == "B")
+            *p = s->B, *ncomp = 3;
+        else if(n == "J")
+            *p = s->J, *ncomp = 3;
+        else if(n == "FieldTmp0")
+            *p = s->rho, *ncomp = 1;
+        else
+            return fail(PICGB_ERR_NOT_FOUND, "DataConnector: unknown field id '%s'", name);
+        return PICGB_OK;
+    }
+
+    int picgb_field_set(picgb_sim* s, const char* name, const float* const* host)
+    {
+        if(int r = checkSim(s))
+            return r;
+        float* p = nullptr;
+        int nc = 0;
+        if(int r = fieldPtr(s, name, &p, &nc))
+            return r;
+        for(int c = 0; c < nc; ++c)
+            CUDA_TRY(cudaMemcpyAsync(p + c * s->ncell, host[c], sizeof(float) * s->ncell, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return PICGB_OK;
+    }
+
+    int picgb_field_get(picgb_sim* s, const char* name, float* const* host)
+    {
+        if(int r = checkSim(s))
+            return r;
+        float* p = nullptr;
+        int nc = 0;
+        if(int r = fieldPtr(s, name, &p, &nc))
+            return r;
+        for(int c = 0; c < nc; ++c)
+            CUDA_TRY(cudaMemcpyAsync(host[c], p + c * s->ncell, sizeof(float) * s->ncell, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return PICGB_OK;
+    }
+
+    // ------------------------------------------------------------ registry
+    int picgb_get_buffer(picgb_sim* s, const char* name, picgb_buffer_desc* out)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(!name || !out)
+            return fail(PICGB_ERR_INVALID, "null argument");
+        auto it = s->registry.find(name);
+        if(it == s->registry.end())
+            return fail(PICGB_ERR_NOT_FOUND, "DataConnector: unknown id '%s'", name);
+        Entry const& e = it->second;
+        switch(e.kind)
+        {
+        case Entry::FieldE:
+            fieldDesc(s, s->E, 3, out);
+            break;
+        case Entry::FieldB:
+            fieldDesc(s, s->B, 3, out);
+            break;
+        case Entry::FieldJ:
+            fieldDesc(s, s->J, 3, out);
+            break;
+        case Entry::FieldTmp:
+            fieldDesc(s, s->rho, 1, out);
+            break;
+        case Entry::SpeciesBuf:
+            speciesDesc(s, *s->species[e.index], out);
+            break;
+        case Entry::Opaque:
+            std::memset(out, 0, sizeof(*out));
+            out->kind = PICGB_BUFFER_OPAQUE;
+            break;
+        case Entry::External:
+            *out = e.desc;
+            break;
+        }
+        return PICGB_OK;
+    }
+
+    int picgb_share(picgb_sim* s, const char* name, const picgb_buffer_desc* desc)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(!name || !name[0] || !desc)
+            return fail(PICGB_ERR_INVALID, "null argument");
+        Entry e{Entry::External};
+        e.desc = *desc;
+        return addEntry(s, name, e);
+    }
+
+    int picgb_unshare(picgb_sim* s, const char* name)
+    {
+        if(int r = checkSim(s))
+            return r;
+        auto it = s->registry.find(name ? name : "");
+        if(it == s->registry.end())
+            return fail(PICGB_ERR_NOT_FOUND, "DataConnector: unknown id '%s'", name ? name : "(null)");
+        if(it->second.kind != Entry::External)
+            return fail(PICGB_ERR_INVALID, "DataConnector: '%s' is owned by the simulation", name);
+        s->registry.erase(it);
+        return PICGB_OK;
+    }
+
+    int picgb_registry_size(picgb_sim* s, int32_t* n)
+    {
+        if(int r = checkSim(s))
+            return r;
+        *n = int32_t(s->registry.size());
+        return PICGB_OK;
+    }
+
+    int picgb_registry_name(picgb_sim* s, int32_t i, char* buf, size_t len)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(i < 0 || i >= int32_t(s->registry.size()) || !buf || len == 0)
+            return fail(PICGB_ERR_INVALID, "registry index %d out of range", int(i));
+        auto it = s->registry.begin();
+        std::advance(it, i);
+        std::snprintf(buf, len, "%s", it->first.c_str());
+        return PICGB_OK;
+    }
+
+    // ------------------------------------------------------------ stages
+    int picgb_stage_current_reset(picgb_sim* s)
+    {
+        if(int r = checkSim(s))
+            return r;
+        CUDA_TRY(cudaMemsetAsync(s->J, 0, sizeof(float) * 3 * s->ncell, s->stream));
+        return PICGB_OK;
+    }
+
+    int picgb_stage_push(picgb_sim* s, uint32_t)
+    {
+        if(int r = checkSim(s))
+            return r;
+        bool const fuse = s->cfg.fuse_deposit != 0;
+        for(auto& sp : s->species)
+        {
+            if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE)
+                continue;
+            PushParams const pp = s->pushParams(*sp, fuse && hasCurrent(*sp));
+            Species& x = *sp;
+            CUDA_TRY(timedLaunch(s, PICGB_KERNEL_PUSH, [&] {
+                return launchPush(x.cfg.shape, s->cfg.supercell, x.dev, s->E, s->B, s->J, s->g, pp, s->status, s->stream);
+            }));
+        }
+        for(auto& sp : s->species)
+        {
+            if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE)
+                continue;
+            Species& x = *sp;
+            CUDA_TRY(timedLaunch(s, PICGB_KERNEL_COMPACT, [&] { return launchCompact(x.dev, s->nsc, s->stream); }));
+        }
+        return PICGB_OK;
+    }
+
+    int picgb_stage_field_before(picgb_sim* s, uint32_t)
+    {
+        if(int r = checkSim(s))
+            return r;
+        CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_B, [&] { return launchYeeBHalf(s->E, s->B, s->g, s->stream); }));
+        // with the fused deposit J is complete here: E += curl B c^2 dt and E += coeff J in one pass
+        float const* J = s->cfg.fuse_deposit ? s->J : nullptr;
+        CUDA_TRY(timedLaunch(
+            s,
+            PICGB_KERNEL_YEE_E,
+            [&] { return launchYeeE(s->B, s->E, J, s->coeffJ(), s->g, s->stream); }));
+        return PICGB_OK;
+    }
+
+    int picgb_stage_deposit(picgb_sim* s, uint32_t)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(s->cfg.fuse_deposit)
+            return PICGB_OK;
+        for(auto& sp : s->species)
+        {
+            if(!sp->allocated || !hasCurrent(*sp))
+                continue;
+            PushParams const pp = s->pushParams(*sp, true);
+            Species& x = *sp;
+            CUDA_TRY(timedLaunch(s, PICGB_KERNEL_DEPOSIT, [&] {
+                return launchDeposit(x.cfg.shape, s->cfg.supercell, x.dev, s->J, s->g, pp, s->status, s->stream);
+            }));
+        }
+        return PICGB_OK;
+    }
+
+    int picgb_stage_add_current(picgb_sim* s)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(s->cfg.fuse_deposit)
+            return PICGB_OK; // folded into the E update of picgb_stage_field_before
+        CUDA_TRY(timedLaunch(
+            s,
+            PICGB_KERNEL_ADD_CURRENT,
+            [&] { return launchAddCurrent(s->E, s->J, s->coeffJ(), s->ncell, s->stream); }));
+        return PICGB_OK;
+    }
+
+    int picgb_stage_field_after(picgb_sim* s, uint32_t)
+    {
+        if(int r = checkSim(s))
+            return r;
+        CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_B, [&] { return launchYeeBHalf(s->E, s->B, s->g, s->stream); }));
+        return PICGB_OK;
+    }
+
+    int picgb_step(picgb_sim* s, uint32_t step)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(int r = picgb_stage_current_reset(s))
+            return r;
+        if(int r = picgb_stage_push(s, step))
+            return r;
+        if(int r = picgb_stage_field_before(s, step))
+            return r;
+        if(int r = picgb_stage_deposit(s, step))
+            return r;
+        if(int r = picgb_stage_add_current(s))
+            return r;
+        if(int r = picgb_stage_field_after(s, step))
+            return r;
+        return afterStep(s);
+    }
+
+    int picgb_run(picgb_sim* s, uint32_t step, uint32_t n)
+    {
+        for(uint32_t i = 0; i < n; ++i)
+            if(int r = picgb_step(s, step + i))
+                return r;
+        return PICGB_OK;
+    }
+
+    // ------------------------------------------------------------ diagnostics
+    int picgb_energies(picgb_sim* s, double* out, size_t len)
+    {
+        if(int r = checkSim(s))
+            return r;
+        size_t const need = 2 + s->species.size();
+        if(!out || len < need)
+            return fail(PICGB_ERR_INVALID, "energies need %zu entries", need);
+        if(need + 4 > 64)
+            return fail(PICGB_ERR_INVALID, "too many species for the energy reduction");
+        CUDA_TRY(cudaMemsetAsync(s->energy, 0, sizeof(double) * 64, s->stream));
+        CUDA_TRY(launchFieldEnergy(s->E, s->ncell, s->energy, s->stream));
+        CUDA_TRY(launchFieldEnergy(s->B, s->ncell, s->energy + 3, s->stream));
+        s->launches += 2;
+        for(size_t i = 0; i < s->species.size(); ++i)
+        {
+            Species& sp = *s->species[i];
+            if(!sp.allocated)
+                continue;
+            CUDA_TRY(launchKineticEnergy(sp.dev, s->nsc, sp.cfg.mass, s->cfg.c, s->energy + 6 + i, s->stream));
+            ++s->launches;
+        }
+        double h[64];
+        CUDA_TRY(cudaMemcpyAsync(h, s->energy, sizeof(double) * (6 + s->species.size()), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        double const V = double(s->cfg.dx) * double(s->cfg.dy) * double(s->cfg.dz);
+        double const mu0 = 1.0 / (double(s->cfg.eps0) * double(s->cfg.c) * double(s->cfg.c));
+        out[0] = out[1] = 0.0;
+        for(int d = 0; d < 3; ++d)
+        {
+            out[0] += h[d] * (double(s->cfg.eps0) * V * 0.5);
+            out[1] += h[3 + d] * (0.5 / mu0 * V);
+        }
+        for(size_t i = 0; i < s->species.size(); ++i)
+            out[2 + i] = h[6 + i];
+        return PICGB_OK;
+    }
+
+    int picgb_charge_residual(picgb_sim* s, double* maxResidual, double* maxRho)
+    {
+        if(int r = checkSim(s))
+            return r;
+        CUDA_TRY(cudaMemsetAsync(s->rho, 0, sizeof(float) * s->ncell, s->stream));
+        CUDA_TRY(cudaMemsetAsync(s->maxBits, 0, sizeof(unsigned) * 2, s->stream));
+        float const V = s->cellVolume();
+        for(auto& sp : s->species)
+        {
+            if(!sp->allocated || !hasCurrent(*sp))
+                continue;
+            CUDA_TRY(launchChargeDensity(sp->cfg.shape, s->cfg.supercell, sp->dev, s->rho, s->g, sp->cfg.charge, V, s->stream));
+            ++s->launches;
+        }
+        CUDA_TRY(launchChargeResidual(s->E, s->rho, s->g, nullptr, s->maxBits, s->maxBits + 1, s->stream));
+        ++s->launches;
+        unsigned bits[2];
+        CUDA_TRY(cudaMemcpyAsync(bits, s->maxBits, sizeof(bits), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        float f0, f1;
+        std::memcpy(&f0, &bits[0], 4);
+        std::memcpy(&f1, &bits[1], 4);
+        if(maxResidual)
+            *maxResidual = f0;
+        if(maxRho)
+            *maxRho = f1;
+        return PICGB_OK;
+    }
+
+    // ------------------------------------------------------------ execution control
+    int picgb_set_stream(picgb_sim* s, void* stream)
+    {
+        if(int r = checkSim(s))
+            return r;
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        if(s->ownStream)
+            cudaStreamDestroy(s->stream);
+        if(stream)
+        {
+            s->stream = static_cast<cudaStream_t>(stream);
+            s->ownStream = false;
+        }
+        else
+        {
+            CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+            s->ownStream = true;
+        }
+        return PICGB_OK;
+    }
+
+    int picgb_synchronize(picgb_sim* s)
+    {
+        if(int r = checkSim(s))
+            return r;
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return PICGB_OK;
+    }
+
+    int picgb_launch_count(picgb_sim* s, uint64_t* n)
+    {
+        if(int r = checkSim(s))
+            return r;
+        *n = s->launches;
+        return PICGB_OK;
+    }
+
+    int picgb_profile_enable(picgb_sim* s, int32_t on)
+    {
+        if(int r = checkSim(s))
+            return r;
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        CUDA_TRY(profFlush(s));
+        s->prof = on != 0;
+        for(int i = 0; i < PICGB_KERNEL_CLASSES; ++i)
+        {
+            s->profMs[i] = 0.0;
+            s->profN[i] = 0;
+        }
+        return PICGB_OK;
+    }
+
+    int picgb_profile_read(picgb_sim* s, int32_t cls, double* ms, uint64_t* n)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(cls < 0 || cls >= PICGB_KERNEL_CLASSES)
+            return fail(PICGB_ERR_INVALID, "kernel class %d out of range", int(cls));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        CUDA_TRY(profFlush(s));
+        if(ms)
+            *ms = s->profMs[cls];
+        if(n)
+            *n = s->profN[cls];
+        return PICGB_OK;
+    }
+
+    int picgb_device_status(picgb_sim* s, uint32_t* bits, int32_t reset)
+    {
+        if(int r = checkSim(s))
+            return r;
+        unsigned b = 0;
+        if(int r = readStatus(s, &b, reset != 0))
+            return r;
+        *bits = b;
+        return PICGB_OK;
+    }
+}

@@ -1,0 +1,142 @@
+// Internal declarations shared by the host runtime (picgb_api.cu) and the
+// kernel translation units.  Not part of the C-ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace picgb
+{
+    struct GridParams; // picgb_device.cuh
+
+    // Status bits written by kernels into a device word (never a trap).
+    enum StatusBits : unsigned
+    {
+        ST_OVERFLOW = 1u, // a supercell ran out of slots; particles were parked in the spill buffer
+        ST_LOST = 2u, // the spill buffer was full as well: particles were dropped
+        ST_BAD_CELL = 4u, // an input particle had an out-of-range supercell or cell index
+        ST_TIMEOUT = 8u // a bounded wait gave up (persistent kernels)
+    };
+
+    // Particle storage of one species on the device: supercell-major SoA with
+    // a fixed number of slots per supercell.  Slots [0, count[sc]) of supercell
+    // sc are valid particles, stored at sc * cap + slot.
+    struct SpeciesDev
+    {
+        float* px;
+        float* py;
+        float* pz;
+        float* ux;
+        float* uy;
+        float* uz;
+        float* w;
+        uint16_t* lcell;
+        uint32_t* id; // optional (nullptr)
+        uint32_t* count; // [nsc] valid particles per supercell
+        uint32_t* tail; // [nsc] append cursor during the push (starts at count)
+        uint32_t* nhole; // [nsc] slots vacated by leaving particles
+        uint16_t* holes; // [nsc * cap] vacated slot indices
+        uint32_t cap; // slots per supercell (multiple of 32, <= 65535)
+        // spill buffer for arrivals that found their supercell full
+        float* sp_attr; // [7 * spill_cap]: px,py,pz,ux,uy,uz,w
+        int32_t* sp_sc; // [spill_cap] destination supercell
+        uint16_t* sp_lcell; // [spill_cap]
+        uint32_t* sp_id; // [spill_cap]
+        uint32_t* sp_count;
+        uint32_t spill_cap;
+    };
+
+    struct PushParams
+    {
+        float charge; // per real particle
+        float mass; // per real particle
+        float dt;
+        float c2; // c * c
+        float rc2; // 1 / (c * c)
+        float invVdt; // 1 / (dx * dy * dz * dt)
+        int pusher; // 0 Boris, 1 Free (2 = not pushed, never launched)
+        int deposit; // deposit the current inside the push kernel
+    };
+
+    // ---- launchers (kernels_*.cu); all asynchronous on `stream`
+    // shape: 1 CIC, 2 TSC, 3 PQS; scId: 0 -> 8x8x4, 1 -> 4x4x4, 2 -> 8x8x8
+    cudaError_t launchPush(
+        int shape,
+        int scId,
+        SpeciesDev const& sp,
+        float const* E,
+        float const* B,
+        float* J,
+        GridParams const& g,
+        PushParams const& pp,
+        unsigned* status,
+        cudaStream_t stream);
+    cudaError_t launchDeposit(
+        int shape,
+        int scId,
+        SpeciesDev const& sp,
+        float* J,
+        GridParams const& g,
+        PushParams const& pp,
+        unsigned* status,
+        cudaStream_t stream);
+    cudaError_t launchCompact(SpeciesDev const& sp, int nsc, cudaStream_t stream);
+    cudaError_t launchHistogram(
+        int scId,
+        uint64_t n,
+        int32_t const* sc,
+        uint16_t const* lcell,
+        float const* const* pos, // 3 position arrays to validate, or nullptr
+        uint32_t* count,
+        int nsc,
+        unsigned* status,
+        cudaStream_t stream);
+    cudaError_t launchScatter(
+        uint64_t n,
+        float const* const* attr, // 7 arrays: px py pz ux uy uz w
+        int32_t const* sc,
+        uint16_t const* lcell,
+        uint32_t const* id,
+        SpeciesDev const& sp,
+        unsigned* status,
+        cudaStream_t stream);
+    cudaError_t launchGatherOut(
+        SpeciesDev const& sp,
+        int nsc,
+        uint64_t const* offsets,
+        float* const* attr,
+        int32_t* sc,
+        uint16_t* lcell,
+        uint32_t* id,
+        cudaStream_t stream);
+    cudaError_t launchChargeDensity(
+        int shape,
+        int scId,
+        SpeciesDev const& sp,
+        float* rho,
+        GridParams const& g,
+        float charge,
+        float cellVolume,
+        cudaStream_t stream);
+    cudaError_t launchKineticEnergy(
+        SpeciesDev const& sp,
+        int nsc,
+        float mass,
+        float c,
+        double* out,
+        cudaStream_t stream);
+
+    // fields (kernels_fields.cu); fields are SoA [3][nz][ny][nx]
+    cudaError_t launchYeeBHalf(float const* E, float* B, GridParams const& g, cudaStream_t stream);
+    cudaError_t launchYeeE(float const* B, float* E, float const* J, float coeff, GridParams const& g, cudaStream_t stream);
+    cudaError_t launchAddCurrent(float* E, float const* J, float coeff, size_t ncell, cudaStream_t stream);
+    cudaError_t launchFieldEnergy(float const* F, size_t ncell, double* out3, cudaStream_t stream);
+    cudaError_t launchChargeResidual(
+        float const* E,
+        float const* rho,
+        GridParams const& g,
+        float* out,
+        unsigned* maxBits,
+        unsigned* maxRhoBits,
+        cudaStream_t stream);
+} // namespace picgb

@@ -1,0 +1,292 @@
+"""Python mirror of the reference's operator surface for the PIC hot path.
+
+``Simulation`` follows simulation/control/Simulation.hpp: fields "E", "B", "J"
+and "FieldTmp0" exist from construction, species are added with the
+``.param`` flags of param/speciesDefinition.param (pusher, shape, current
+solver, charge and mass), ``step()`` runs Simulation::runOneStep and
+``data_connector.get(id)`` resolves a registered id like
+pmacc::DataConnector::get (raising on an unknown id).  All work runs in the
+CUDA library libpicgb.so through its C-ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+# .param policy names -> C-ABI enums (param/species.param:49-90, param/fieldSolver.param:57)
+PUSHERS = {"Boris": L.PUSHER_BORIS, "Free": L.PUSHER_FREE, None: L.PUSHER_NONE}
+SHAPES = {"CIC": L.SHAPE_CIC, "TSC": L.SHAPE_TSC, "PQS": L.SHAPE_PQS}
+CURRENTS = {"Esirkepov": L.CURRENT_ESIRKEPOV, None: L.CURRENT_NONE}
+SOLVERS = {"Yee": L.SOLVER_YEE}
+SUPERCELLS = {(8, 8, 4): L.SUPERCELL_8x8x4, (4, 4, 4): L.SUPERCELL_4x4x4, (8, 8, 8): L.SUPERCELL_8x8x8}
+
+
+@dataclass
+class Grid:
+    nx: int
+    ny: int
+    nz: int
+    dx: float = 1.0
+    dy: float = 1.0
+    dz: float = 1.0
+    dt: float = float(np.float32(0.99 / np.sqrt(3.0)))
+    c: float = 1.0
+    eps0: float = 1.0
+    supercell: tuple = (8, 8, 4)
+    solver: str = "Yee"
+    fuse_deposit: bool = True
+    device: int = 0
+
+    @property
+    def sx(self):
+        return self.supercell[0]
+
+    @property
+    def sy(self):
+        return self.supercell[1]
+
+    @property
+    def sz(self):
+        return self.supercell[2]
+
+    def as_dict(self):
+        return dict(nx=self.nx, ny=self.ny, nz=self.nz, sx=self.sx, sy=self.sy, sz=self.sz, dx=self.dx, dy=self.dy,
+                    dz=self.dz, dt=self.dt, c=self.c, eps0=self.eps0)
+
+
+@dataclass
+class Species:
+    name: str
+    charge: float
+    mass: float
+    pusher: str | None = "Boris"
+    shape: str = "TSC"
+    current: str | None = "Esirkepov"
+    capacity: int = 0
+    with_ids: bool = False
+
+    def as_dict(self):
+        return dict(charge=self.charge, mass=self.mass, shape=SHAPES[self.shape],
+                    pusher=PUSHERS[self.pusher] if self.pusher in PUSHERS else L.PUSHER_NONE,
+                    current=CURRENTS[self.current])
+
+
+def _ptr(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class DataConnector:
+    """Named registry of simulation data (pmacc/dataManagement/DataConnector.hpp:48-136)."""
+
+    def __init__(self, sim: "Simulation"):
+        self._sim = sim
+
+    def get(self, name: str) -> L.BufferDesc:
+        d = L.BufferDesc()
+        L.call("picgb_get_buffer", self._sim.handle, name.encode(), ctypes.byref(d))
+        return d
+
+    def share(self, name: str, desc: L.BufferDesc) -> None:
+        L.call("picgb_share", self._sim.handle, name.encode(), ctypes.byref(desc))
+
+    def unshare(self, name: str) -> None:
+        L.call("picgb_unshare", self._sim.handle, name.encode())
+
+    def ids(self) -> list[str]:
+        n = ctypes.c_int32()
+        L.call("picgb_registry_size", self._sim.handle, ctypes.byref(n))
+        out = []
+        buf = ctypes.create_string_buffer(256)
+        for i in range(n.value):
+            L.call("picgb_registry_name", self._sim.handle, i, buf, 256)
+            out.append(buf.value.decode())
+        return out
+
+
+class Simulation:
+    def __init__(self, grid: Grid):
+        self.grid = grid
+        cfg = L.GridConfig(grid.nx, grid.ny, grid.nz, SUPERCELLS[tuple(grid.supercell)], grid.dx, grid.dy, grid.dz,
+                           grid.dt, grid.c, grid.eps0, SOLVERS[grid.solver], int(bool(grid.fuse_deposit)),
+                           grid.device)
+        h = ctypes.c_void_p()
+        L.call("picgb_create", ctypes.byref(cfg), ctypes.byref(h))
+        self.handle = h
+        self.species: list[Species] = []
+        self.data_connector = DataConnector(self)
+        self.current_step = 0
+
+    # ------------------------------------------------------------ lifetime
+    def close(self):
+        if self.handle:
+            L.load().picgb_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ species
+    def add_species(self, sp: Species) -> int:
+        pusher = PUSHERS.get(sp.pusher, L.PUSHER_NONE)
+        cfg = L.SpeciesConfig(sp.name.encode(), sp.charge, sp.mass, pusher, SHAPES[sp.shape],
+                              CURRENTS[sp.current], sp.capacity, int(sp.with_ids))
+        idx = ctypes.c_int32()
+        L.call("picgb_add_species", self.handle, ctypes.byref(cfg), ctypes.byref(idx))
+        self.species.append(sp)
+        return idx.value
+
+    def species_index(self, name: str) -> int:
+        for i, s in enumerate(self.species):
+            if s.name == name:
+                return i
+        raise RuntimeError(f"unknown species '{name}'")
+
+    def set_particles(self, name: str, p: dict) -> None:
+        i = self.species_index(name)
+        arrs = {k: np.ascontiguousarray(p[k]) for k in ("pos", "mom", "w", "sc", "lcell")}
+        assert arrs["pos"].dtype == np.float32 and arrs["mom"].dtype == np.float32 and arrs["w"].dtype == np.float32
+        arrs["sc"] = arrs["sc"].astype(np.int32, copy=False)
+        arrs["lcell"] = arrs["lcell"].astype(np.uint16, copy=False)
+        ids = np.ascontiguousarray(p["id"], dtype=np.uint32) if "id" in p else None
+        d = L.Particles()
+        d.n = arrs["w"].shape[0]
+        for k in range(3):
+            d.pos[k] = arrs["pos"][k].ctypes.data
+            d.mom[k] = arrs["mom"][k].ctypes.data
+        d.w = arrs["w"].ctypes.data
+        d.sc = arrs["sc"].ctypes.data
+        d.lcell = arrs["lcell"].ctypes.data
+        d.id = ids.ctypes.data if ids is not None else None
+        L.call("picgb_species_set", self.handle, i, ctypes.byref(d))
+
+    def init_plasma(self, name: str, ppc: int, density: float, u_th: float, drift_lo=(0, 0, 0), drift_hi=None,
+                    split_axis: int = -1, split_cell: int = 0, seed: int = 42, position_seed: int = 42) -> None:
+        ip = L.PlasmaInit(ppc, density, u_th, (ctypes.c_float * 3)(*drift_lo),
+                          (ctypes.c_float * 3)(*(drift_hi if drift_hi is not None else drift_lo)), split_axis,
+                          split_cell, seed, position_seed)
+        L.call("picgb_species_init_plasma", self.handle, self.species_index(name), ctypes.byref(ip))
+
+    def particle_count(self, name: str) -> int:
+        n = ctypes.c_uint64()
+        L.call("picgb_species_count", self.handle, self.species_index(name), ctypes.byref(n))
+        return n.value
+
+    def get_particles(self, name: str, with_ids: bool | None = None, out: dict | None = None) -> dict:
+        """Copy a species out in the host exchange format; ``out`` may hold preallocated
+        (e.g. pinned) arrays with room for every particle."""
+        i = self.species_index(name)
+        n = self.particle_count(name)
+        if with_ids is None:
+            with_ids = self.species[i].with_ids
+        if out is None:
+            out = dict(pos=np.empty((3, n), np.float32), mom=np.empty((3, n), np.float32),
+                       w=np.empty(n, np.float32), sc=np.empty(n, np.int32), lcell=np.empty(n, np.uint16))
+            if with_ids:
+                out["id"] = np.empty(n, np.uint32)
+        else:
+            with_ids = "id" in out
+            if out["w"].shape[0] < n or out["pos"].shape[1] < n:
+                raise ValueError(f"output arrays hold fewer than {n} particles")
+        d = L.Particles()
+        d.n = n
+        for k in range(3):
+            d.pos[k] = out["pos"][k].ctypes.data
+            d.mom[k] = out["mom"][k].ctypes.data
+        d.w = out["w"].ctypes.data
+        d.sc = out["sc"].ctypes.data
+        d.lcell = out["lcell"].ctypes.data
+        d.id = out["id"].ctypes.data if with_ids else None
+        L.call("picgb_species_get", self.handle, i, ctypes.byref(d))
+        return out
+
+    # ------------------------------------------------------------ fields
+    def _field_shape(self, name):
+        nc = 1 if name == "FieldTmp0" else 3
+        return (nc, self.grid.nz, self.grid.ny, self.grid.nx)
+
+    def set_field(self, name: str, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float32).reshape(self._field_shape(name))
+        ptrs = (ctypes.c_void_p * a.shape[0])(*[a[c].ctypes.data for c in range(a.shape[0])])
+        L.call("picgb_field_set", self.handle, name.encode(), ptrs)
+
+    def get_field(self, name: str) -> np.ndarray:
+        a = np.empty(self._field_shape(name), np.float32)
+        ptrs = (ctypes.c_void_p * a.shape[0])(*[a[c].ctypes.data for c in range(a.shape[0])])
+        L.call("picgb_field_get", self.handle, name.encode(), ptrs)
+        return a
+
+    # ------------------------------------------------------------ stepping
+    def step(self) -> None:
+        L.call("picgb_step", self.handle, self.current_step)
+        self.current_step += 1
+
+    def run(self, n: int) -> None:
+        L.call("picgb_run", self.handle, self.current_step, n)
+        self.current_step += n
+
+    def stage(self, name: str) -> None:
+        fn = "picgb_stage_" + name
+        if name in ("current_reset", "add_current"):
+            L.call(fn, self.handle)
+        else:
+            L.call(fn, self.handle, self.current_step)
+
+    def synchronize(self) -> None:
+        L.call("picgb_synchronize", self.handle)
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        L.call("picgb_set_stream", self.handle, ctypes.c_void_p(stream_ptr) if stream_ptr else None)
+
+    # ------------------------------------------------------------ diagnostics
+    def energies(self) -> dict:
+        n = 2 + len(self.species)
+        out = (ctypes.c_double * n)()
+        L.call("picgb_energies", self.handle, out, n)
+        d = {"E": out[0], "B": out[1]}
+        for i, s in enumerate(self.species):
+            d[s.name] = out[2 + i]
+        return d
+
+    def charge_residual(self) -> tuple[float, float]:
+        r = ctypes.c_double()
+        m = ctypes.c_double()
+        L.call("picgb_charge_residual", self.handle, ctypes.byref(r), ctypes.byref(m))
+        return r.value, m.value
+
+    def launch_count(self) -> int:
+        n = ctypes.c_uint64()
+        L.call("picgb_launch_count", self.handle, ctypes.byref(n))
+        return n.value
+
+    def profile(self, on: bool = True) -> None:
+        """Per-kernel CUDA-event timing on the launching stream; enabling resets the counters."""
+        L.call("picgb_profile_enable", self.handle, int(on))
+
+    def kernel_times(self) -> dict:
+        """{kernel class: (total device ms, launches)} since profiling was enabled."""
+        out = {}
+        for name, k in L.KERNEL_CLASSES.items():
+            ms = ctypes.c_double()
+            n = ctypes.c_uint64()
+            L.call("picgb_profile_read", self.handle, k, ctypes.byref(ms), ctypes.byref(n))
+            out[name] = (ms.value, n.value)
+        return out
+
+    def device_status(self, reset: bool = False) -> int:
+        b = ctypes.c_uint32()
+        L.call("picgb_device_status", self.handle, ctypes.byref(b), int(reset))
+        return b.value
