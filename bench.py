@@ -228,6 +228,7 @@ def run_gpu(args, wl, rank, world, local_rank):
     ms = ev0.elapsed_time(ev1)
     launches = sim.launch_count() - launches0
     kt = sim.kernel_times()
+    kinds = sim.deposit_kinds()
     sim.profile(False)
     if dist:
         t = torch.tensor([ms], device=f"cuda:{local_rank}")
@@ -248,7 +249,8 @@ def run_gpu(args, wl, rank, world, local_rank):
             "traffic": traffic, "algorithmic_bytes_per_launch": (B_PARTICLE * npart + 2 * B_PUSH_CELL * ncell) / 2,
             "mean_launch_ms": push_ms / max(push_n, 1),
             "step_frac_of_peak": round(value / world * (B_PARTICLE + B_CELL / (2 * wl["ppc"])) / (peak * 1e9), 4),
-            "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]}}
+            "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]},
+            "deposit_short_footprint_frac": round(kinds[0] / max(kinds[0] + kinds[1], 1), 4)}
 
     e2e = None
     if not args.no_e2e:

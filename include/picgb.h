@@ -260,6 +260,9 @@ extern "C"
     int picgb_profile_enable(picgb_sim* sim, int32_t on);
     /* Total device milliseconds and launch count of one kernel class; synchronises. */
     int picgb_profile_read(picgb_sim* sim, int32_t kernel_class, double* total_ms, uint64_t* launches);
+    /* Deposits done by the fused push while profiling: out[0] particles that stayed in their
+     * assignment cell along every axis (short footprint), out[1] the others.  Synchronises. */
+    int picgb_profile_deposit_kinds(picgb_sim* sim, uint64_t* out);
 
 #ifdef __cplusplus
 }

@@ -411,6 +411,8 @@ namespace orc
             ShapeFn<T>::baseArray(shape, p[0], sx);
             ShapeFn<T>::baseArray(shape, p[1], sy);
             ShapeFn<T>::baseArray(shape, p[2], sz);
+            // `result += value * weight` evaluated as one fused multiply-add, the
+            // contraction the reference's CUDA build (nvcc, -fmad=true) applies here
             T result_z = T(0.0);
             for(int z = begin; z <= end; ++z)
             {
@@ -421,11 +423,11 @@ namespace orc
                     for(int x = begin; x <= end; ++x)
                     {
                         size_t i = g.idx(cell[0] + shift[0] + x, cell[1] + shift[1] + y, cell[2] + shift[2] + z);
-                        result_x += F.c[comp][i] * sx[x - begin];
+                        result_x = std::fma(F.c[comp][i], sx[x - begin], result_x);
                     }
-                    result_y += result_x * sy[y - begin];
+                    result_y = std::fma(result_x, sy[y - begin], result_y);
                 }
-                result_z += result_y * sz[z - begin];
+                result_z = std::fma(result_y, sz[z - begin], result_z);
             }
             out[comp] = result_z;
         }

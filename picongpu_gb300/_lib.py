@@ -91,6 +91,7 @@ SIGNATURES = [
     ("picgb_device_status", c_int, [c_void_p, P(c_uint32), c_int]),
     ("picgb_profile_enable", c_int, [c_void_p, c_int]),
     ("picgb_profile_read", c_int, [c_void_p, c_int, P(c_double), P(c_uint64)]),
+    ("picgb_profile_deposit_kinds", c_int, [c_void_p, P(c_uint64)]),
 ]
 
 KERNEL_CLASSES = {"push": 0, "compact": 1, "yee_b": 2, "yee_e": 3, "deposit": 4, "add_current": 5}

@@ -58,6 +58,9 @@ def build(force: bool = False, debug: bool = False, verbose: bool = False) -> st
     ]
     if debug:
         common += ["-DPICGB_DEBUG"]
+    # tuning knobs, e.g. PICGB_NVCC_DEFINES="PICGB_PUSH_MIN_BLOCKS=2"
+    for d in os.environ.get("PICGB_NVCC_DEFINES", "").split():
+        common += [f"-D{d}"]
     if verbose:
         common += ["-Xptxas", "-v"]
 

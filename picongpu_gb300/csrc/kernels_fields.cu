@@ -28,12 +28,12 @@ namespace picgb
         float const* Ey = E + nc;
         float const* Ez = E + 2 * nc;
         float const ex = __ldg(Ex + i), ey = __ldg(Ey + i), ez = __ldg(Ez + i);
-        float const dFdx_y = fdv(fs(__ldg(Ey + ix), ey), g.dx);
-        float const dFdx_z = fdv(fs(__ldg(Ez + ix), ez), g.dx);
-        float const dFdy_x = fdv(fs(__ldg(Ex + iy), ex), g.dy);
-        float const dFdy_z = fdv(fs(__ldg(Ez + iy), ez), g.dy);
-        float const dFdz_x = fdv(fs(__ldg(Ex + iz), ex), g.dz);
-        float const dFdz_y = fdv(fs(__ldg(Ey + iz), ey), g.dz);
+        float const dFdx_y = divCell(fs(__ldg(Ey + ix), ey), 0, g);
+        float const dFdx_z = divCell(fs(__ldg(Ez + ix), ez), 0, g);
+        float const dFdy_x = divCell(fs(__ldg(Ex + iy), ex), 1, g);
+        float const dFdy_z = divCell(fs(__ldg(Ez + iy), ez), 1, g);
+        float const dFdz_x = divCell(fs(__ldg(Ex + iz), ex), 2, g);
+        float const dFdz_y = divCell(fs(__ldg(Ey + iz), ey), 2, g);
         float const c0 = fs(dFdy_z, dFdz_y), c1 = fs(dFdz_x, dFdx_z), c2 = fs(dFdx_y, dFdy_x);
         B[i] = fs(B[i], fm(fm(c0, 0.5f), g.dt));
         B[nc + i] = fs(B[nc + i], fm(fm(c1, 0.5f), g.dt));
@@ -60,12 +60,12 @@ namespace picgb
         float const* By = B + nc;
         float const* Bz = B + 2 * nc;
         float const bx = __ldg(Bx + i), by = __ldg(By + i), bz = __ldg(Bz + i);
-        float const dFdx_y = fdv(fs(by, __ldg(By + ix)), g.dx);
-        float const dFdx_z = fdv(fs(bz, __ldg(Bz + ix)), g.dx);
-        float const dFdy_x = fdv(fs(bx, __ldg(Bx + iy)), g.dy);
-        float const dFdy_z = fdv(fs(bz, __ldg(Bz + iy)), g.dy);
-        float const dFdz_x = fdv(fs(bx, __ldg(Bx + iz)), g.dz);
-        float const dFdz_y = fdv(fs(by, __ldg(By + iz)), g.dz);
+        float const dFdx_y = divCell(fs(by, __ldg(By + ix)), 0, g);
+        float const dFdx_z = divCell(fs(bz, __ldg(Bz + ix)), 0, g);
+        float const dFdy_x = divCell(fs(bx, __ldg(Bx + iy)), 1, g);
+        float const dFdy_z = divCell(fs(bz, __ldg(Bz + iy)), 1, g);
+        float const dFdz_x = divCell(fs(bx, __ldg(Bx + iz)), 2, g);
+        float const dFdz_y = divCell(fs(by, __ldg(By + iz)), 2, g);
         float const c2 = fm(g.c, g.c);
         float const cu[3] = {fs(dFdy_z, dFdz_y), fs(dFdz_x, dFdx_z), fs(dFdx_y, dFdy_x)};
 #pragma unroll

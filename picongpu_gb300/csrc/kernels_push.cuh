@@ -15,6 +15,16 @@
 namespace picgb
 {
     constexpr int kPushThreads = 256;
+#ifndef PICGB_PUSH_MIN_BLOCKS
+    // resident blocks per SM the push kernel's register budget is sized for
+#    define PICGB_PUSH_MIN_BLOCKS 3
+#endif
+
+    // Per-warp queue of deposit jobs of particles that cross a cell boundary
+    // (see kPush): kQueueCap jobs of kJobWords words for every warp.
+    constexpr int kQueueCap = 64;
+    constexpr int kJobWords = 9;
+    constexpr int kQueueWords = (kPushThreads / 32) * kQueueCap * kJobWords;
 
     template<typename SH, typename SC>
     struct TileGeom
@@ -27,8 +37,10 @@ namespace picgb
         static constexpr int JY = SC::SY + SH::jLo + SH::jHi;
         static constexpr int JZ = SC::SZ + SH::jLo + SH::jHi;
         static constexpr int JT = JX * JY * JZ;
-        static constexpr size_t pushSmem = sizeof(float) * (6 * GT + 3 * JT);
-        static constexpr size_t depositSmem = sizeof(float) * (3 * JT);
+        // E and B tiles, the J tile, the per-warp queues of deposit jobs
+        static constexpr int JWords = (PICGB_J_FIXED ? 6 : 3) * JT; // words of the J tile
+        static constexpr size_t pushSmem = sizeof(float) * (6 * GT + JWords) + sizeof(float) * kQueueWords;
+        static constexpr size_t depositSmem = sizeof(float) * JWords;
     };
 
     __device__ __forceinline__ void scCoords(int sc, GridParams const& g, int& x, int& y, int& z)
@@ -70,11 +82,13 @@ namespace picgb
         int oy,
         int oz,
         GridParams const& g,
-        size_t ncell)
+        size_t ncell,
+        JFixed const& f)
     {
         for(int t = threadIdx.x; t < TT; t += blockDim.x)
         {
-            float const vx = Js[t], vy = Js[TT + t], vz = Js[2 * TT + t];
+            float const vx = tileValue<TT>(Js, t, f), vy = tileValue<TT>(Js, TT + t, f),
+                        vz = tileValue<TT>(Js, 2 * TT + t, f);
             if(vx == 0.0f && vy == 0.0f && vz == 0.0f)
                 continue;
             int const tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
@@ -89,8 +103,65 @@ namespace picgb
         }
     }
 
+    __device__ __forceinline__ unsigned laneMaskLt() { return (1u << (threadIdx.x & 31)) - 1u; }
+
+    // Per-warp queue of deposit jobs: trajectory in the virtual coordinate
+    // system, charge, tile origin and packed status bits.
+    struct WarpQueue
+    {
+        float* w; // kQueueCap jobs, structure of arrays of kJobWords words
+
+        __device__ __forceinline__ void put(
+            int i,
+            float const p0[3],
+            float const p1[3],
+            float q,
+            int org,
+            int const st[3]) const
+        {
+#pragma unroll
+            for(int d = 0; d < 3; ++d)
+            {
+                w[d * kQueueCap + i] = p0[d];
+                w[(3 + d) * kQueueCap + i] = p1[d];
+            }
+            w[6 * kQueueCap + i] = q;
+            w[7 * kQueueCap + i] = __int_as_float(org);
+            w[8 * kQueueCap + i] = __int_as_float(st[0] | (st[1] << 3) | (st[2] << 6));
+        }
+
+        __device__ __forceinline__ void get(int i, float p0[3], float p1[3], float& q, int& org, int st[3]) const
+        {
+#pragma unroll
+            for(int d = 0; d < 3; ++d)
+            {
+                p0[d] = w[d * kQueueCap + i];
+                p1[d] = w[(3 + d) * kQueueCap + i];
+            }
+            q = w[6 * kQueueCap + i];
+            org = __float_as_int(w[7 * kQueueCap + i]);
+            int const pk = __float_as_int(w[8 * kQueueCap + i]);
+            st[0] = pk & 7;
+            st[1] = (pk >> 3) & 7;
+            st[2] = (pk >> 6) & 7;
+        }
+
+        __device__ __forceinline__ void move(int from, int to) const
+        {
+#pragma unroll
+            for(int r = 0; r < kJobWords; ++r)
+                w[r * kQueueCap + to] = w[r * kQueueCap + from];
+        }
+    };
+
+    // Fused push kernel.  Each thread pushes one particle per round; then the
+    // warp deposits at once the lanes whose particle stays in its assignment
+    // cell along every axis (the short fixed footprint, most particles), and
+    // queues the other lanes' jobs in its shared-memory queue, which it drains
+    // 32 at a time with the general footprint.  Without the split every warp
+    // would pay, through divergence, the largest footprint of any of its lanes.
     template<int SHAPE, int SX, int SY, int SZ>
-    __global__ void __launch_bounds__(kPushThreads) kPush(
+    __global__ void __launch_bounds__(kPushThreads, PICGB_PUSH_MIN_BLOCKS) kPush(
         SpeciesDev sp,
         float const* __restrict__ E,
         float const* __restrict__ B,
@@ -102,10 +173,14 @@ namespace picgb
         using SH = Shape<SHAPE>;
         using SC = SuperCell<SX, SY, SZ>;
         using TG = TileGeom<SH, SC>;
-        extern __shared__ float smem[];
+        using ES = Esirkepov<SH>;
+        using Tile = TileJ<TG::JX, TG::JY, TG::JT>;
+        extern __shared__ __align__(16) float smem[];
         float* const Es = smem;
         float* const Bs = smem + 3 * TG::GT;
         float* const Js = smem + 6 * TG::GT;
+        int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        WarpQueue const queue{smem + 6 * TG::GT + TG::JWords + warp * kQueueCap * kJobWords};
         __shared__ unsigned s_nhole;
 
         int const sc = blockIdx.x;
@@ -129,132 +204,168 @@ namespace picgb
             loadTile<TG::GX, TG::GY, TG::GT>(Bs, B, ox - SH::gLo, oy - SH::gLo, oz - SH::gLo, g, ncell);
         }
         if(pp.deposit)
-            for(int t = threadIdx.x; t < 3 * TG::JT; t += blockDim.x)
+            for(int t = threadIdx.x; t < TG::JWords; t += blockDim.x)
                 Js[t] = 0.0f;
         __syncthreads();
 
-        float const cs[3] = {g.dx, g.dy, g.dz};
         size_t const base = size_t(sc) * sp.cap;
-        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        int queued = 0; // jobs in this warp's queue (warp-uniform)
+        for(uint32_t c0 = 0; c0 < n; c0 += kPushThreads)
         {
-            size_t const slot = base + k;
-            float pos[3] = {sp.px[slot], sp.py[slot], sp.pz[slot]};
-            float mom[3] = {sp.ux[slot], sp.uy[slot], sp.uz[slot]};
-            float const w = sp.w[slot];
-            int const lc = sp.lcell[slot];
-            int const lx = lc % SX, ly = (lc / SX) % SY, lz = lc / (SX * SY);
-            float const mass = fm(pp.mass, w);
-            float const charge = fm(pp.charge, w);
-            float vel[3];
-            if(useBoris)
+            uint32_t const k = c0 + threadIdx.x;
+            int kind = -1; // 0: stays in its assignment cell, 1: crosses a cell boundary
+            float p0[3], p1[3], charge = 0.0f;
+            int stat[3], org = 0;
+            if(k < n)
             {
-                float Ev[3], Bv[3];
-                // Yee positions (fields/YeeCell.hpp:70-131)
-                Bv[0] = gatherComponent<SH, TG::GX, TG::GY>(Bs, lx, ly, lz, pos[0], pos[1], pos[2], 0.f, .5f, .5f);
-                Bv[1] = gatherComponent<SH, TG::GX, TG::GY>(
-                    Bs + TG::GT, lx, ly, lz, pos[0], pos[1], pos[2], .5f, 0.f, .5f);
-                Bv[2] = gatherComponent<SH, TG::GX, TG::GY>(
-                    Bs + 2 * TG::GT, lx, ly, lz, pos[0], pos[1], pos[2], .5f, .5f, 0.f);
-                Ev[0] = gatherComponent<SH, TG::GX, TG::GY>(Es, lx, ly, lz, pos[0], pos[1], pos[2], .5f, 0.f, 0.f);
-                Ev[1] = gatherComponent<SH, TG::GX, TG::GY>(
-                    Es + TG::GT, lx, ly, lz, pos[0], pos[1], pos[2], 0.f, .5f, 0.f);
-                Ev[2] = gatherComponent<SH, TG::GX, TG::GY>(
-                    Es + 2 * TG::GT, lx, ly, lz, pos[0], pos[1], pos[2], 0.f, 0.f, .5f);
-                boris(charge, mass, Ev, Bv, pp.dt, pp.c2, pp.rc2, mom, vel);
-            }
-            else
-                velocity(mom, mass, pp.rc2, vel);
-#pragma unroll
-            for(int d = 0; d < 3; ++d)
-                pos[d] = fa(pos[d], fdv(fm(vel[d], pp.dt), cs[d]));
-            int nlc = lc;
-            int mv[3], dir[3];
-            bool const leave = moveParticle<SC>(pos, nlc, mv, dir);
-            if(pp.deposit)
-            {
-                int const cellRel[3] = {lx + mv[0], ly + mv[1], lz + mv[2]};
-                if(!Esirkepov<SH, TG::JX, TG::JY>::deposit(
-                       Js,
-                       Js + TG::JT,
-                       Js + 2 * TG::JT,
-                       cellRel,
-                       pos,
-                       vel,
-                       charge,
-                       g,
-                       pp.invVdt))
-                    atomicOr(status, ST_BAD_CELL);
-            }
-            if(!leave)
-            {
-                sp.px[slot] = pos[0];
-                sp.py[slot] = pos[1];
-                sp.pz[slot] = pos[2];
-                sp.ux[slot] = mom[0];
-                sp.uy[slot] = mom[1];
-                sp.uz[slot] = mom[2];
-                if(nlc != lc)
-                    sp.lcell[slot] = uint16_t(nlc);
-            }
-            else
-            {
-                int const dx = wrapi(scx + dir[0], g.nscx), dy = wrapi(scy + dir[1], g.nscy),
-                          dz = wrapi(scz + dir[2], g.nscz);
-                int const dsc = dx + g.nscx * (dy + g.nscy * dz);
-                uint32_t const id = sp.id ? sp.id[slot] : 0u;
-                uint32_t const s = atomicAdd(sp.tail + dsc, 1u);
-                if(s < sp.cap)
+                size_t const slot = base + k;
+                float pos[3] = {sp.px[slot], sp.py[slot], sp.pz[slot]};
+                float mom[3] = {sp.ux[slot], sp.uy[slot], sp.uz[slot]};
+                float const w = sp.w[slot];
+                int const lc = sp.lcell[slot];
+                int const lx = lc % SX, ly = (lc / SX) % SY, lz = lc / (SX * SY);
+                float const mass = fm(pp.mass, w);
+                charge = fm(pp.charge, w);
+                float vel[3];
+                if(useBoris)
                 {
-                    size_t const d = size_t(dsc) * sp.cap + s;
-                    sp.px[d] = pos[0];
-                    sp.py[d] = pos[1];
-                    sp.pz[d] = pos[2];
-                    sp.ux[d] = mom[0];
-                    sp.uy[d] = mom[1];
-                    sp.uz[d] = mom[2];
-                    sp.w[d] = w;
-                    sp.lcell[d] = uint16_t(nlc);
-                    if(sp.id)
-                        sp.id[d] = id;
+                    float Ev[3], Bv[3];
+                    GatherWeights<SH> gw;
+                    gw.compute(pos);
+                    // Yee positions (fields/YeeCell.hpp:70-131): E_x (1/2,0,0) ... B_x (0,1/2,1/2) ...
+                    Bv[0] = gw.template gather<TG::GX, TG::GY, 0, 1, 1>(Bs, lx, ly, lz);
+                    Bv[1] = gw.template gather<TG::GX, TG::GY, 1, 0, 1>(Bs + TG::GT, lx, ly, lz);
+                    Bv[2] = gw.template gather<TG::GX, TG::GY, 1, 1, 0>(Bs + 2 * TG::GT, lx, ly, lz);
+                    Ev[0] = gw.template gather<TG::GX, TG::GY, 1, 0, 0>(Es, lx, ly, lz);
+                    Ev[1] = gw.template gather<TG::GX, TG::GY, 0, 1, 0>(Es + TG::GT, lx, ly, lz);
+                    Ev[2] = gw.template gather<TG::GX, TG::GY, 0, 0, 1>(Es + 2 * TG::GT, lx, ly, lz);
+                    boris(charge, mass, Ev, Bv, pp.dt, pp.c2, pp.rc2, mom, vel);
+                }
+                else
+                    velocity(mom, mass, pp.rc2, vel);
+#pragma unroll
+                for(int d = 0; d < 3; ++d)
+                    pos[d] = fa(pos[d], divCell(fm(vel[d], pp.dt), d, g));
+                int nlc = lc;
+                int mv[3], dir[3];
+                bool const leave = moveParticle<SC>(pos, nlc, mv, dir);
+                if(pp.deposit)
+                {
+                    int gs[3];
+                    if(!ES::prepare(pos, vel, g, p0, p1, gs, stat))
+                        atomicOr(status, ST_BAD_CELL);
+                    else
+                    {
+                        // tile index of the Esirkepov origin; the new cell lies in [-1, S]
+                        org = (lx + mv[0] + gs[0] + SH::jLo)
+                            + TG::JX * ((ly + mv[1] + gs[1] + SH::jLo) + TG::JY * (lz + mv[2] + gs[2] + SH::jLo));
+                        kind = (stat[0] == ES::kInCell && stat[1] == ES::kInCell && stat[2] == ES::kInCell) ? 0 : 1;
+                    }
+                }
+                if(!leave)
+                {
+                    sp.px[slot] = pos[0];
+                    sp.py[slot] = pos[1];
+                    sp.pz[slot] = pos[2];
+                    sp.ux[slot] = mom[0];
+                    sp.uy[slot] = mom[1];
+                    sp.uz[slot] = mom[2];
+                    if(nlc != lc)
+                        sp.lcell[slot] = uint16_t(nlc);
                 }
                 else
                 {
-                    uint32_t const q = atomicAdd(sp.sp_count, 1u);
-                    if(q < sp.spill_cap)
+                    int const dx = wrapi(scx + dir[0], g.nscx), dy = wrapi(scy + dir[1], g.nscy),
+                              dz = wrapi(scz + dir[2], g.nscz);
+                    int const dsc = dx + g.nscx * (dy + g.nscy * dz);
+                    uint32_t const id = sp.id ? sp.id[slot] : 0u;
+                    uint32_t const s = atomicAdd(sp.tail + dsc, 1u);
+                    if(s < sp.cap)
                     {
-                        float* a = sp.sp_attr;
-                        size_t const C = sp.spill_cap;
-                        a[q] = pos[0];
-                        a[C + q] = pos[1];
-                        a[2 * C + q] = pos[2];
-                        a[3 * C + q] = mom[0];
-                        a[4 * C + q] = mom[1];
-                        a[5 * C + q] = mom[2];
-                        a[6 * C + q] = w;
-                        sp.sp_sc[q] = dsc;
-                        sp.sp_lcell[q] = uint16_t(nlc);
-                        sp.sp_id[q] = id;
-                        atomicOr(status, ST_OVERFLOW);
+                        size_t const d = size_t(dsc) * sp.cap + s;
+                        sp.px[d] = pos[0];
+                        sp.py[d] = pos[1];
+                        sp.pz[d] = pos[2];
+                        sp.ux[d] = mom[0];
+                        sp.uy[d] = mom[1];
+                        sp.uz[d] = mom[2];
+                        sp.w[d] = w;
+                        sp.lcell[d] = uint16_t(nlc);
+                        if(sp.id)
+                            sp.id[d] = id;
                     }
                     else
-                        atomicOr(status, ST_OVERFLOW | ST_LOST);
+                    {
+                        uint32_t const q = atomicAdd(sp.sp_count, 1u);
+                        if(q < sp.spill_cap)
+                        {
+                            float* a = sp.sp_attr;
+                            size_t const C = sp.spill_cap;
+                            a[q] = pos[0];
+                            a[C + q] = pos[1];
+                            a[2 * C + q] = pos[2];
+                            a[3 * C + q] = mom[0];
+                            a[4 * C + q] = mom[1];
+                            a[5 * C + q] = mom[2];
+                            a[6 * C + q] = w;
+                            sp.sp_sc[q] = dsc;
+                            sp.sp_lcell[q] = uint16_t(nlc);
+                            sp.sp_id[q] = id;
+                            atomicOr(status, ST_OVERFLOW);
+                        }
+                        else
+                            atomicOr(status, ST_OVERFLOW | ST_LOST);
+                    }
+                    uint32_t const h = atomicAdd(&s_nhole, 1u);
+                    sp.holes[base + h] = uint16_t(k);
                 }
-                uint32_t const h = atomicAdd(&s_nhole, 1u);
-                sp.holes[base + h] = uint16_t(k);
+            }
+            if(!pp.deposit)
+                continue;
+            // particles that stay in their cell: deposit now with the short footprint
+            if(kind == 0)
+                ES::template run<false>(Tile{Js, org, pp.jf}, p0, p1, stat, charge, g, pp.invVdt);
+            // the others: into the warp's queue, drained 32 at a time
+            unsigned const crossing = __ballot_sync(0xffffffffu, kind == 1);
+            if(pp.kindCount)
+            {
+                unsigned const shortFp = __ballot_sync(0xffffffffu, kind == 0);
+                if(lane == 0)
+                {
+                    atomicAdd(pp.kindCount, (unsigned long long) __popc(shortFp));
+                    atomicAdd(pp.kindCount + 1, (unsigned long long) __popc(crossing));
+                }
+            }
+            if(kind == 1)
+                queue.put(queued + __popc(crossing & laneMaskLt()), p0, p1, charge, org, stat);
+            queued += __popc(crossing);
+            __syncwarp();
+            if(queued >= 32)
+            {
+                float q0[3], q1[3], qc;
+                int qo, qs[3];
+                queue.get(lane, q0, q1, qc, qo, qs);
+                ES::template run<true>(Tile{Js, qo, pp.jf}, q0, q1, qs, qc, g, pp.invVdt);
+                __syncwarp();
+                if(lane < queued - 32)
+                    queue.move(32 + lane, lane);
+                queued -= 32;
+                __syncwarp();
             }
         }
-        __syncthreads();
+        // the jobs still queued
+        if(pp.deposit && lane < queued)
+        {
+            float q0[3], q1[3], qc;
+            int qo, qs[3];
+            queue.get(lane, q0, q1, qc, qo, qs);
+            ES::template run<true>(Tile{Js, qo, pp.jf}, q0, q1, qs, qc, g, pp.invVdt);
+        }
+        __syncthreads(); // every hole is recorded and every deposit done
         if(threadIdx.x == 0)
             sp.nhole[sc] = s_nhole;
         if(pp.deposit)
-            flushTile<TG::JX, TG::JY, TG::JT>(
-                Js,
-                J,
-                ox - SH::jLo,
-                oy - SH::jLo,
-                oz - SH::jLo,
-                g,
-                ncell);
+            flushTile<TG::JX, TG::JY, TG::JT>(Js, J, ox - SH::jLo, oy - SH::jLo, oz - SH::jLo, g, ncell, pp.jf);
     }
 
     // Deposit-only kernel over the sorted particles (the reference's separate
@@ -266,8 +377,8 @@ namespace picgb
         using SH = Shape<SHAPE>;
         using SC = SuperCell<SX, SY, SZ>;
         using TG = TileGeom<SH, SC>;
-        extern __shared__ float smem[];
-        float* const Js = smem;
+        extern __shared__ __align__(16) float jsm[];
+        float* const Js = jsm;
         int const sc = blockIdx.x;
         uint32_t const n = sp.count[sc];
         if(n == 0)
@@ -275,7 +386,7 @@ namespace picgb
         int scx, scy, scz;
         scCoords(sc, g, scx, scy, scz);
         size_t const ncell = size_t(g.nx) * g.ny * g.nz;
-        for(int t = threadIdx.x; t < 3 * TG::JT; t += blockDim.x)
+        for(int t = threadIdx.x; t < TG::JWords; t += blockDim.x)
             Js[t] = 0.0f;
         __syncthreads();
         size_t const base = size_t(sc) * sp.cap;
@@ -289,17 +400,19 @@ namespace picgb
             int const cellRel[3] = {lc % SX, (lc / SX) % SY, lc / (SX * SY)};
             float vel[3];
             velocity(mom, fm(pp.mass, w), pp.rc2, vel);
-            if(!Esirkepov<SH, TG::JX, TG::JY>::deposit(
-                   Js,
-                   Js + TG::JT,
-                   Js + 2 * TG::JT,
-                   cellRel,
-                   pos,
-                   vel,
-                   fm(pp.charge, w),
-                   g,
-                   pp.invVdt))
+            float p0[3], p1[3];
+            int gs[3], stat[3];
+            if(!Esirkepov<SH>::prepare(pos, vel, g, p0, p1, gs, stat))
+            {
                 atomicOr(status, ST_BAD_CELL);
+                continue;
+            }
+            TileJ<TG::JX, TG::JY, TG::JT> const acc{
+                Js,
+                (cellRel[0] + gs[0] + SH::jLo)
+                    + TG::JX * ((cellRel[1] + gs[1] + SH::jLo) + TG::JY * (cellRel[2] + gs[2] + SH::jLo)),
+                pp.jf};
+            Esirkepov<SH>::template run<true>(acc, p0, p1, stat, fm(pp.charge, w), g, pp.invVdt);
         }
         __syncthreads();
         flushTile<TG::JX, TG::JY, TG::JT>(
@@ -309,7 +422,8 @@ namespace picgb
             scy * SY - SH::jLo,
             scz * SZ - SH::jLo,
             g,
-            ncell);
+            ncell,
+            pp.jf);
     }
 
     // Charge density at the cell origin with ChargeAssignment

@@ -76,6 +76,7 @@ namespace
         SpeciesDev dev{};
         int nsc = 0;
         bool allocated = false;
+        float wmax = 0.0f; // largest |weighting| (bounds a single J contribution)
 
         void freeAll()
         {
@@ -136,6 +137,7 @@ struct picgb_sim
     unsigned* hostStatus = nullptr; // pinned
     double* energy = nullptr; // device accumulators
     unsigned* maxBits = nullptr; // device: residual max, rho max
+    unsigned long long* kindCount = nullptr; // device: deposits by footprint (profiling)
     cudaStream_t stream = nullptr;
     bool ownStream = false;
     uint64_t launches = 0;
@@ -172,6 +174,27 @@ struct picgb_sim
         p.invVdt = 1.0f / vdt;
         p.pusher = s.cfg.pusher;
         p.deposit = deposit ? 1 : 0;
+        p.kindCount = prof ? kindCount : nullptr;
+        // Fixed-point format of the J tile (kernels built with PICGB_J_FIXED).  A
+        // deposited value is a running sum acc_k = sum DS * tmp with
+        // |tmp| <= |q w| d / (V dt) and sum |DS| <= 2, so |acc| <= 2 |q| wmax dmax / (V dt)
+        // =: vmax.  A tile node receives at most one value per particle of its
+        // supercell (< 2^cb).  With k = 31 - cb and vmax * 2^s <= 2^(61 - 2 cb) the sums
+        // of the high and of the low parts stay below 2^30 + 2^(cb - 1).
+        int cb = 1;
+        while((1u << cb) < s.dev.cap)
+            ++cb;
+        double const dmax = std::max(std::max(double(cfg.dx), double(cfg.dy)), double(cfg.dz));
+        double const vmax = 2.0 * std::fabs(double(s.cfg.charge)) * double(s.wmax) * dmax * double(p.invVdt);
+        int e = 0;
+        if(vmax > 0.0 && std::isfinite(vmax))
+            std::frexp(vmax, &e); // vmax < 2^e
+        int const sExp = std::min(std::max(61 - 2 * cb - e, -126), 126);
+        p.jf.k = 31 - cb;
+        p.jf.scale = std::ldexp(1.0f, sExp);
+        p.jf.invScale = std::ldexp(1.0f, -sExp);
+        p.jf.hiStep = std::ldexp(1.0f, -p.jf.k);
+        p.jf.hiUnit = std::ldexp(1.0f, p.jf.k);
         return p;
     }
 };
@@ -525,6 +548,16 @@ extern "C"
         s->g.dt = cfg->dt;
         s->g.c = cfg->c;
         s->g.eps0 = cfg->eps0;
+        // cell sizes that are powers of two divide exactly as a multiplication by their reciprocal
+        auto pow2 = [](float v)
+        {
+            int e = 0;
+            return std::frexp(v, &e) == 0.5f;
+        };
+        s->g.rd[0] = 1.0f / cfg->dx;
+        s->g.rd[1] = 1.0f / cfg->dy;
+        s->g.rd[2] = 1.0f / cfg->dz;
+        s->g.recipExact = (pow2(cfg->dx) && pow2(cfg->dy) && pow2(cfg->dz)) ? 1 : 0;
         s->nsc = s->g.nscx * s->g.nscy * s->g.nscz;
         s->ncell = size_t(cfg->nx) * cfg->ny * cfg->nz;
         CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -536,6 +569,8 @@ extern "C"
         CUDA_TRY(dalloc(s->status, 1));
         CUDA_TRY(dalloc(s->energy, 64));
         CUDA_TRY(dalloc(s->maxBits, 2));
+        CUDA_TRY(dalloc(s->kindCount, 2));
+        CUDA_TRY(cudaMemsetAsync(s->kindCount, 0, 2 * sizeof(unsigned long long), s->stream));
         CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&s->hostStatus), sizeof(unsigned)));
         CUDA_TRY(cudaMemsetAsync(s->E, 0, sizeof(float) * 3 * s->ncell, s->stream));
         CUDA_TRY(cudaMemsetAsync(s->B, 0, sizeof(float) * 3 * s->ncell, s->stream));
@@ -570,6 +605,7 @@ extern "C"
         dfree(s->status);
         dfree(s->energy);
         dfree(s->maxBits);
+        dfree(s->kindCount);
         if(s->hostStatus)
             cudaFreeHost(s->hostStatus);
         profFlush(s);
@@ -653,6 +689,12 @@ extern "C"
             return fail(PICGB_ERR_INVALID, "species '%s': a particle has an out-of-range supercell, cell index or in-cell position",
                         sp.name.c_str());
         uint32_t const mx = cnt.empty() ? 0u : *std::max_element(cnt.begin(), cnt.end());
+        float wmax = 0.0f;
+        for(uint64_t i = 0; i < n; ++i)
+            wmax = std::max(wmax, std::fabs(h->w[i]));
+        if(!std::isfinite(wmax))
+            return fail(PICGB_ERR_INVALID, "species '%s': a weighting is not finite", sp.name.c_str());
+        sp.wmax = wmax;
         uint32_t cap = sp.cfg.capacity;
         if(cap == 0)
             cap = uint32_t(std::max<uint64_t>(32, uint64_t(std::ceil(1.25 * mx))));
@@ -706,6 +748,7 @@ extern "C"
         InitParams ip{};
         ip.ppc = init->ppc;
         ip.weight = init->density * s->cellVolume() / float(init->ppc);
+        sp.wmax = std::fabs(ip.weight);
         ip.mass = sp.cfg.mass;
         ip.c = s->cfg.c;
         ip.u_th = init->u_th;
@@ -1146,6 +1189,7 @@ extern "C"
             s->profMs[i] = 0.0;
             s->profN[i] = 0;
         }
+        CUDA_TRY(cudaMemsetAsync(s->kindCount, 0, 2 * sizeof(unsigned long long), s->stream));
         return PICGB_OK;
     }
 
@@ -1161,6 +1205,20 @@ extern "C"
             *ms = s->profMs[cls];
         if(n)
             *n = s->profN[cls];
+        return PICGB_OK;
+    }
+
+    int picgb_profile_deposit_kinds(picgb_sim* s, uint64_t* out)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(!out)
+            return fail(PICGB_ERR_INVALID, "null argument");
+        unsigned long long h[2];
+        CUDA_TRY(cudaMemcpyAsync(h, s->kindCount, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        out[0] = h[0];
+        out[1] = h[1];
         return PICGB_OK;
     }
 

@@ -2,11 +2,15 @@
 // Boris push, moveParticle and the Esirkepov deposit.
 //
 // Operations that decide particle positions (shapes, gather, push, move) use
-// the explicit round-to-nearest intrinsics (__fmul_rn, __fadd_rn, ...) so the
-// compiler cannot contract them into FMAs: the result is bit-identical to a
-// scalar IEEE evaluation in the reference's association order, which is what
-// makes the per-cell particle counts after a step bit-exact.
+// the explicit round-to-nearest intrinsics (__fmul_rn, __fadd_rn, __fmaf_rn,
+// ...) so the compiler can neither contract nor reorder them: the result is
+// bit-identical to the CPU oracle, which evaluates the same operations in the
+// reference's association order (fused multiply-adds exactly where the gather
+// accumulates `result += value * weight`).  That is what makes positions,
+// momenta and the per-cell particle counts after a step bit-exact.
 #pragma once
+
+#include "picgb_internal.hpp"
 
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -35,7 +39,7 @@ namespace picgb
         // gather margins (FieldToParticleInterpolation.hpp:43-44)
         static constexpr int gLo = supp / 2;
         static constexpr int gHi = (supp + 1) / 2;
-        // deposit node range relative to a cell in [-1, S] (particle may have
+        // deposit node range relative to a cell in [-1, S] (a particle may have
         // left the supercell by one cell): gridShift in [-1, even ? 0 : 1],
         // node offset in [caBegin, caEnd]
         static constexpr int jLo = 2 - caBegin;
@@ -166,7 +170,20 @@ namespace picgb
         int nx, ny, nz; // cells
         int nscx, nscy, nscz; // supercells
         float dx, dy, dz, dt, c, eps0;
+        float rd[3]; // 1/dx, 1/dy, 1/dz
+        int recipExact; // all cell sizes are powers of two: x / d == x * (1/d) exactly
     };
+
+    // x / cellSize[d]: a multiplication by the exact reciprocal when the cell size is a
+    // power of two (bit-identical to the IEEE division), the division otherwise.
+    __device__ __forceinline__ float divCell(float x, int d, GridParams const& g)
+    {
+        if(g.recipExact)
+            return fm(x, g.rd[d]);
+        return fdv(x, d == 0 ? g.dx : (d == 1 ? g.dy : g.dz));
+    }
+
+    __device__ __forceinline__ float frcp(float x) { return __frcp_rn(x); } // == 1.0f / x, correctly rounded
 
     __device__ __forceinline__ int wrapi(int i, int n)
     {
@@ -175,10 +192,97 @@ namespace picgb
     }
 
     // ------------------------------------------------------------ gather
-    // FieldToParticleInterpolation (algorithms/FieldToParticleInterpolation.hpp:97-124),
-    // ShiftCoordinateSystem (ShiftCoordinateSystem.hpp:54-79), AssignedTrilinearInterpolation
-    // (AssignedTrilinearInterpolation.hpp:54-86), reading a shared-memory tile whose
-    // origin is the supercell origin minus Shape::gLo in every direction.
+    // AssignedTrilinearInterpolation::interpolate (algorithms/AssignedTrilinearInterpolation.hpp:54-86):
+    // z-y-x nested weighted sums over the support, each accumulation one fused
+    // multiply-add (the contraction the reference's CUDA build applies to
+    // `result += value * weight`; the oracle uses std::fma at the same places).
+    // The tile origin is the supercell origin minus Shape::gLo in every direction.
+    template<typename SH, int TX, int TY>
+    __device__ __forceinline__ float interpolate(
+        float const* __restrict__ tile,
+        int lx,
+        int ly,
+        int lz,
+        int shx,
+        int shy,
+        int shz,
+        float const* sx,
+        float const* sy,
+        float const* sz)
+    {
+        constexpr int S = SH::supp;
+        int const bx = lx + SH::gLo + shx + SH::osBegin;
+        int const by = ly + SH::gLo + shy + SH::osBegin;
+        int const bz = lz + SH::gLo + shz + SH::osBegin;
+        float const* base = tile + (bx + TX * (by + TY * bz));
+        float rz = 0.0f;
+#pragma unroll
+        for(int z = 0; z < S; ++z)
+        {
+            float ry = 0.0f;
+#pragma unroll
+            for(int y = 0; y < S; ++y)
+            {
+                float rx = 0.0f;
+                float const* row = base + TX * (y + TY * z);
+#pragma unroll
+                for(int x = 0; x < S; ++x)
+                    rx = __fmaf_rn(row[x], sx[x], rx);
+                ry = __fmaf_rn(rx, sy[y], ry);
+            }
+            rz = __fmaf_rn(ry, sz[z], rz);
+        }
+        return rz;
+    }
+
+    // ShiftCoordinateSystem (algorithms/ShiftCoordinateSystem.hpp:54-79) and the
+    // on-support shape array for the two staggering offsets a Yee component can
+    // have along an axis (0 and 1/2, fields/YeeCell.hpp:70-131).  The six
+    // components of E and B reuse these six weight arrays.
+    template<typename SH>
+    struct GatherWeights
+    {
+        int sh[2][3];
+        float w[2][3][SH::supp];
+
+        __device__ __forceinline__ void compute(float const pos[3])
+        {
+#pragma unroll
+            for(int a = 0; a < 2; ++a)
+#pragma unroll
+                for(int d = 0; d < 3; ++d)
+                {
+                    float const v = fs(fs(pos[d], a ? 0.5f : 0.0f), 0.5f);
+                    int s;
+                    if constexpr(SH::even)
+                        s = v >= -0.5f ? 0 : -1;
+                    else
+                        s = v >= 0.0f ? 1 : 0;
+                    sh[a][d] = s;
+                    SH::base(fa(fs(v, float(s)), 0.5f), w[a][d]);
+                }
+        }
+
+        // ax, ay, az: staggering (0 or 1) of the component along x, y, z
+        template<int TX, int TY, int ax, int ay, int az>
+        __device__ __forceinline__ float gather(float const* __restrict__ tile, int lx, int ly, int lz) const
+        {
+            return interpolate<SH, TX, TY>(
+                tile,
+                lx,
+                ly,
+                lz,
+                sh[ax][0],
+                sh[ay][1],
+                sh[az][2],
+                w[ax][0],
+                w[ay][1],
+                w[az][2]);
+        }
+    };
+
+    // FieldToParticleInterpolation (algorithms/FieldToParticleInterpolation.hpp:97-124) of one
+    // component with field position (fx, fy, fz).
     template<typename SH, int TX, int TY>
     __device__ __forceinline__ float gatherComponent(
         float const* __restrict__ tile,
@@ -211,27 +315,7 @@ namespace picgb
         SH::base(p[0], sx);
         SH::base(p[1], sy);
         SH::base(p[2], sz);
-        int const bx = lx + SH::gLo + shift[0] + SH::osBegin;
-        int const by = ly + SH::gLo + shift[1] + SH::osBegin;
-        int const bz = lz + SH::gLo + shift[2] + SH::osBegin;
-        float rz = 0.0f;
-#pragma unroll
-        for(int z = 0; z < S; ++z)
-        {
-            float ry = 0.0f;
-#pragma unroll
-            for(int y = 0; y < S; ++y)
-            {
-                float rx = 0.0f;
-                float const* row = tile + (bx + TX * ((by + y) + TY * (bz + z)));
-#pragma unroll
-                for(int x = 0; x < S; ++x)
-                    rx = fa(rx, fm(row[x], sx[x]));
-                ry = fa(ry, fm(rx, sy[y]));
-            }
-            rz = fa(rz, fm(ry, sz[z]));
-        }
-        return rz;
+        return interpolate<SH, TX, TY>(tile, lx, ly, lz, shift[0], shift[1], shift[2], sx, sy, sz);
     }
 
     // ------------------------------------------------------------ push
@@ -242,7 +326,7 @@ namespace picgb
     {
         float const m0_2 = fm(mass, mass);
         float const fMom2 = l2n2(mom[0], mom[1], mom[2]);
-        float const t = fdv(1.0f, fsq(fa(m0_2, fm(fMom2, rc2))));
+        float const t = frcp(fsq(fa(m0_2, fm(fMom2, rc2))));
 #pragma unroll
         for(int d = 0; d < 3; ++d)
             vel[d] = fm(t, mom[d]);
@@ -267,15 +351,15 @@ namespace picgb
         for(int d = 0; d < 3; ++d)
             mm[d] = fa(mom[d], fm(fm(hq, E[d]), dt));
         // Gamma (algorithms/Gamma.hpp:30-37)
-        float const m2_c2_reci = fdv(1.0f, fm(fm(mass, mass), c2));
+        float const m2_c2_reci = frcp(fm(fm(mass, mass), c2));
         float const gamma = fsq(fa(1.0f, fm(l2n2(mm[0], mm[1], mm[2]), m2_c2_reci)));
-        float const gamma_reci = fdv(1.0f, gamma);
+        float const gamma_reci = frcp(gamma);
         float const hqm = fm(0.5f, QoM);
         float t[3];
 #pragma unroll
         for(int d = 0; d < 3; ++d)
             t[d] = fm(fm(fm(hqm, B[d]), gamma_reci), dt);
-        float const sf = fdv(1.0f, fa(1.0f, l2n2(t[0], t[1], t[2])));
+        float const sf = frcp(fa(1.0f, l2n2(t[0], t[1], t[2])));
         float s[3];
 #pragma unroll
         for(int d = 0; d < 3; ++d)
@@ -332,93 +416,113 @@ namespace picgb
         return leave;
     }
 
+    // ------------------------------------------------------------ J accumulators
+    // Maps the rotated axes (i, j, k) of current component C to real axes:
+    // J_x: i->y, j->z, k->x; J_y: i->z, j->x, k->y; J_z: i->x, j->y, k->z
+    // (rotateOrigin / PermutatedFieldValueAccess, Esirkepov.hpp:112-129).
+    template<int C>
+    __device__ __forceinline__ void rotToReal(int ri, int rj, int rk, int& x, int& y, int& z)
+    {
+        if constexpr(C == 0)
+        {
+            x = rk;
+            y = ri;
+            z = rj;
+        }
+        else if constexpr(C == 1)
+        {
+            x = rj;
+            y = rk;
+            z = ri;
+        }
+        else
+        {
+            x = ri;
+            y = rj;
+            z = rk;
+        }
+    }
+
+#ifndef PICGB_J_FIXED
+    // 1: the shared-memory J tile holds 32-bit fixed-point high and low parts
+    // added with native fire-and-forget integer atomics; 0: floats added with
+    // atomicAdd, which for shared memory is a load/compare-and-swap loop on this
+    // target that retries whenever another warp updated the node in between
+    // (measured on the 256^3 two-stream workload: 30.9 vs 39.7 ms per launch)
+#    define PICGB_J_FIXED 1
+#endif
+
+    // Shared-memory J tile of one supercell: [3][TT] floats, or [2][3][TT] ints in fixed point.
+    template<int TX, int TY, int TT>
+    struct TileJ
+    {
+        float* J;
+        int base; // tile index of the particle's Esirkepov origin (cell + gridShift)
+        JFixed f;
+
+        template<int C>
+        __device__ __forceinline__ void add(int ri, int rj, int rk, float v) const
+        {
+            int x, y, z;
+            rotToReal<C>(ri, rj, rk, x, y, z);
+            int const idx = C * TT + base + x + TX * (y + TY * z);
+#if PICGB_J_FIXED
+            int* hi = reinterpret_cast<int*>(J);
+            float const vs = fm(v, f.scale); // exact: power of two
+            float const a = rintf(fm(vs, f.hiStep));
+            float const r = __fmaf_rn(-a, f.hiUnit, vs); // exact (Sterbenz)
+            atomicAdd(hi + idx, __float2int_rn(a));
+            atomicAdd(hi + 3 * TT + idx, __float2int_rn(r));
+#else
+            atomicAdd(J + idx, v);
+#endif
+        }
+    };
+
+    // Value of tile node t of component c (the flush of the tile).
+    template<int TT>
+    __device__ __forceinline__ float tileValue(float const* J, int i, JFixed const& f)
+    {
+#if PICGB_J_FIXED
+        int const* hi = reinterpret_cast<int const*>(J);
+        long long const t = (static_cast<long long>(hi[i]) << f.k) + hi[3 * TT + i];
+        return fm(__ll2float_rn(t), f.invScale);
+#else
+        (void) f;
+        return J[i];
+#endif
+    }
+
     // ------------------------------------------------------------ Esirkepov
-    // Deposits into a shared-memory J tile (3 arrays of TX*TY*TZ floats) whose
-    // origin is the supercell origin minus Shape::jLo per axis.  cellRel = new
-    // cell of the particle relative to the supercell origin (in [-1, S]).
     // Esirkepov::operator() (fields/currentDeposition/Esirkepov/Esirkepov.hpp:62-134),
     // cptCurrent1D (:147-242), relayPoint (relayPoint.hpp:48-64).
-    template<typename SH, int TX, int TY>
+    template<typename SH>
     struct Esirkepov
     {
         static constexpr int S = SH::supp;
         static constexpr int begin = SH::caBegin;
         static constexpr int end = SH::caEnd;
 
-        // one rotated 1D current: axes (i,j,k) of the rotated frame map to the
-        // tile strides st[0..2]; the running sum runs along k.
-        __device__ static void cpt1D(
-            float* __restrict__ Jc,
-            int const stat[3],
-            float const q0[3],
-            float const q1[3],
-            int base,
-            int const st[3],
-            float csd)
-        {
-            if(q0[2] == q1[2])
-                return;
-            float sj0[S + 1], sj1[S + 1], sk0[S + 1], sk1[S + 1];
-            SH::caArray(q0[1], !(stat[1] & 2), sj0);
-            SH::caArray(q1[1], !(stat[1] & 4), sj1);
-            SH::caArray(q0[2], !(stat[2] & 2), sk0);
-            SH::caArray(q1[2], !(stat[2] & 4), sk1);
-            float dsk[S];
-#pragma unroll
-            for(int k = 0; k < S; ++k)
-                dsk[k] = fs(sk1[k], sk0[k]);
-            int const leaveI = stat[0] & 1, leaveJ = stat[1] & 1, leaveK = stat[2] & 1;
-            float const ncsd = -csd;
-#pragma unroll
-            for(int i = begin; i < end + 1; ++i)
-                if(i < end + leaveI)
-                {
-                    float const s0i = SH::ca(fs(float(i), q0[0]));
-                    float const dsi = fs(SH::ca(fs(float(i), q1[0])), s0i);
-#pragma unroll
-                    for(int j = begin; j < end + 1; ++j)
-                        if(j < end + leaveJ)
-                        {
-                            float const s0j = sj0[j - begin];
-                            float const dsj = fs(sj1[j - begin], s0j);
-                            float const tmp = fm(
-                                ncsd,
-                                fa(fa(fm(s0i, s0j), fm(0.5f, fa(fm(dsi, s0j), fm(s0i, dsj)))),
-                                   fm(fm(1.0f / 3.0f, dsj), dsi)));
-                            float acc = 0.0f;
-                            int const ij = base + i * st[0] + j * st[1];
-#pragma unroll
-                            for(int k = begin; k < end; ++k)
-                                if(k < end + leaveK - 1)
-                                {
-                                    acc = fa(acc, fm(dsk[k - begin], tmp));
-                                    atomicAdd(Jc + ij + k * st[2], acc);
-                                }
-                        }
-                }
-        }
+        // status bits (Esirkepov/bitPacking.hpp:37-47): particle stays in its assignment cell
+        static constexpr int kInCell = 2 | 4;
 
-        // pos = in-cell position after the move, vel from the new momentum.
-        // Returns false (and deposits nothing) when the trajectory would leave
-        // the tile, which valid inputs (|v| dt < cell size) never do.
-        __device__ static bool deposit(
-            float* __restrict__ Jx,
-            float* __restrict__ Jy,
-            float* __restrict__ Jz,
-            int const cellRel[3],
+        // Trajectory of the particle in the virtual coordinate system: pos = in-cell
+        // position after the move, vel from the new momentum.  Returns false when
+        // the relay shift is out of range, which valid inputs (|v| dt < cell size)
+        // never produce.
+        __device__ __forceinline__ static bool prepare(
             float const pos[3],
             float const vel[3],
-            float charge,
             GridParams const& g,
-            float invVdt)
+            float p0[3],
+            float p1[3],
+            int gs[3],
+            int stat[3])
         {
-            float const cs[3] = {g.dx, g.dy, g.dz};
-            float p0[3], p1[3];
-            int gs[3], stat[3];
 #pragma unroll
             for(int d = 0; d < 3; ++d)
             {
-                float const dp = fdv(fm(vel[d], g.dt), cs[d]);
+                float const dp = divCell(fm(vel[d], g.dt), d, g);
                 p0[d] = fs(pos[d], dp);
                 p1[d] = pos[d];
                 int iS, iE;
@@ -438,33 +542,94 @@ namespace picgb
                 p1[d] = fs(p1[d], float(gs[d]));
             }
             constexpr int gsHi = SH::even ? 0 : 1;
+            bool ok = true;
 #pragma unroll
             for(int d = 0; d < 3; ++d)
-                if(gs[d] < -1 || gs[d] > gsHi || cellRel[d] < -1)
-                    return false;
-            constexpr int TYX = TX * TY;
-            int const base =(cellRel[0] + gs[0] + SH::jLo) + TX * (cellRel[1] + gs[1] + SH::jLo)
-                + TYX * (cellRel[2] + gs[2] + SH::jLo);
-            // currentSurfaceDensity = charge * (1/(V*dt)) * cellEdgeLength (Esirkepov.hpp:188-190)
+                ok &= (gs[d] >= -1 && gs[d] <= gsHi);
+            return ok;
+        }
+
+        // One rotated 1D current (cptCurrent1D); the running sum runs along k.
+        // kGeneral = false: the particle stays in its assignment cell along every
+        // axis (status kInCell everywhere), so the loops have their short fixed
+        // extent and the cached shapes need no out-of-range shift.
+        template<int C, bool kGeneral, typename Acc>
+        __device__ __forceinline__ static void cpt1D(
+            Acc const& acc,
+            int const stat[3],
+            float const q0[3],
+            float const q1[3],
+            float csd)
+        {
+            if(q0[2] == q1[2])
+                return;
+            float sj0[S + 1], sj1[S + 1], sk0[S + 1], sk1[S + 1];
+            SH::caArray(q0[1], kGeneral && !(stat[1] & 2), sj0);
+            SH::caArray(q1[1], kGeneral && !(stat[1] & 4), sj1);
+            SH::caArray(q0[2], kGeneral && !(stat[2] & 2), sk0);
+            SH::caArray(q1[2], kGeneral && !(stat[2] & 4), sk1);
+            float dsk[S];
+#pragma unroll
+            for(int k = 0; k < S; ++k)
+                dsk[k] = fs(sk1[k], sk0[k]);
+            int const leaveI = kGeneral ? (stat[0] & 1) : 0;
+            int const leaveJ = kGeneral ? (stat[1] & 1) : 0;
+            int const leaveK = kGeneral ? (stat[2] & 1) : 0;
+            constexpr int endIJ = kGeneral ? end + 1 : end; // loop bound before the leave guard
+            constexpr int endK = kGeneral ? end : end - 1;
+            float const ncsd = -csd;
+#pragma unroll
+            for(int i = begin; i < endIJ; ++i)
+                if(i < end + leaveI)
+                {
+                    float const s0i = SH::ca(fs(float(i), q0[0]));
+                    float const dsi = fs(SH::ca(fs(float(i), q1[0])), s0i);
+#pragma unroll
+                    for(int j = begin; j < endIJ; ++j)
+                        if(j < end + leaveJ)
+                        {
+                            float const s0j = sj0[j - begin];
+                            float const dsj = fs(sj1[j - begin], s0j);
+                            // s0i s0j + 1/2 (dsi s0j + s0i dsj) + 1/3 dsj dsi (Esirkepov.hpp:214-215),
+                            // contracted to fused multiply-adds; J is compared within tolerance
+                            float const half = fm(0.5f, __fmaf_rn(dsi, s0j, fm(s0i, dsj)));
+                            float const tmp = fm(ncsd, __fmaf_rn(fm(1.0f / 3.0f, dsj), dsi, __fmaf_rn(s0i, s0j, half)));
+                            float run = 0.0f;
+#pragma unroll
+                            for(int k = begin; k < endK; ++k)
+                                if(k < end + leaveK - 1)
+                                {
+                                    run = __fmaf_rn(dsk[k - begin], tmp, run);
+                                    acc.template add<C>(i, j, k, run);
+                                }
+                        }
+                }
+        }
+
+        // the three rotated calls; csd = charge * (1/(V*dt)) * cellEdgeLength (Esirkepov.hpp:188-190)
+        template<bool kGeneral, typename Acc>
+        __device__ __forceinline__ static void run(
+            Acc const& acc,
+            float const p0[3],
+            float const p1[3],
+            int const stat[3],
+            float charge,
+            GridParams const& g,
+            float invVdt)
+        {
+            float const qv = fm(charge, invVdt);
             {
-                // J_x: rotation (1,2,0): i->y, j->z, k->x
                 int const st[3] = {stat[1], stat[2], stat[0]};
                 float const a0[3] = {p0[1], p0[2], p0[0]}, a1[3] = {p1[1], p1[2], p1[0]};
-                int const stride[3] = {TX, TYX, 1};
-                cpt1D(Jx, st, a0, a1, base, stride, fm(fm(charge, invVdt), g.dx));
+                cpt1D<0, kGeneral>(acc, st, a0, a1, fm(qv, g.dx));
             }
             {
-                // J_y: rotation (2,0,1): i->z, j->x, k->y
                 int const st[3] = {stat[2], stat[0], stat[1]};
                 float const a0[3] = {p0[2], p0[0], p0[1]}, a1[3] = {p1[2], p1[0], p1[1]};
-                int const stride[3] = {TYX, 1, TX};
-                cpt1D(Jy, st, a0, a1, base, stride, fm(fm(charge, invVdt), g.dy));
+                cpt1D<1, kGeneral>(acc, st, a0, a1, fm(qv, g.dy));
             }
-            {
-                int const stride[3] = {1, TX, TYX};
-                cpt1D(Jz, stat, p0, p1, base, stride, fm(fm(charge, invVdt), g.dz));
-            }
-            return true;
+            cpt1D<2, kGeneral>(acc, stat, p0, p1, fm(qv, g.dz));
         }
     };
+
 } // namespace picgb

@@ -9,6 +9,20 @@ namespace picgb
 {
     struct GridParams; // picgb_device.cuh
 
+    // Fixed-point format of the shared-memory J tile (PICGB_J_FIXED): a value v
+    // becomes v * 2^s units, split into a high part a (a multiple of 2^k) and a
+    // low part b.  The host picks s and k so that neither part's sum over the
+    // values of one tile node can leave the int32 range.
+    struct JFixed
+    {
+        float scale; // 2^s
+        float invScale; // 2^-s
+        float hiStep; // 2^-k
+        float hiUnit; // 2^k
+        int k;
+    };
+
+
     // Status bits written by kernels into a device word (never a trap).
     enum StatusBits : unsigned
     {
@@ -56,6 +70,8 @@ namespace picgb
         float invVdt; // 1 / (dx * dy * dz * dt)
         int pusher; // 0 Boris, 1 Free (2 = not pushed, never launched)
         int deposit; // deposit the current inside the push kernel
+        unsigned long long* kindCount; // profiling only: [0] deposits with the short footprint, [1] general; or nullptr
+        JFixed jf; // fixed-point format of the J tile (used when built with PICGB_J_FIXED)
     };
 
     // ---- launchers (kernels_*.cu); all asynchronous on `stream`

@@ -286,6 +286,12 @@ class Simulation:
             out[name] = (ms.value, n.value)
         return out
 
+    def deposit_kinds(self) -> tuple[int, int]:
+        """(deposits with the short footprint, general deposits) since profiling was enabled."""
+        out = (ctypes.c_uint64 * 2)()
+        L.call("picgb_profile_deposit_kinds", self.handle, out)
+        return out[0], out[1]
+
     def device_status(self, reset: bool = False) -> int:
         b = ctypes.c_uint32()
         L.call("picgb_device_status", self.handle, ctypes.byref(b), int(reset))
