@@ -234,6 +234,36 @@ extern "C"
      * current into "FieldTmp0", returns max|eps0 div E - rho| and max|rho|.  Synchronises. */
     int picgb_charge_residual(picgb_sim* sim, double* max_residual, double* max_rho);
 
+    /* Charge-conservation residual without any device allocation.  No counterpart in the
+     * reference: it exists for callers that cannot call cudaMalloc, e.g. a plugin inside a
+     * host application that has already reserved nearly all device memory for itself (as a
+     * PIC code does when it sizes its particle heap to the free memory at start-up).
+     * Inputs are caller-owned device arrays: E as three component arrays of nx*ny*nz floats
+     * (x fastest), and nspecies particle lists in the host exchange format but in device
+     * memory (pos, w, sc, lcell are read; mom and id are not); charge[] and shape[] are host
+     * arrays with each species' charge per real particle and shape (CIC, TSC, PQS).  Outputs
+     * are host doubles: max|eps0 div E - rho| and max|rho|, the same quantities as
+     * picgb_charge_residual.  The charge density is accumulated in a file-scope device array
+     * of at most picgb_noalloc_max_cells() = 2^22 cells (16 MiB), which every GPU that loads
+     * this library holds until the process exits; larger grids are rejected with
+     * PICGB_ERR_INVALID.  The first call on a device looks up that array's device address
+     * (cudaGetSymbolAddress) and should come before any stream capture.  All calls share the
+     * array (each call clears it first), so calls that overlap on the GPU race.  Work is
+     * enqueued on `stream` (cudaStream_t, NULL = default stream) and the call waits for it.
+     * Errors are reported by picgb_noalloc_last_error(). */
+    uint64_t picgb_noalloc_max_cells(void);
+    const char* picgb_noalloc_last_error(void);
+    int picgb_charge_residual_noalloc(
+        const picgb_grid_config* grid,
+        const float* const* E,
+        int32_t nspecies,
+        const picgb_particles* species,
+        const float* charge,
+        const int32_t* shape,
+        void* stream,
+        double* max_residual,
+        double* max_rho);
+
     /* ------------------------------------------------------------ execution control */
     /* Enqueue on a caller's CUDA stream (cudaStream_t passed as void*); NULL = own stream. */
     int picgb_set_stream(picgb_sim* sim, void* stream);

@@ -92,6 +92,10 @@ SIGNATURES = [
     ("picgb_profile_enable", c_int, [c_void_p, c_int]),
     ("picgb_profile_read", c_int, [c_void_p, c_int, P(c_double), P(c_uint64)]),
     ("picgb_profile_deposit_kinds", c_int, [c_void_p, P(c_uint64)]),
+    ("picgb_noalloc_max_cells", c_uint64, []),
+    ("picgb_noalloc_last_error", c_char_p, []),
+    ("picgb_charge_residual_noalloc", c_int,
+     [P(GridConfig), P(c_void_p), c_int, P(Particles), P(c_float), P(c_int), c_void_p, P(c_double), P(c_double)]),
 ]
 
 KERNEL_CLASSES = {"push": 0, "compact": 1, "yee_b": 2, "yee_e": 3, "deposit": 4, "add_current": 5}
