@@ -310,6 +310,70 @@ def run_e2e(args, wl, sim, pg, torch, local_rank, world):
             "wall_s": round(dt, 4)}
 
 
+# ---------------------------------------------------------------------- batched ensemble
+EDGES = (16, 24, 32, 48, 64)
+
+
+def ensemble_boxes(nbox, seed=4):
+    """Seeded uneven boxes: edges from EDGES per axis, 4-16 ppc, u_th in [0.005, 0.05],
+    omega_p dt in [0.05, 0.2] (the density follows from omega_p with q = m = eps0 = 1)."""
+    rng = np.random.default_rng(seed)
+    dims = rng.choice(EDGES, size=(nbox, 3))
+    ppc = rng.integers(4, 17, size=nbox)
+    u_th = rng.uniform(0.005, 0.05, size=nbox)
+    wpdt = rng.uniform(0.05, 0.2, size=nbox)
+    return dims, ppc, u_th, (wpdt / DT) ** 2
+
+
+def ensemble_inits(pg, ppc, u_th, dens):
+    e = [pg.plasma_init(int(ppc[b]), float(dens[b]), float(u_th[b]), seed=1000 + b, position_seed=5000 + b)
+         for b in range(len(ppc))]
+    i = [pg.plasma_init(int(ppc[b]), float(dens[b]), float(u_th[b] / np.sqrt(MASS_P)), seed=3000 + b,
+                        position_seed=5000 + b) for b in range(len(ppc))]
+    return [e, i]
+
+
+def run_ensemble(args, local_rank):
+    """512 boxes: autotuned batched step (one graph launch per step) vs the single-box path box by box."""
+    import picongpu_gb300 as pg
+
+    shape = "TSC"
+    species = [pg.Species("e", -1.0, 1.0, shape=shape), pg.Species("i", 1.0, MASS_P, shape=shape)]
+    dims, ppc, u_th, dens = ensemble_boxes(args.ensemble_boxes)
+    ntune = min(64, len(dims))
+    g = pg.Grid(8, 8, 4, dt=DT, device=local_rank)
+    sc, th, rates = pg.autotune(dims[:ntune], species, ensemble_inits(pg, ppc[:ntune], u_th[:ntune], dens[:ntune]),
+                                grid=g, warmup=2, steps=3)
+    g = pg.Grid(8, 8, 4, dt=DT, supercell=sc, device=local_rank)
+    out = {"workload": f"{len(dims)} periodic boxes, edges from {list(EDGES)} per axis, 4-16 ppc per species, "
+                       f"u_th in [0.005, 0.05], omega_p dt in [0.05, 0.2], {shape}, Boris, Esirkepov, Yee, fp32",
+           "cells": int(np.prod(dims, axis=1).sum()), "supercell": list(sc), "threads_per_supercell": th,
+           "autotune": {f"{c[0][0]}x{c[0][1]}x{c[0][2]}/{c[1]}": round(r, 1) for c, r in rates.items()},
+           "autotune_boxes": ntune, "unit": "particle-steps/s"}
+    with pg.Ensemble(dims, grid=g, threads=th) as ens:
+        for sp in species:
+            ens.add_species(sp)
+        inits = ensemble_inits(pg, ppc, u_th, dens)
+        ens.init_plasma("e", inits[0])
+        ens.init_plasma("i", inits[1])
+        npart = ens.particle_count()
+        ens.run(args.warmup)
+        l0 = ens.launch_count()
+        t0 = time.perf_counter()
+        ens.run(args.ensemble_steps)
+        t_batched = time.perf_counter() - t0
+        launches = ens.launch_count() - l0
+        ens.run_sequential(1)
+        t0 = time.perf_counter()
+        ens.run_sequential(args.ensemble_steps)
+        t_seq = time.perf_counter() - t0
+    out.update({"particles": npart, "steps": args.ensemble_steps, "value": npart * args.ensemble_steps / t_batched,
+                "plain_sequential": npart * args.ensemble_steps / t_seq, "speedup": t_seq / t_batched,
+                "ms_per_step": 1e3 * t_batched / args.ensemble_steps, "gpu_launches": launches,
+                "timing": "host clock around run(); every step ends with a status read (stream synchronised)"})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -319,6 +383,9 @@ def main():
     ap.add_argument("--workload", default="two_stream_256", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--ensemble-boxes", type=int, default=512)
+    ap.add_argument("--ensemble-steps", type=int, default=10)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -358,6 +425,9 @@ def main():
 
             torch.distributed.destroy_process_group()
         return
+    batched = None
+    if not args.no_ensemble:
+        batched = run_ensemble(args, local_rank)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         val, cores, sample = cpu_sample_rate(wl, 10, 1, budget_s=20.0)
@@ -366,7 +436,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded device init)", "config": config,
             "particles": r["npart"], "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"],
-            "clocks": r["clocks"], "gpu_launches": r["launches"]}
+            "clocks": r["clocks"], "gpu_launches": r["launches"], "batched": batched}
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch

@@ -294,6 +294,57 @@ extern "C"
      * assignment cell along every axis (short footprint), out[1] the others.  Synchronises. */
     int picgb_profile_deposit_kinds(picgb_sim* sim, uint64_t* out);
 
+    /* ------------------------------------------------------------ batched ensemble */
+    /* Many independent periodic boxes of uneven size stepped together.  The reference runs one
+     * simulation per process (one Simulation, simulation/control/Simulation.hpp:522-542, per
+     * MPI domain); this form has no counterpart there.  Every box is a complete simulation
+     * handle (picgb_ensemble_box) that the single-box API reads and writes as usual; the
+     * ensemble adds the batched step: each kernel of picgb_step runs once over all boxes (the
+     * push as one persistent launch over every supercell of every box), and the whole step
+     * is one CUDA graph launch.  Results per box equal those of picgb_step on that box (the
+     * same per-particle and per-cell arithmetic; J sums in another atomic order).  All boxes
+     * enqueue on the ensemble's stream. */
+    typedef struct picgb_ensemble picgb_ensemble;
+    typedef struct picgb_ensemble_config
+    {
+        picgb_grid_config grid; /* settings shared by all boxes; grid.nx, ny, nz are ignored */
+        int32_t nbox;
+        const int32_t* dims; /* nbox * 3 cell counts (x, y, z), each a multiple of the supercell */
+        int32_t threads; /* threads per supercell of the batched push: 128 or 256 (0 = 256) */
+    } picgb_ensemble_config;
+    int picgb_ensemble_create(const picgb_ensemble_config* cfg, picgb_ensemble** out);
+    int picgb_ensemble_destroy(picgb_ensemble* ens);
+    int picgb_ensemble_size(picgb_ensemble* ens, int32_t* nbox);
+    /* Borrowed handle of box `box` (valid until picgb_ensemble_destroy; picgb_destroy refuses it). */
+    int picgb_ensemble_box(picgb_ensemble* ens, int32_t box, picgb_sim** out);
+    /* Adds the species to every box (picgb_add_species on each). */
+    int picgb_ensemble_add_species(picgb_ensemble* ens, const picgb_species_config* cfg, int32_t* index);
+    /* picgb_species_init_plasma on every box with its own parameters: per_box[nbox]. */
+    int picgb_ensemble_init_plasma(picgb_ensemble* ens, int32_t species, const picgb_plasma_init* per_box);
+    /* nsteps batched steps; one graph launch per step, then a status check (an overflowing
+     * supercell is re-laid out before the next step, as in picgb_step). */
+    int picgb_ensemble_run(picgb_ensemble* ens, uint32_t nsteps);
+    /* nsteps steps of the single-box path, box after box (picgb_run on each box). */
+    int picgb_ensemble_run_sequential(picgb_ensemble* ens, uint32_t nsteps);
+    /* Kernels launched by batched steps so far (nodes of the step graph times replays). */
+    int picgb_ensemble_launch_count(picgb_ensemble* ens, uint64_t* n);
+    /* Autotuner: builds the ensemble `cfg` once for each candidate supercell (8x8x4, 4x4x4,
+     * 8x8x8) and threads per supercell (128, 256), initialises the species (nspecies configs,
+     * inits[s * nbox + box]), runs `warmup` + `steps` batched steps and measures
+     * particle-steps/s with CUDA events.  rates[6] (may be NULL) receives the rate of each
+     * candidate in the order (8x8x4,128), (8x8x4,256), (4x4x4,128), ... and 0 for candidates
+     * that do not divide every box; *supercell and *threads receive the fastest. */
+    int picgb_ensemble_autotune(
+        const picgb_ensemble_config* cfg,
+        int32_t nspecies,
+        const picgb_species_config* species,
+        const picgb_plasma_init* inits,
+        uint32_t warmup,
+        uint32_t steps,
+        int32_t* supercell,
+        int32_t* threads,
+        double* rates);
+
 #ifdef __cplusplus
 }
 #endif

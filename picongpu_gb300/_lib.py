@@ -57,6 +57,10 @@ class PlasmaInit(ctypes.Structure):
                 ("position_seed", c_uint64)]
 
 
+class EnsembleConfig(ctypes.Structure):
+    _fields_ = [("grid", GridConfig), ("nbox", c_int), ("dims", P(c_int)), ("threads", c_int)]
+
+
 # (name, restype, argtypes) of every symbol declared in include/picgb.h
 SIGNATURES = [
     ("picgb_abi_version", c_int, []),
@@ -96,6 +100,18 @@ SIGNATURES = [
     ("picgb_noalloc_last_error", c_char_p, []),
     ("picgb_charge_residual_noalloc", c_int,
      [P(GridConfig), P(c_void_p), c_int, P(Particles), P(c_float), P(c_int), c_void_p, P(c_double), P(c_double)]),
+    ("picgb_ensemble_create", c_int, [P(EnsembleConfig), P(c_void_p)]),
+    ("picgb_ensemble_destroy", c_int, [c_void_p]),
+    ("picgb_ensemble_size", c_int, [c_void_p, P(c_int)]),
+    ("picgb_ensemble_box", c_int, [c_void_p, c_int, P(c_void_p)]),
+    ("picgb_ensemble_add_species", c_int, [c_void_p, P(SpeciesConfig), P(c_int)]),
+    ("picgb_ensemble_init_plasma", c_int, [c_void_p, c_int, P(PlasmaInit)]),
+    ("picgb_ensemble_run", c_int, [c_void_p, c_uint32]),
+    ("picgb_ensemble_run_sequential", c_int, [c_void_p, c_uint32]),
+    ("picgb_ensemble_launch_count", c_int, [c_void_p, P(c_uint64)]),
+    ("picgb_ensemble_autotune", c_int,
+     [P(EnsembleConfig), c_int, P(SpeciesConfig), P(PlasmaInit), c_uint32, c_uint32, P(c_int), P(c_int),
+      P(c_double)]),
 ]
 
 KERNEL_CLASSES = {"push": 0, "compact": 1, "yee_b": 2, "yee_e": 3, "deposit": 4, "add_current": 5}

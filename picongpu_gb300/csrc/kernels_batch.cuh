@@ -1,0 +1,148 @@
+// Persistent push kernel of a batched ensemble: many independent periodic boxes
+// of uneven size in one launch.  A fixed grid of resident blocks takes work
+// items (box, supercell) from a global counter, so large and small boxes share
+// the GPU without a launch per box; each item runs the same supercell push as
+// the single-box kernel (kernels_push.cuh) on that box's fields and particles.
+#pragma once
+
+#include "kernels_push.cuh"
+#include "picgb_batch.hpp"
+
+namespace picgb
+{
+    // Resident blocks the batched kernel's register budget is sized for.
+    template<int THREADS>
+    constexpr int batchMinBlocks()
+    {
+        return THREADS >= 256 ? PICGB_PUSH_MIN_BLOCKS : 2 * PICGB_PUSH_MIN_BLOCKS;
+    }
+
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS>
+    __global__ void __launch_bounds__(THREADS, batchMinBlocks<THREADS>()) kPushBatch(
+        BatchSpecies const* __restrict__ table,
+        uint32_t const* __restrict__ items,
+        uint32_t nitems,
+        uint32_t* __restrict__ counter,
+        unsigned* __restrict__ status)
+    {
+        extern __shared__ __align__(16) float smem[];
+        __shared__ unsigned s_nhole;
+        __shared__ uint32_t s_item;
+        __shared__ __align__(16) BatchSpecies s_box;
+        static_assert(sizeof(BatchSpecies) % 4 == 0, "BatchSpecies is copied as 32-bit words");
+        constexpr int kWords = int(sizeof(BatchSpecies) / 4);
+        for(;;)
+        {
+            if(threadIdx.x == 0)
+                s_item = atomicAdd(counter, 1u);
+            __syncthreads();
+            uint32_t const it = s_item;
+            if(it >= nitems)
+                break;
+            uint32_t const v = __ldg(items + it);
+            uint32_t const* src = reinterpret_cast<uint32_t const*>(table + batchBox(v));
+            for(int i = threadIdx.x; i < kWords; i += THREADS)
+                reinterpret_cast<uint32_t*>(&s_box)[i] = __ldg(src + i);
+            __syncthreads();
+            pushSupercell<SHAPE, SX, SY, SZ, THREADS>(
+                s_box.sp,
+                s_box.E,
+                s_box.B,
+                s_box.J,
+                s_box.g,
+                s_box.pp,
+                status,
+                int(batchSc(v)),
+                smem,
+                s_nhole);
+            __syncthreads(); // the next item reuses the tiles, s_box and s_item
+        }
+    }
+
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS>
+    cudaError_t launchPushBatchT(
+        BatchSpecies const* table,
+        uint32_t const* items,
+        uint32_t nitems,
+        uint32_t* counter,
+        unsigned* status,
+        cudaStream_t stream)
+    {
+        using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>, THREADS>;
+        auto k = kPushBatch<SHAPE, SX, SY, SZ, THREADS>;
+        size_t const smem = TG::pushSmem;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if(e != cudaSuccess)
+            return e;
+        int occ = 0, dev = 0, nsm = 0;
+        if((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, THREADS, smem)) != cudaSuccess)
+            return e;
+        if((e = cudaGetDevice(&dev)) != cudaSuccess)
+            return e;
+        if((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            return e;
+        if(occ < 1)
+            return cudaErrorInvalidConfiguration;
+        uint32_t const blocks = std::min<uint32_t>(uint32_t(occ) * uint32_t(nsm), nitems);
+        if(blocks == 0)
+            return cudaSuccess;
+        k<<<blocks, THREADS, smem, stream>>>(table, items, nitems, counter, status);
+        return cudaGetLastError();
+    }
+
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS>
+    int pushBatchOccupancyT()
+    {
+        using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>, THREADS>;
+        auto k = kPushBatch<SHAPE, SX, SY, SZ, THREADS>;
+        if(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TG::pushSmem)) != cudaSuccess)
+            return 0;
+        int occ = 0;
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, THREADS, TG::pushSmem) != cudaSuccess)
+            return 0;
+        return occ;
+    }
+
+// Instantiates the batched launchers of one shape for the supercell sizes
+// 8x8x4, 4x4x4, 8x8x8 and 128 or 256 threads per supercell.
+#define PICGB_BATCH_CASES(F, SHAPE, ...)                                                                              \
+    switch(scId * 2 + (threads == 128 ? 0 : 1))                                                                       \
+    {                                                                                                                 \
+    case 0:                                                                                                           \
+        return F<SHAPE, 8, 8, 4, 128>(__VA_ARGS__);                                                                   \
+    case 1:                                                                                                           \
+        return F<SHAPE, 8, 8, 4, 256>(__VA_ARGS__);                                                                   \
+    case 2:                                                                                                           \
+        return F<SHAPE, 4, 4, 4, 128>(__VA_ARGS__);                                                                   \
+    case 3:                                                                                                           \
+        return F<SHAPE, 4, 4, 4, 256>(__VA_ARGS__);                                                                   \
+    case 4:                                                                                                           \
+        return F<SHAPE, 8, 8, 8, 128>(__VA_ARGS__);                                                                   \
+    case 5:                                                                                                           \
+        return F<SHAPE, 8, 8, 8, 256>(__VA_ARGS__);                                                                   \
+    }
+
+#define PICGB_BATCH_LAUNCHERS(SHAPE, NAME)                                                                            \
+    cudaError_t launchPushBatch##NAME(                                                                                \
+        int scId,                                                                                                     \
+        int threads,                                                                                                  \
+        BatchSpecies const* table,                                                                                    \
+        uint32_t const* items,                                                                                        \
+        uint32_t nitems,                                                                                              \
+        uint32_t* counter,                                                                                            \
+        unsigned* status,                                                                                             \
+        cudaStream_t stream)                                                                                          \
+    {                                                                                                                 \
+        if(threads != 128 && threads != 256)                                                                          \
+            return cudaErrorInvalidValue;                                                                             \
+        PICGB_BATCH_CASES(launchPushBatchT, SHAPE, table, items, nitems, counter, status, stream)                     \
+        return cudaErrorInvalidValue;                                                                                 \
+    }                                                                                                                 \
+    int pushBatchOccupancy##NAME(int scId, int threads)                                                               \
+    {                                                                                                                 \
+        if(threads != 128 && threads != 256)                                                                          \
+            return 0;                                                                                                 \
+        PICGB_BATCH_CASES(pushBatchOccupancyT, SHAPE)                                                                 \
+        return 0;                                                                                                     \
+    }
+} // namespace picgb

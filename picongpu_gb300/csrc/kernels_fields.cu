@@ -3,6 +3,7 @@
 // Fields are SoA [component][z][y][x] without guard cells; the periodic
 // neighbour is reached by index wrap, which replaces the reference's guard
 // exchange of E and B (MaxwellSolver/FDTD/FDTDBase.hpp:111,168,181).
+#include "picgb_batch.hpp"
 #include "picgb_device.cuh"
 #include "picgb_internal.hpp"
 
@@ -10,14 +11,16 @@ namespace picgb
 {
     constexpr int kFieldBX = 128;
 
-    // B -= curl(E) * 0.5 * dt with forward differences
+    // B -= curl(E) * 0.5 * dt with forward differences at cell (x, y, z)
     // (FDTDBase.kernel:92-121 UpdateBHalfFunctor, differentiation/ForwardDerivative.hpp:45-63, Curl.hpp:84-89).
-    __global__ void __launch_bounds__(kFieldBX) kYeeBHalf(float const* __restrict__ E, float* __restrict__ B, GridParams g)
+    __device__ __forceinline__ void yeeBHalfAt(
+        float const* __restrict__ E,
+        float* __restrict__ B,
+        GridParams const& g,
+        int const x,
+        int const y,
+        int const z)
     {
-        int const x = blockIdx.x * blockDim.x + threadIdx.x;
-        int const y = blockIdx.y, z = blockIdx.z;
-        if(x >= g.nx)
-            return;
         size_t const nc = size_t(g.nx) * g.ny * g.nz;
         size_t const row = size_t(g.nx) * (size_t(y) + size_t(g.ny) * z);
         size_t const i = row + x;
@@ -40,16 +43,26 @@ namespace picgb
         B[2 * nc + i] = fs(B[2 * nc + i], fm(fm(c2, 0.5f), g.dt));
     }
 
-    // E += curl(B) * c^2 * dt with backward differences (FDTDBase.kernel:51-81 UpdateEFunctor,
-    // BackwardDerivative.hpp:45-63); optionally followed by E += coeff * J
-    // (currentInterpolation/None.hpp:60-65) as a separate rounding step.
-    __global__ void __launch_bounds__(kFieldBX)
-        kYeeE(float const* __restrict__ B, float* __restrict__ E, float const* __restrict__ J, float coeff, GridParams g)
+    __global__ void __launch_bounds__(kFieldBX) kYeeBHalf(float const* __restrict__ E, float* __restrict__ B, GridParams g)
     {
         int const x = blockIdx.x * blockDim.x + threadIdx.x;
-        int const y = blockIdx.y, z = blockIdx.z;
-        if(x >= g.nx)
-            return;
+        if(x < g.nx)
+            yeeBHalfAt(E, B, g, x, blockIdx.y, blockIdx.z);
+    }
+
+    // E += curl(B) * c^2 * dt with backward differences at cell (x, y, z) (FDTDBase.kernel:51-81
+    // UpdateEFunctor, BackwardDerivative.hpp:45-63); optionally followed by E += coeff * J
+    // (currentInterpolation/None.hpp:60-65) as a separate rounding step.
+    __device__ __forceinline__ void yeeEAt(
+        float const* __restrict__ B,
+        float* __restrict__ E,
+        float const* __restrict__ J,
+        float const coeff,
+        GridParams const& g,
+        int const x,
+        int const y,
+        int const z)
+    {
         size_t const nc = size_t(g.nx) * g.ny * g.nz;
         size_t const row = size_t(g.nx) * (size_t(y) + size_t(g.ny) * z);
         size_t const i = row + x;
@@ -77,6 +90,92 @@ namespace picgb
                 e = fa(e, fm(coeff, __ldg(J + k)));
             E[k] = e;
         }
+    }
+
+    __global__ void __launch_bounds__(kFieldBX)
+        kYeeE(float const* __restrict__ B, float* __restrict__ E, float const* __restrict__ J, float coeff, GridParams g)
+    {
+        int const x = blockIdx.x * blockDim.x + threadIdx.x;
+        if(x < g.nx)
+            yeeEAt(B, E, J, coeff, g, x, blockIdx.y, blockIdx.z);
+    }
+
+    // ------------------------------------------------------------ ensemble of boxes
+    // Block b of a batched field launch covers kBatchFieldThreads consecutive
+    // cells of box blockBox[b]; returns false for threads past the box's end.
+    __device__ __forceinline__ bool batchCell(
+        BatchBox const* __restrict__ boxes,
+        uint32_t const* __restrict__ blockBox,
+        BatchBox const*& box,
+        int& x,
+        int& y,
+        int& z)
+    {
+        box = boxes + __ldg(blockBox + blockIdx.x);
+        GridParams const& g = box->g;
+        size_t const cell = size_t(blockIdx.x - box->block0) * kBatchFieldThreads + threadIdx.x;
+        if(cell >= size_t(g.nx) * g.ny * g.nz)
+            return false;
+        x = int(cell % unsigned(g.nx));
+        size_t const r = cell / unsigned(g.nx);
+        y = int(r % unsigned(g.ny));
+        z = int(r / unsigned(g.ny));
+        return true;
+    }
+
+    __global__ void __launch_bounds__(kBatchFieldThreads)
+        kYeeBHalfBatch(BatchBox const* __restrict__ boxes, uint32_t const* __restrict__ blockBox)
+    {
+        BatchBox const* b;
+        int x, y, z;
+        if(batchCell(boxes, blockBox, b, x, y, z))
+            yeeBHalfAt(b->E, b->B, b->g, x, y, z);
+    }
+
+    // E update with the J add of the fused deposit (as kYeeE with J).
+    __global__ void __launch_bounds__(kBatchFieldThreads)
+        kYeeEBatch(BatchBox const* __restrict__ boxes, uint32_t const* __restrict__ blockBox)
+    {
+        BatchBox const* b;
+        int x, y, z;
+        if(batchCell(boxes, blockBox, b, x, y, z))
+            yeeEAt(b->B, b->E, b->J, b->coeffJ, b->g, x, y, z);
+    }
+
+    __global__ void __launch_bounds__(kBatchFieldThreads)
+        kZeroJBatch(BatchBox const* __restrict__ boxes, uint32_t const* __restrict__ blockBox)
+    {
+        BatchBox const* b;
+        int x, y, z;
+        if(batchCell(boxes, blockBox, b, x, y, z))
+        {
+            size_t const nc = size_t(b->g.nx) * b->g.ny * b->g.nz;
+            size_t const i = size_t(x) + size_t(b->g.nx) * (size_t(y) + size_t(b->g.ny) * z);
+            b->J[i] = 0.0f;
+            b->J[nc + i] = 0.0f;
+            b->J[2 * nc + i] = 0.0f;
+        }
+    }
+
+    cudaError_t launchYeeBHalfBatch(BatchBox const* boxes, uint32_t const* blockBox, uint32_t nblocks, cudaStream_t stream)
+    {
+        if(nblocks)
+            kYeeBHalfBatch<<<nblocks, kBatchFieldThreads, 0, stream>>>(boxes, blockBox);
+        return cudaGetLastError();
+    }
+
+    cudaError_t launchYeeEBatch(BatchBox const* boxes, uint32_t const* blockBox, uint32_t nblocks, cudaStream_t stream)
+    {
+        if(nblocks)
+            kYeeEBatch<<<nblocks, kBatchFieldThreads, 0, stream>>>(boxes, blockBox);
+        return cudaGetLastError();
+    }
+
+    cudaError_t launchZeroJBatch(BatchBox const* boxes, uint32_t const* blockBox, uint32_t nblocks, cudaStream_t stream)
+    {
+        if(nblocks)
+            kZeroJBatch<<<nblocks, kBatchFieldThreads, 0, stream>>>(boxes, blockBox);
+        return cudaGetLastError();
     }
 
     __global__ void kAddCurrent(float* __restrict__ E, float const* __restrict__ J, float coeff, size_t n)

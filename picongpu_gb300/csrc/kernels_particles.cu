@@ -3,12 +3,23 @@
 // pmacc/particles/ParticlesBase.kernel:183-359), upload scatter into the
 // supercell layout, download gather, and the FP64 kinetic-energy reduction
 // (plugins/EnergyParticles.x.cpp:58-160).
+#include "picgb_batch.hpp"
 #include "picgb_device.cuh"
 #include "picgb_internal.hpp"
 
 namespace picgb
 {
 #define PICGB_DECL_SHAPE(NAME)                                                                                        \
+    cudaError_t launchPushBatch##NAME(                                                                                \
+        int,                                                                                                          \
+        int,                                                                                                          \
+        BatchSpecies const*,                                                                                          \
+        uint32_t const*,                                                                                              \
+        uint32_t,                                                                                                     \
+        uint32_t*,                                                                                                    \
+        unsigned*,                                                                                                    \
+        cudaStream_t);                                                                                                \
+    int pushBatchOccupancy##NAME(int, int);                                                                           \
     cudaError_t launchPush##NAME(                                                                                     \
         int,                                                                                                          \
         SpeciesDev const&,                                                                                            \
@@ -54,6 +65,43 @@ namespace picgb
             return launchPushPQS(scId, sp, E, B, J, g, pp, status, stream);
         }
         return cudaErrorInvalidValue;
+    }
+
+    cudaError_t launchPushBatch(
+        int shape,
+        int scId,
+        int threads,
+        BatchSpecies const* table,
+        uint32_t const* items,
+        uint32_t nitems,
+        uint32_t* counter,
+        unsigned* status,
+        cudaStream_t stream)
+    {
+        switch(shape)
+        {
+        case 1:
+            return launchPushBatchCIC(scId, threads, table, items, nitems, counter, status, stream);
+        case 2:
+            return launchPushBatchTSC(scId, threads, table, items, nitems, counter, status, stream);
+        case 3:
+            return launchPushBatchPQS(scId, threads, table, items, nitems, counter, status, stream);
+        }
+        return cudaErrorInvalidValue;
+    }
+
+    int pushBatchOccupancy(int shape, int scId, int threads)
+    {
+        switch(shape)
+        {
+        case 1:
+            return pushBatchOccupancyCIC(scId, threads);
+        case 2:
+            return pushBatchOccupancyTSC(scId, threads);
+        case 3:
+            return pushBatchOccupancyPQS(scId, threads);
+        }
+        return 0;
     }
 
     cudaError_t launchDeposit(
@@ -178,12 +226,10 @@ namespace picgb
     }
 
     // Fill the slots vacated by leaving particles with the last valid particles
-    // of the supercell so that slots [0, count) are dense again.
-    __global__ void __launch_bounds__(256) kCompact(SpeciesDev sp)
+    // of supercell `sc` so that slots [0, count) are dense again.  One block;
+    // `csm` holds 3 * ceil(cap / 32) words.
+    __device__ __forceinline__ void compactSupercell(SpeciesDev const& sp, int const sc, uint32_t* csm, uint32_t* warpSums)
     {
-        extern __shared__ uint32_t csm[];
-        __shared__ uint32_t warpSums[32];
-        int const sc = blockIdx.x;
         uint32_t const tail = sp.tail[sc];
         uint32_t const n = tail < sp.cap ? tail : sp.cap;
         uint32_t const h = sp.nhole[sc];
@@ -257,6 +303,44 @@ namespace picgb
             sp.tail[sc] = newc;
             sp.nhole[sc] = 0u;
         }
+    }
+
+    __global__ void __launch_bounds__(256) kCompact(SpeciesDev sp)
+    {
+        extern __shared__ uint32_t csm[];
+        __shared__ uint32_t warpSums[32];
+        compactSupercell(sp, blockIdx.x, csm, warpSums);
+    }
+
+    // Compaction over the supercells of every box of an ensemble: block b
+    // handles work item b (box, supercell).
+    __global__ void __launch_bounds__(256)
+        kCompactBatch(BatchSpecies const* __restrict__ boxes, uint32_t const* __restrict__ items)
+    {
+        extern __shared__ uint32_t csm[];
+        __shared__ uint32_t warpSums[32];
+        uint32_t const it = items[blockIdx.x];
+        compactSupercell(boxes[batchBox(it)].sp, int(batchSc(it)), csm, warpSums);
+    }
+
+    cudaError_t launchCompactBatch(
+        BatchSpecies const* boxes,
+        uint32_t const* items,
+        uint32_t nitems,
+        uint32_t maxCap,
+        cudaStream_t stream)
+    {
+        if(nitems == 0)
+            return cudaSuccess;
+        size_t const smem = sizeof(uint32_t) * 3 * ((maxCap + 31) / 32);
+        if(smem > 48 * 1024)
+        {
+            cudaError_t e = cudaFuncSetAttribute(kCompactBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if(e != cudaSuccess)
+                return e;
+        }
+        kCompactBatch<<<nitems, 256, smem, stream>>>(boxes, items);
+        return cudaGetLastError();
     }
 
     cudaError_t launchCompact(SpeciesDev const& sp, int nsc, cudaStream_t stream)

@@ -24,9 +24,8 @@ namespace picgb
     // (see kPush): kQueueCap jobs of kJobWords words for every warp.
     constexpr int kQueueCap = 64;
     constexpr int kJobWords = 9;
-    constexpr int kQueueWords = (kPushThreads / 32) * kQueueCap * kJobWords;
 
-    template<typename SH, typename SC>
+    template<typename SH, typename SC, int THREADS = kPushThreads>
     struct TileGeom
     {
         static constexpr int GX = SC::SX + SH::gLo + SH::gHi;
@@ -39,7 +38,8 @@ namespace picgb
         static constexpr int JT = JX * JY * JZ;
         // E and B tiles, the J tile, the per-warp queues of deposit jobs
         static constexpr int JWords = (PICGB_J_FIXED ? 6 : 3) * JT; // words of the J tile
-        static constexpr size_t pushSmem = sizeof(float) * (6 * GT + JWords) + sizeof(float) * kQueueWords;
+        static constexpr int QueueWords = (THREADS / 32) * kQueueCap * kJobWords;
+        static constexpr size_t pushSmem = sizeof(float) * (6 * GT + JWords) + sizeof(float) * QueueWords;
         static constexpr size_t depositSmem = sizeof(float) * JWords;
     };
 
@@ -154,36 +154,39 @@ namespace picgb
         }
     };
 
-    // Fused push kernel.  Each thread pushes one particle per round; then the
-    // warp deposits at once the lanes whose particle stays in its assignment
-    // cell along every axis (the short fixed footprint, most particles), and
-    // queues the other lanes' jobs in its shared-memory queue, which it drains
-    // 32 at a time with the general footprint.  Without the split every warp
-    // would pay, through divergence, the largest footprint of any of its lanes.
-    template<int SHAPE, int SX, int SY, int SZ>
-    __global__ void __launch_bounds__(kPushThreads, PICGB_PUSH_MIN_BLOCKS) kPush(
-        SpeciesDev sp,
+    // Push of the particles of supercell `sc` by one block of THREADS threads.
+    // Each thread pushes one particle per round; then the warp deposits at once
+    // the lanes whose particle stays in its assignment cell along every axis
+    // (the short fixed footprint, most particles), and queues the other lanes'
+    // jobs in its shared-memory queue, which it drains 32 at a time with the
+    // general footprint.  Without the split every warp would pay, through
+    // divergence, the largest footprint of any of its lanes.  `smem` holds
+    // TileGeom::pushSmem bytes; the block must be synchronised before a second
+    // call reuses it.
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS>
+    __device__ __forceinline__ void pushSupercell(
+        SpeciesDev const& sp,
         float const* __restrict__ E,
         float const* __restrict__ B,
         float* __restrict__ J,
-        GridParams g,
-        PushParams pp,
-        unsigned* __restrict__ status)
+        GridParams const& g,
+        PushParams const& pp,
+        unsigned* __restrict__ status,
+        int const sc,
+        float* const smem,
+        unsigned& s_nhole)
     {
         using SH = Shape<SHAPE>;
         using SC = SuperCell<SX, SY, SZ>;
-        using TG = TileGeom<SH, SC>;
+        using TG = TileGeom<SH, SC, THREADS>;
         using ES = Esirkepov<SH>;
         using Tile = TileJ<TG::JX, TG::JY, TG::JT>;
-        extern __shared__ __align__(16) float smem[];
         float* const Es = smem;
         float* const Bs = smem + 3 * TG::GT;
         float* const Js = smem + 6 * TG::GT;
         int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
         WarpQueue const queue{smem + 6 * TG::GT + TG::JWords + warp * kQueueCap * kJobWords};
-        __shared__ unsigned s_nhole;
 
-        int const sc = blockIdx.x;
         uint32_t const n = sp.count[sc];
         if(threadIdx.x == 0)
             s_nhole = 0u;
@@ -210,7 +213,7 @@ namespace picgb
 
         size_t const base = size_t(sc) * sp.cap;
         int queued = 0; // jobs in this warp's queue (warp-uniform)
-        for(uint32_t c0 = 0; c0 < n; c0 += kPushThreads)
+        for(uint32_t c0 = 0; c0 < n; c0 += THREADS)
         {
             uint32_t const k = c0 + threadIdx.x;
             int kind = -1; // 0: stays in its assignment cell, 1: crosses a cell boundary
@@ -366,6 +369,22 @@ namespace picgb
             sp.nhole[sc] = s_nhole;
         if(pp.deposit)
             flushTile<TG::JX, TG::JY, TG::JT>(Js, J, ox - SH::jLo, oy - SH::jLo, oz - SH::jLo, g, ncell, pp.jf);
+    }
+
+    // Fused push kernel of one box: one block per supercell.
+    template<int SHAPE, int SX, int SY, int SZ>
+    __global__ void __launch_bounds__(kPushThreads, PICGB_PUSH_MIN_BLOCKS) kPush(
+        SpeciesDev sp,
+        float const* __restrict__ E,
+        float const* __restrict__ B,
+        float* __restrict__ J,
+        GridParams g,
+        PushParams pp,
+        unsigned* __restrict__ status)
+    {
+        extern __shared__ __align__(16) float smem[];
+        __shared__ unsigned s_nhole;
+        pushSupercell<SHAPE, SX, SY, SZ, kPushThreads>(sp, E, B, J, g, pp, status, blockIdx.x, smem, s_nhole);
     }
 
     // Deposit-only kernel over the sorted particles (the reference's separate

@@ -1,26 +1,24 @@
 // Host runtime behind the C-ABI of include/picgb.h: the simulation handle,
 // the DataConnector-style registry, species upload/download, the stage
 // sequence of one PIC step and the diagnostics.
-#include "picgb.h"
-#include "picgb_device.cuh"
+#include "picgb_sim.hpp"
 #include "picgb_init.hpp"
-#include "picgb_internal.hpp"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <map>
-#include <memory>
-#include <string>
-#include <vector>
 
 using namespace picgb;
+using namespace picgb::host;
 
-namespace
+namespace picgb::host
 {
-    thread_local std::string g_lastError;
+    namespace
+    {
+        thread_local std::string g_lastError;
+    }
 
     int fail(int code, char const* fmt, ...)
     {
@@ -32,174 +30,45 @@ namespace
         g_lastError = buf;
         return code;
     }
+} // namespace picgb::host
 
-#define CUDA_TRY(expr)                                                                                                \
-    do                                                                                                                \
-    {                                                                                                                 \
-        cudaError_t e_ = (expr);                                                                                      \
-        if(e_ != cudaSuccess)                                                                                         \
-            return fail(PICGB_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__);   \
-    } while(0)
-
-    template<typename T>
-    cudaError_t dalloc(T*& p, size_t n)
-    {
-        p = nullptr;
-        if(n == 0)
-            return cudaSuccess;
-        return cudaMalloc(reinterpret_cast<void**>(&p), n * sizeof(T));
-    }
-
-    template<typename T>
-    void dfree(T*& p)
-    {
-        if(p)
-            cudaFree(p);
-        p = nullptr;
-    }
-
-    int scSize(int id, int* s)
-    {
-        static int const tab[3][3] = {{8, 8, 4}, {4, 4, 4}, {8, 8, 8}};
-        if(id < 0 || id > 2)
-            return 0;
-        s[0] = tab[id][0];
-        s[1] = tab[id][1];
-        s[2] = tab[id][2];
-        return 1;
-    }
-
-    struct Species
-    {
-        std::string name;
-        picgb_species_config cfg{};
-        SpeciesDev dev{};
-        int nsc = 0;
-        bool allocated = false;
-        float wmax = 0.0f; // largest |weighting| (bounds a single J contribution)
-
-        void freeAll()
-        {
-            dfree(dev.px);
-            dfree(dev.py);
-            dfree(dev.pz);
-            dfree(dev.ux);
-            dfree(dev.uy);
-            dfree(dev.uz);
-            dfree(dev.w);
-            dfree(dev.lcell);
-            dfree(dev.id);
-            dfree(dev.count);
-            dfree(dev.tail);
-            dfree(dev.nhole);
-            dfree(dev.holes);
-            dfree(dev.sp_attr);
-            dfree(dev.sp_sc);
-            dfree(dev.sp_lcell);
-            dfree(dev.sp_id);
-            dfree(dev.sp_count);
-            allocated = false;
-        }
-    };
-
-    // Registry entry (pmacc/dataManagement/DataConnector.hpp:48-136): either an
-    // internal buffer (field or species, resolved at lookup so relayouts are
-    // seen) or caller-shared device data.
-    struct Entry
-    {
-        enum Kind
-        {
-            FieldE,
-            FieldB,
-            FieldJ,
-            FieldTmp,
-            SpeciesBuf,
-            Opaque,
-            External
-        } kind;
-        int index = 0;
-        picgb_buffer_desc desc{};
-    };
-} // namespace
-
-struct picgb_sim
+PushParams picgb_sim::pushParams(Species const& s, bool deposit) const
 {
-    picgb_grid_config cfg{};
-    GridParams g{};
-    int sc[3] = {8, 8, 4};
-    int nsc = 0;
-    size_t ncell = 0;
-    float* E = nullptr;
-    float* B = nullptr;
-    float* J = nullptr;
-    float* rho = nullptr;
-    unsigned* status = nullptr; // device status word
-    unsigned* hostStatus = nullptr; // pinned
-    double* energy = nullptr; // device accumulators
-    unsigned* maxBits = nullptr; // device: residual max, rho max
-    unsigned long long* kindCount = nullptr; // device: deposits by footprint (profiling)
-    cudaStream_t stream = nullptr;
-    bool ownStream = false;
-    uint64_t launches = 0;
-    std::vector<std::unique_ptr<Species>> species;
-    std::map<std::string, Entry> registry;
-    // per-kernel event timing (picgb_profile_enable)
-    bool prof = false;
-    struct Pending
-    {
-        int cls;
-        cudaEvent_t a, b;
-    };
-    std::vector<Pending> pending;
-    std::vector<cudaEvent_t> eventPool;
-    double profMs[PICGB_KERNEL_CLASSES] = {};
-    uint64_t profN[PICGB_KERNEL_CLASSES] = {};
+    PushParams p{};
+    p.charge = s.cfg.charge;
+    p.mass = s.cfg.mass;
+    p.dt = cfg.dt;
+    p.c2 = cfg.c * cfg.c;
+    p.rc2 = 1.0f / (cfg.c * cfg.c);
+    float const vdt = cellVolume() * cfg.dt;
+    p.invVdt = 1.0f / vdt;
+    p.pusher = s.cfg.pusher;
+    p.deposit = deposit ? 1 : 0;
+    p.kindCount = prof ? kindCount : nullptr;
+    // Fixed-point format of the J tile (kernels built with PICGB_J_FIXED).  A
+    // deposited value is a running sum acc_k = sum DS * tmp with
+    // |tmp| <= |q w| d / (V dt) and sum |DS| <= 2, so |acc| <= 2 |q| wmax dmax / (V dt)
+    // =: vmax.  A tile node receives at most one value per particle of its
+    // supercell (< 2^cb).  With k = 31 - cb and vmax * 2^s <= 2^(61 - 2 cb) the sums
+    // of the high and of the low parts stay below 2^30 + 2^(cb - 1).
+    int cb = 1;
+    while((1u << cb) < s.dev.cap)
+        ++cb;
+    double const dmax = std::max(std::max(double(cfg.dx), double(cfg.dy)), double(cfg.dz));
+    double const vmax = 2.0 * std::fabs(double(s.cfg.charge)) * double(s.wmax) * dmax * double(p.invVdt);
+    int e = 0;
+    if(vmax > 0.0 && std::isfinite(vmax))
+        std::frexp(vmax, &e); // vmax < 2^e
+    int const sExp = std::min(std::max(61 - 2 * cb - e, -126), 126);
+    p.jf.k = 31 - cb;
+    p.jf.scale = std::ldexp(1.0f, sExp);
+    p.jf.invScale = std::ldexp(1.0f, -sExp);
+    p.jf.hiStep = std::ldexp(1.0f, -p.jf.k);
+    p.jf.hiUnit = std::ldexp(1.0f, p.jf.k);
+    return p;
+}
 
-    float coeffJ() const { return -(1.0f / cfg.eps0) * cfg.dt; } // FDTD.hpp:84
-    float cellVolume() const
-    {
-        float v = cfg.dx * cfg.dy;
-        v = v * cfg.dz;
-        return v;
-    }
-    PushParams pushParams(Species const& s, bool deposit) const
-    {
-        PushParams p{};
-        p.charge = s.cfg.charge;
-        p.mass = s.cfg.mass;
-        p.dt = cfg.dt;
-        p.c2 = cfg.c * cfg.c;
-        p.rc2 = 1.0f / (cfg.c * cfg.c);
-        float const vdt = cellVolume() * cfg.dt;
-        p.invVdt = 1.0f / vdt;
-        p.pusher = s.cfg.pusher;
-        p.deposit = deposit ? 1 : 0;
-        p.kindCount = prof ? kindCount : nullptr;
-        // Fixed-point format of the J tile (kernels built with PICGB_J_FIXED).  A
-        // deposited value is a running sum acc_k = sum DS * tmp with
-        // |tmp| <= |q w| d / (V dt) and sum |DS| <= 2, so |acc| <= 2 |q| wmax dmax / (V dt)
-        // =: vmax.  A tile node receives at most one value per particle of its
-        // supercell (< 2^cb).  With k = 31 - cb and vmax * 2^s <= 2^(61 - 2 cb) the sums
-        // of the high and of the low parts stay below 2^30 + 2^(cb - 1).
-        int cb = 1;
-        while((1u << cb) < s.dev.cap)
-            ++cb;
-        double const dmax = std::max(std::max(double(cfg.dx), double(cfg.dy)), double(cfg.dz));
-        double const vmax = 2.0 * std::fabs(double(s.cfg.charge)) * double(s.wmax) * dmax * double(p.invVdt);
-        int e = 0;
-        if(vmax > 0.0 && std::isfinite(vmax))
-            std::frexp(vmax, &e); // vmax < 2^e
-        int const sExp = std::min(std::max(61 - 2 * cb - e, -126), 126);
-        p.jf.k = 31 - cb;
-        p.jf.scale = std::ldexp(1.0f, sExp);
-        p.jf.invScale = std::ldexp(1.0f, -sExp);
-        p.jf.hiStep = std::ldexp(1.0f, -p.jf.k);
-        p.jf.hiUnit = std::ldexp(1.0f, p.jf.k);
-        return p;
-    }
-};
-
-namespace
+namespace picgb::host
 {
     int checkSim(picgb_sim* s)
     {
@@ -593,30 +462,40 @@ extern "C"
     {
         if(!s)
             return PICGB_OK;
-        cudaSetDevice(s->cfg.device);
-        if(s->stream)
-            cudaStreamSynchronize(s->stream);
-        for(auto& sp : s->species)
-            sp->freeAll();
-        dfree(s->E);
-        dfree(s->B);
-        dfree(s->J);
-        dfree(s->rho);
-        dfree(s->status);
-        dfree(s->energy);
-        dfree(s->maxBits);
-        dfree(s->kindCount);
-        if(s->hostStatus)
-            cudaFreeHost(s->hostStatus);
-        profFlush(s);
-        for(auto e : s->eventPool)
-            cudaEventDestroy(e);
-        if(s->ownStream && s->stream)
-            cudaStreamDestroy(s->stream);
-        delete s;
-        return PICGB_OK;
+        if(s->inEnsemble)
+            return fail(PICGB_ERR_INVALID, "the handle belongs to an ensemble; destroy the ensemble instead");
+        return destroySim(s);
     }
+}
 
+int picgb::host::destroySim(picgb_sim* s)
+{
+    cudaSetDevice(s->cfg.device);
+    if(s->stream)
+        cudaStreamSynchronize(s->stream);
+    for(auto& sp : s->species)
+        sp->freeAll();
+    dfree(s->E);
+    dfree(s->B);
+    dfree(s->J);
+    dfree(s->rho);
+    dfree(s->status);
+    dfree(s->energy);
+    dfree(s->maxBits);
+    dfree(s->kindCount);
+    if(s->hostStatus)
+        cudaFreeHost(s->hostStatus);
+    profFlush(s);
+    for(auto e : s->eventPool)
+        cudaEventDestroy(e);
+    if(s->ownStream && s->stream)
+        cudaStreamDestroy(s->stream);
+    delete s;
+    return PICGB_OK;
+}
+
+extern "C"
+{
     int picgb_add_species(picgb_sim* s, const picgb_species_config* cfg, int32_t* index)
     {
         if(int r = checkSim(s))

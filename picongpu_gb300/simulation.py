@@ -116,15 +116,29 @@ class Simulation:
                            grid.device)
         h = ctypes.c_void_p()
         L.call("picgb_create", ctypes.byref(cfg), ctypes.byref(h))
+        self._init_handle(h, grid, owned=True)
+
+    def _init_handle(self, h, grid: Grid, owned: bool):
+        self.grid = grid
         self.handle = h
+        self._owned = owned
         self.species: list[Species] = []
         self.data_connector = DataConnector(self)
         self.current_step = 0
 
+    @classmethod
+    def borrowed(cls, handle: ctypes.c_void_p, grid: Grid, species: list[Species]) -> "Simulation":
+        """Wrapper of a handle owned elsewhere (a box of an ensemble); close() leaves it alive."""
+        self = cls.__new__(cls)
+        self._init_handle(handle, grid, owned=False)
+        self.species = list(species)
+        return self
+
     # ------------------------------------------------------------ lifetime
     def close(self):
         if self.handle:
-            L.load().picgb_destroy(self.handle)
+            if self._owned:
+                L.load().picgb_destroy(self.handle)
             self.handle = None
 
     def __enter__(self):

@@ -52,8 +52,9 @@ def test_struct_sizes_match_header():
     prog = r"""
 #include <stdio.h>
 #include "picgb.h"
-int main(void){printf("%zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), sizeof(picgb_species_config),
- sizeof(picgb_particles), sizeof(picgb_buffer_desc), sizeof(picgb_plasma_init));return 0;}
+int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), sizeof(picgb_species_config),
+ sizeof(picgb_particles), sizeof(picgb_buffer_desc), sizeof(picgb_plasma_init), sizeof(picgb_ensemble_config));
+ return 0;}
 """
     with tempfile.TemporaryDirectory() as d:
         c = os.path.join(d, "s.c")
@@ -62,7 +63,7 @@ int main(void){printf("%zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), sizeof
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     mine = [ctypes.sizeof(t) for t in (_lib.GridConfig, _lib.SpeciesConfig, _lib.Particles, _lib.BufferDesc,
-                                       _lib.PlasmaInit)]
+                                       _lib.PlasmaInit, _lib.EnsembleConfig)]
     assert mine == sizes
 
 
@@ -82,5 +83,8 @@ def test_errors_are_reported_not_raised(lib):
     with pytest.raises(pg.PicError) as e:
         pg.Simulation(pg.Grid(16, 16, 8))
     assert e.value.code in (pg._lib.ERR_CUDA, pg._lib.ERR_INVALID)
+    with pytest.raises(pg.PicError):
+        pg.Ensemble([(16, 16, 8), (24, 16, 8)])
     assert lib.picgb_step(None, 0) == pg._lib.ERR_INVALID
+    assert lib.picgb_ensemble_run(None, 1) == pg._lib.ERR_INVALID
     assert b"null" in lib.picgb_last_error()
