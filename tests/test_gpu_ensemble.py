@@ -53,7 +53,7 @@ def box_inputs(dims, seed):
     return out
 
 
-def make_ensemble(dims, inputs, shape="TSC", threads=256):
+def make_ensemble(dims, inputs, shape="TSC", threads=256, fields=True):
     ens = pg.Ensemble(dims, threads=threads)
     for sp in species(shape):
         ens.add_species(sp)
@@ -61,8 +61,9 @@ def make_ensemble(dims, inputs, shape="TSC", threads=256):
         box = ens.box(b)
         box.set_particles("e", pe)
         box.set_particles("i", pi)
-        box.set_field("E", E)
-        box.set_field("B", B)
+        if fields:
+            box.set_field("E", E)
+            box.set_field("B", B)
     return ens
 
 
@@ -85,8 +86,9 @@ def test_batched_step_matches_single_box_step(shape, threads):
 
 
 def test_batched_energies_follow_single_box_path():
+    """Quasi-neutral start with E = B = 0, so eps0 div E - rho starts (and stays) at zero."""
     inputs = box_inputs(DIMS, 23)
-    with make_ensemble(DIMS, inputs) as a, make_ensemble(DIMS, inputs) as b:
+    with make_ensemble(DIMS, inputs, fields=False) as a, make_ensemble(DIMS, inputs, fields=False) as b:
         a.run(10)
         b.run_sequential(10)
         for i in range(len(DIMS)):
