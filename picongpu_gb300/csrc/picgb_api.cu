@@ -49,8 +49,9 @@ PushParams picgb_sim::pushParams(Species const& s, bool deposit) const
     // deposited value is a running sum acc_k = sum DS * tmp with
     // |tmp| <= |q w| d / (V dt) and sum |DS| <= 2, so |acc| <= 2 |q| wmax dmax / (V dt)
     // =: vmax.  A tile node receives at most one value per particle of its
-    // supercell (< 2^cb).  With k = 31 - cb and vmax * 2^s <= 2^(61 - 2 cb) the sums
-    // of the high and of the low parts stay below 2^30 + 2^(cb - 1).
+    // supercell (at most 2^cb).  With k = min(31 - cb, 22) and
+    // vmax * 2^s <= 2^min(61 - 2 cb, k + 21), a high part stays within 2^21 and a low
+    // part within 2^(k - 1), and the sums of either over 2^cb values stay in int32.
     int cb = 1;
     while((1u << cb) < s.dev.cap)
         ++cb;
@@ -59,12 +60,13 @@ PushParams picgb_sim::pushParams(Species const& s, bool deposit) const
     int e = 0;
     if(vmax > 0.0 && std::isfinite(vmax))
         std::frexp(vmax, &e); // vmax < 2^e
-    int const sExp = std::min(std::max(61 - 2 * cb - e, -126), 126);
-    p.jf.k = 31 - cb;
+    int const k = std::min(31 - cb, 22);
+    int const sExp = std::min(std::max(std::min(61 - 2 * cb, k + 21) - e, -126), 126);
+    p.jf.k = k;
     p.jf.scale = std::ldexp(1.0f, sExp);
     p.jf.invScale = std::ldexp(1.0f, -sExp);
-    p.jf.hiStep = std::ldexp(1.0f, -p.jf.k);
-    p.jf.hiUnit = std::ldexp(1.0f, p.jf.k);
+    p.jf.hiStep = std::ldexp(1.0f, -k);
+    p.jf.hiUnit = std::ldexp(1.0f, k);
     return p;
 }
 

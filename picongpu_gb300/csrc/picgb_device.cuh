@@ -460,6 +460,20 @@ namespace picgb
         int base; // tile index of the particle's Esirkepov origin (cell + gridShift)
         JFixed f;
 
+        // Scale of the values passed to add(): 2^s in fixed point, 1 for floats.
+        __device__ __forceinline__ float unit() const
+        {
+#if PICGB_J_FIXED
+            return f.scale;
+#else
+            return 1.0f;
+#endif
+        }
+
+        // v in units of unit().  In fixed point: a = rint(v / 2^k) and the remainder
+        // r = v - a 2^k (exact), both rounded to integers by adding 1.5 * 2^23 (valid
+        // for magnitudes below 2^22, which the host's choice of s and k guarantees),
+        // so the whole conversion runs on the FMA pipe.
         template<int C>
         __device__ __forceinline__ void add(int ri, int rj, int rk, float v) const
         {
@@ -467,12 +481,14 @@ namespace picgb
             rotToReal<C>(ri, rj, rk, x, y, z);
             int const idx = C * TT + base + x + TX * (y + TY * z);
 #if PICGB_J_FIXED
+            constexpr float kMagic = 12582912.0f; // 1.5 * 2^23
+            constexpr int kMagicBits = 0x4B400000;
             int* hi = reinterpret_cast<int*>(J);
-            float const vs = fm(v, f.scale); // exact: power of two
-            float const a = rintf(fm(vs, f.hiStep));
-            float const r = __fmaf_rn(-a, f.hiUnit, vs); // exact (Sterbenz)
-            atomicAdd(hi + idx, __float2int_rn(a));
-            atomicAdd(hi + 3 * TT + idx, __float2int_rn(r));
+            float const t = __fmaf_rn(v, f.hiStep, kMagic); // kMagic + rint(v / 2^k)
+            float const a = __fsub_rn(t, kMagic);
+            float const r = __fmaf_rn(-a, f.hiUnit, v); // exact (Sterbenz)
+            atomicAdd(hi + idx, __float_as_int(t) - kMagicBits);
+            atomicAdd(hi + 3 * TT + idx, __float_as_int(__fadd_rn(r, kMagic)) - kMagicBits);
 #else
             atomicAdd(J + idx, v);
 #endif
@@ -618,17 +634,20 @@ namespace picgb
             float invVdt)
         {
             float const qv = fm(charge, invVdt);
+            // the accumulator's unit (a power of two) is applied to csd: exact, and the
+            // deposited values arrive already scaled
+            float const u = acc.unit();
             {
                 int const st[3] = {stat[1], stat[2], stat[0]};
                 float const a0[3] = {p0[1], p0[2], p0[0]}, a1[3] = {p1[1], p1[2], p1[0]};
-                cpt1D<0, kGeneral>(acc, st, a0, a1, fm(qv, g.dx));
+                cpt1D<0, kGeneral>(acc, st, a0, a1, fm(fm(qv, g.dx), u));
             }
             {
                 int const st[3] = {stat[2], stat[0], stat[1]};
                 float const a0[3] = {p0[2], p0[0], p0[1]}, a1[3] = {p1[2], p1[0], p1[1]};
-                cpt1D<1, kGeneral>(acc, st, a0, a1, fm(qv, g.dy));
+                cpt1D<1, kGeneral>(acc, st, a0, a1, fm(fm(qv, g.dy), u));
             }
-            cpt1D<2, kGeneral>(acc, stat, p0, p1, fm(qv, g.dz));
+            cpt1D<2, kGeneral>(acc, stat, p0, p1, fm(fm(qv, g.dz), u));
         }
     };
 

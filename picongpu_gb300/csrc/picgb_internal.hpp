@@ -10,9 +10,10 @@ namespace picgb
     struct GridParams; // picgb_device.cuh
 
     // Fixed-point format of the shared-memory J tile (PICGB_J_FIXED): a value v
-    // becomes v * 2^s units, split into a high part a (a multiple of 2^k) and a
-    // low part b.  The host picks s and k so that neither part's sum over the
-    // values of one tile node can leave the int32 range.
+    // becomes v * 2^s units, split into a high part a = rint(v 2^s / 2^k) and the
+    // low part v 2^s - a 2^k, each rounded to an integer.  The host picks s and k
+    // so that both parts stay below 2^22 in magnitude and neither part's sum over
+    // the values of one tile node can leave the int32 range.
     struct JFixed
     {
         float scale; // 2^s
