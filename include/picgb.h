@@ -345,6 +345,57 @@ extern "C"
         int32_t* threads,
         double* rates);
 
+    /* ------------------------------------------------------------ differentiable run */
+    /* Forward steps of the PIC cycle on particles kept in a fixed order and the hand-written
+     * adjoint of those steps (no counterpart in the reference, which has no gradients).  The
+     * forward step is Simulation::runOneStep with the fused deposit: gather, Boris, move and
+     * Esirkepov deposit per particle, then the Yee split.  The backward pass gives dL/d(initial
+     * state) from dL/d(final state): transposed curls for the field update, the transposed
+     * Jacobian of the Boris rotation and of Velocity for the push, a deposit of the adjoint
+     * force for the gather and a gather of the adjoint current with the derivatives of the
+     * Esirkepov weights for the deposit.  The forward keeps a state every checkpoint_every
+     * steps; the backward replays each segment from its checkpoint.  T = float (precision 4)
+     * or double (precision 8); all arrays are device memory the caller owns. */
+#define PICGB_DIFF_MAX_SPECIES 4
+    typedef struct picgb_diff picgb_diff;
+    typedef struct picgb_diff_config
+    {
+        int32_t nx, ny, nz;
+        double dx, dy, dz, dt, c, eps0;
+        int32_t shape; /* PICGB_SHAPE_CIC, _TSC or _PQS */
+        int32_t precision; /* 4 or 8 */
+        int32_t checkpoint_every;
+        int32_t device;
+    } picgb_diff_config;
+    typedef struct picgb_diff_species
+    {
+        double charge, mass; /* per real particle */
+        uint64_t n;
+    } picgb_diff_species;
+    /* E, B: [3][nz][ny][nx] of T; per species s: cell[s] [3][n] int32 (cell index per axis),
+     * pos[s] [3][n] T (in-cell position in [0,1)), mom[s] [3][n] T (macro-weighted momentum),
+     * w[s] [n] T (weighting; read by the forward and kept for the backward). */
+    typedef struct picgb_diff_state
+    {
+        void* E;
+        void* B;
+        int32_t nspecies;
+        int32_t* cell[PICGB_DIFF_MAX_SPECIES];
+        void* pos[PICGB_DIFF_MAX_SPECIES];
+        void* mom[PICGB_DIFF_MAX_SPECIES];
+        const void* w[PICGB_DIFF_MAX_SPECIES];
+    } picgb_diff_state;
+    int picgb_diff_create(const picgb_diff_config* cfg, int32_t nspecies, const picgb_diff_species* species, picgb_diff** out);
+    int picgb_diff_destroy(picgb_diff* d);
+    /* Advances `state` in place by nsteps; work is enqueued on `stream` (cudaStream_t). */
+    int picgb_diff_forward(picgb_diff* d, picgb_diff_state* state, uint32_t nsteps, void* stream);
+    /* grad: dL/dE, dL/dB, dL/dpos, dL/dmom of the state after the last forward; overwritten in
+     * place with the gradients with respect to the state before it (cell and w unused). */
+    int picgb_diff_backward(picgb_diff* d, picgb_diff_state* grad, void* stream);
+    /* Sum over the species' particles of (gamma - 1) m w c^2, in FP64 (KinEnergy.hpp:43-66
+     * without the low-energy branch); synchronises the stream. */
+    int picgb_diff_kinetic_energy(picgb_diff* d, const picgb_diff_state* state, int32_t species, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

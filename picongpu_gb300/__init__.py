@@ -1,10 +1,11 @@
 """GB300-native PIC cycle: Yee field solver, Boris push with form-factor gather,
 Esirkepov deposition and supercell bookkeeping, hand-written CUDA for sm_103a
 behind the C-ABI of include/picgb.h (libpicgb.so, built in-tree)."""
-from . import _lib
+from . import _lib, adjoint
 from ._lib import PicError, load
+from .adjoint import DiffPIC, DiffSpecies
 from .ensemble import Ensemble, autotune, plasma_init
 from .simulation import DataConnector, Grid, Simulation, Species
 
-__all__ = ["DataConnector", "Ensemble", "Grid", "PicError", "Simulation", "Species", "autotune", "load", "plasma_init",
-           "_lib"]
+__all__ = ["DataConnector", "DiffPIC", "DiffSpecies", "Ensemble", "Grid", "PicError", "Simulation", "Species", "autotune", "load", "plasma_init",
+           "adjoint", "_lib"]

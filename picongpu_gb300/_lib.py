@@ -61,6 +61,25 @@ class EnsembleConfig(ctypes.Structure):
     _fields_ = [("grid", GridConfig), ("nbox", c_int), ("dims", P(c_int)), ("threads", c_int)]
 
 
+DIFF_MAX_SPECIES = 4
+
+
+class DiffConfig(ctypes.Structure):
+    _fields_ = [("nx", c_int), ("ny", c_int), ("nz", c_int), ("dx", c_double), ("dy", c_double), ("dz", c_double),
+                ("dt", c_double), ("c", c_double), ("eps0", c_double), ("shape", c_int), ("precision", c_int),
+                ("checkpoint_every", c_int), ("device", c_int)]
+
+
+class DiffSpecies(ctypes.Structure):
+    _fields_ = [("charge", c_double), ("mass", c_double), ("n", c_uint64)]
+
+
+class DiffState(ctypes.Structure):
+    _fields_ = [("E", c_void_p), ("B", c_void_p), ("nspecies", c_int), ("cell", c_void_p * DIFF_MAX_SPECIES),
+                ("pos", c_void_p * DIFF_MAX_SPECIES), ("mom", c_void_p * DIFF_MAX_SPECIES),
+                ("w", c_void_p * DIFF_MAX_SPECIES)]
+
+
 # (name, restype, argtypes) of every symbol declared in include/picgb.h
 SIGNATURES = [
     ("picgb_abi_version", c_int, []),
@@ -112,6 +131,11 @@ SIGNATURES = [
     ("picgb_ensemble_autotune", c_int,
      [P(EnsembleConfig), c_int, P(SpeciesConfig), P(PlasmaInit), c_uint32, c_uint32, P(c_int), P(c_int),
       P(c_double)]),
+    ("picgb_diff_create", c_int, [P(DiffConfig), c_int, P(DiffSpecies), P(c_void_p)]),
+    ("picgb_diff_destroy", c_int, [c_void_p]),
+    ("picgb_diff_forward", c_int, [c_void_p, P(DiffState), c_uint32, c_void_p]),
+    ("picgb_diff_backward", c_int, [c_void_p, P(DiffState), c_void_p]),
+    ("picgb_diff_kinetic_energy", c_int, [c_void_p, P(DiffState), c_int, P(c_double), c_void_p]),
 ]
 
 KERNEL_CLASSES = {"push": 0, "compact": 1, "yee_b": 2, "yee_e": 3, "deposit": 4, "add_current": 5}

@@ -54,6 +54,7 @@ def test_struct_sizes_match_header():
 #include "picgb.h"
 int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), sizeof(picgb_species_config),
  sizeof(picgb_particles), sizeof(picgb_buffer_desc), sizeof(picgb_plasma_init), sizeof(picgb_ensemble_config));
+ printf("%zu %zu %zu\n", sizeof(picgb_diff_config), sizeof(picgb_diff_species), sizeof(picgb_diff_state));
  return 0;}
 """
     with tempfile.TemporaryDirectory() as d:
@@ -63,7 +64,8 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), si
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     mine = [ctypes.sizeof(t) for t in (_lib.GridConfig, _lib.SpeciesConfig, _lib.Particles, _lib.BufferDesc,
-                                       _lib.PlasmaInit, _lib.EnsembleConfig)]
+                                       _lib.PlasmaInit, _lib.EnsembleConfig, _lib.DiffConfig, _lib.DiffSpecies,
+                                       _lib.DiffState)]
     assert mine == sizes
 
 
