@@ -374,6 +374,95 @@ def run_ensemble(args, local_rank):
     return out
 
 
+# ---------------------------------------------------------------------- differentiable run
+def adjoint_case(A, n, ppc, precision, checkpoint_every):
+    dens = (0.1 / DT) ** 2
+    npart = n ** 3 * ppc
+    sp = [A.DiffSpecies("e", -1.0, 1.0, npart), A.DiffSpecies("i", 1.0, MASS_P, npart)]
+    pic = A.DiffPIC(n, n, n, sp, dt=DT, shape="TSC", precision=precision, checkpoint_every=checkpoint_every)
+    parts = [A.thermal_species(pic, 0, ppc, dens, 0.02, seed=11),
+             A.thermal_species(pic, 1, ppc, dens, 0.02 / np.sqrt(MASS_P), seed=12, position_seed=11)]
+    return pic, parts
+
+
+def adjoint_loss(A, torch, pic, parts, a0, waist, steps, n):
+    E, B = A.gaussian_pulse(pic, a0, waist, 12.0, 6.0, (n / 4.0, n / 2.0, n / 2.0))
+    _, _, out = A.run(pic, steps, E, B, parts)
+    return A.kinetic_energy(out[0]["mom"], parts[0]["w"], 1.0)
+
+
+def run_adjoint(args):
+    """64^3 TSC e/p plasma with a Gaussian pulse (a0 = 1, waist 6, wavelength 12): forward and
+    adjoint timing over the full run (FP32, checkpoints every 20 steps), the plain single-box
+    step on the same plasma, and an FP64 central-difference check of dL/da0 on a shorter run."""
+    import torch
+
+    import picongpu_gb300 as pg
+    from picongpu_gb300 import adjoint as A
+
+    n, ppc, K = 64, 8, 20
+    steps = args.adjoint_steps
+    pic, parts = adjoint_case(A, n, ppc, 4, K)
+    a0 = torch.tensor(1.0, device="cuda", requires_grad=True)
+    waist = torch.tensor(6.0, device="cuda", requires_grad=True)
+    # warm-up (builds the kernels' caches and the checkpoint buffers)
+    adjoint_loss(A, torch, pic, parts, a0, waist, 2, n).backward()
+    a0.grad = None
+    waist.grad = None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    L = adjoint_loss(A, torch, pic, parts, a0, waist, steps, n)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    L.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    fwd_ms, bwd_ms = 1e3 * (t1 - t0) / steps, 1e3 * (t2 - t1) / steps
+    grad_a0 = float(a0.grad)
+    pic.close()
+    # the plain single-box step on the same plasma (production path)
+    g = pg.Grid(n, n, n, dt=DT)
+    with pg.Simulation(g) as sim:
+        sim.add_species(pg.Species("e", -1.0, 1.0, shape="TSC"))
+        sim.add_species(pg.Species("i", 1.0, MASS_P, shape="TSC"))
+        dens = (0.1 / DT) ** 2
+        sim.init_plasma("e", ppc, dens, 0.02, seed=1, position_seed=7)
+        sim.init_plasma("i", ppc, dens, 0.02 / np.sqrt(MASS_P), seed=2, position_seed=7)
+        for _ in range(3):
+            sim.step()
+        sim.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(20):
+            sim.step()
+        sim.synchronize()
+        plain_ms = 1e3 * (time.perf_counter() - t0) / 20
+    # FP64: adjoint against central differences (h = 1e-4 relative) on a shorter run
+    fd_steps = args.adjoint_fd_steps
+    p64, parts64 = adjoint_case(A, n, ppc, 8, 10)
+    a = torch.tensor(1.0, dtype=torch.float64, device="cuda", requires_grad=True)
+    w = torch.tensor(6.0, dtype=torch.float64, device="cuda")
+    adjoint_loss(A, torch, p64, parts64, a, w, fd_steps, n).backward()
+    g64 = float(a.grad)
+    h = 1e-4
+    with torch.no_grad():
+        lp = float(adjoint_loss(A, torch, p64, parts64, torch.tensor(1 + h, dtype=torch.float64, device="cuda"), w,
+                                fd_steps, n))
+        lm = float(adjoint_loss(A, torch, p64, parts64, torch.tensor(1 - h, dtype=torch.float64, device="cuda"), w,
+                                fd_steps, n))
+    fd = (lp - lm) / (2 * h)
+    p64.close()
+    return {"workload": f"{n}^3 cells, TSC, e/p 2 x {ppc} ppc (u_th 0.02), Gaussian pulse a0 = 1, waist 6, "
+                        f"wavelength 12 in E/B, loss = electron kinetic energy after {steps} steps, "
+                        f"checkpoints every {K} steps, fp32",
+            "steps": steps, "loss": float(L.detach()), "grad_a0": grad_a0,
+            "forward_ms_per_step": round(fwd_ms, 4), "adjoint_ms_per_step": round(bwd_ms, 4),
+            "adjoint_over_forward": round(bwd_ms / fwd_ms, 3),
+            "plain_step_ms": round(plain_ms, 4), "adjoint_over_plain_step": round(bwd_ms / plain_ms, 3),
+            "fd_check": {"precision": "fp64", "steps": fd_steps, "h_rel": h, "adjoint": g64, "central_difference": fd,
+                         "rel_err": abs(g64 - fd) / abs(fd) if fd else None},
+            "timing": "host clock around forward and backward with device synchronisation"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -386,6 +475,9 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-boxes", type=int, default=512)
     ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=300)
+    ap.add_argument("--adjoint-fd-steps", type=int, default=20)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -428,6 +520,9 @@ def main():
     batched = None
     if not args.no_ensemble:
         batched = run_ensemble(args, local_rank)
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = run_adjoint(args)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         val, cores, sample = cpu_sample_rate(wl, 10, 1, budget_s=20.0)
@@ -436,7 +531,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded device init)", "config": config,
             "particles": r["npart"], "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"],
-            "clocks": r["clocks"], "gpu_launches": r["launches"], "batched": batched}
+            "clocks": r["clocks"], "gpu_launches": r["launches"], "batched": batched, "adjoint": adjoint}
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch

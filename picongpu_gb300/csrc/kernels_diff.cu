@@ -27,7 +27,6 @@ namespace picgb::diff
         int cell[3], newCell[3];
         T pos[3], mom[3], newPos[3], newMom[3], vel[3], dp[3];
         T qw, mw;
-        DGather<SHAPE, T> gw;
         T Ef[3], Bf[3];
         DBoris<T> boris;
         DTrajectory<SHAPE, T> traj;
@@ -44,13 +43,19 @@ namespace picgb::diff
             T const w = sp.w[p];
             qw = sp.charge * w;
             mw = sp.mass * w;
-            gw.compute(cell, pos);
-            Ef[0] = gw.template value<0>(E, g);
-            Ef[1] = gw.template value<1>(E + nc, g);
-            Ef[2] = gw.template value<2>(E + 2 * nc, g);
-            Bf[0] = gw.template value<3>(B, g);
-            Bf[1] = gw.template value<4>(B + nc, g);
-            Bf[2] = gw.template value<5>(B + 2 * nc, g);
+            // the gather weights are not kept: the adjoint recomputes them at its end, which keeps
+            // them out of the registers during the deposit adjoint
+            DGather<SHAPE, T> gw;
+            gw.compute(cell, pos, g);
+            T f6[6];
+#pragma unroll 1
+            for(int comp = 0; comp < 6; ++comp)
+                f6[comp] = gw.valueAt(comp < 3 ? E + comp * nc : B + (comp - 3) * nc, comp);
+            for(int d = 0; d < 3; ++d)
+            {
+                Ef[d] = f6[d];
+                Bf[d] = f6[3 + d];
+            }
             boris.forward(qw, mw, Ef, Bf, g.dt, g.c, mom, newMom);
             dVelocity(mw, g.c, newMom, vel);
             int const n3[3] = {g.nx, g.ny, g.nz};
@@ -67,7 +72,7 @@ namespace picgb::diff
                 newPos[d] = (x - T(m)) + T(0.5);
                 newCell[d] = wrapIdx(cell[d] + m, n3[d]);
             }
-            traj.compute(newCell, newPos, dp);
+            traj.compute(newCell, newPos, dp, g);
         }
 
         __device__ T qvdt(DiffGrid<T> const& g) const { return qw / (g.dx * g.dy * g.dz * g.dt); }
@@ -133,12 +138,16 @@ namespace picgb::diff
         T lp[3], lE[3], lB[3];
         st.boris.adjoint(st.qw, st.mw, st.Bf, g.dt, g.c, lmom, lp, lE, lB);
         T gpos[3] = {T(0), T(0), T(0)};
-        st.gw.template adjoint<0>(E, lamE, g, lE[0], gpos);
-        st.gw.template adjoint<1>(E + nc, lamE + nc, g, lE[1], gpos);
-        st.gw.template adjoint<2>(E + 2 * nc, lamE + 2 * nc, g, lE[2], gpos);
-        st.gw.template adjoint<3>(B, lamB, g, lB[0], gpos);
-        st.gw.template adjoint<4>(B + nc, lamB + nc, g, lB[1], gpos);
-        st.gw.template adjoint<5>(B + 2 * nc, lamB + 2 * nc, g, lB[2], gpos);
+        DGather<SHAPE, T> gw;
+        gw.compute(st.cell, st.pos, g);
+        T const l6[6] = {lE[0], lE[1], lE[2], lB[0], lB[1], lB[2]};
+#pragma unroll 1
+        for(int comp = 0; comp < 6; ++comp)
+        {
+            size_t const o = size_t(comp % 3) * nc;
+            T const lam = comp == 0 ? l6[0] : comp == 1 ? l6[1] : comp == 2 ? l6[2] : comp == 3 ? l6[3] : comp == 4 ? l6[4] : l6[5];
+            gw.adjointAt(comp < 3 ? E + o : B + o, comp < 3 ? lamE + o : lamB + o, comp, lam, gpos);
+        }
         for(int d = 0; d < 3; ++d)
         {
             lamPos[d * sp.n + p] = lposOld[d] + gpos[d];

@@ -204,8 +204,8 @@ extern "C"
         if(!cfg || !out || nspecies < 0 || nspecies > kMaxSpecies || (nspecies && !species))
             return fail(PICGB_ERR_INVALID, "invalid arguments (at most %d species)", kMaxSpecies);
         *out = nullptr;
-        if(cfg->nx <= 0 || cfg->ny <= 0 || cfg->nz <= 0)
-            return fail(PICGB_ERR_INVALID, "grid must be positive");
+        if(cfg->nx < 4 || cfg->ny < 4 || cfg->nz < 4 || double(cfg->nx) * cfg->ny * cfg->nz >= 4294967296.0)
+            return fail(PICGB_ERR_INVALID, "grid needs at least 4 cells per axis and fewer than 2^32 cells");
         if(cfg->precision != 4 && cfg->precision != 8)
             return fail(PICGB_ERR_INVALID, "precision must be 4 (float) or 8 (double)");
         if(cfg->shape < PICGB_SHAPE_CIC || cfg->shape > PICGB_SHAPE_PQS)

@@ -27,11 +27,8 @@ namespace picgb::diff
         T dx, dy, dz, dt, c, eps0;
     };
 
-    __device__ __forceinline__ int wrapIdx(int i, int n)
-    {
-        i %= n;
-        return i < 0 ? i + n : i;
-    }
+    // periodic index for i in [-n, 2n) (stencil offsets of a few cells; grids have n >= 4)
+    __device__ __forceinline__ int wrapIdx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
     template<typename T>
     __device__ __forceinline__ T cellSize(DiffGrid<T> const& g, int d)
@@ -90,6 +87,7 @@ namespace picgb::diff
         }
 
         // ChargeAssignment (the piecewise function of the distance) and its derivative
+        // both branches are evaluated and selected (no divergence between lanes)
         __device__ static T ca(T t)
         {
             T const a = t < T(0) ? -t : t;
@@ -97,17 +95,15 @@ namespace picgb::diff
                 return a < T(1) ? T(1) - a : T(0);
             else if constexpr(SHAPE == 2)
             {
-                if(a < T(0.5))
-                    return T(0.75) - t * t;
                 T const b = T(1.5) - a;
-                return a < T(1.5) ? T(0.5) * b * b : T(0);
+                T const inner = T(0.75) - t * t, outer = T(0.5) * b * b;
+                return a < T(0.5) ? inner : (a < T(1.5) ? outer : T(0));
             }
             else
             {
-                if(a < T(1))
-                    return (T(4) - T(6) * t * t + T(3) * a * a * a) / T(6);
                 T const b = T(2) - a;
-                return a < T(2) ? b * b * b / T(6) : T(0);
+                T const inner = (T(4) - T(6) * t * t + T(3) * a * a * a) / T(6), outer = b * b * b / T(6);
+                return a < T(1) ? inner : (a < T(2) ? outer : T(0));
             }
         }
 
@@ -119,16 +115,14 @@ namespace picgb::diff
                 return a < T(1) ? -sg : T(0);
             else if constexpr(SHAPE == 2)
             {
-                if(a < T(0.5))
-                    return T(-2) * t;
-                return a < T(1.5) ? -(T(1.5) - a) * sg : T(0);
+                T const inner = T(-2) * t, outer = -(T(1.5) - a) * sg;
+                return a < T(0.5) ? inner : (a < T(1.5) ? outer : T(0));
             }
             else
             {
-                if(a < T(1))
-                    return T(-2) * t + T(1.5) * t * a;
                 T const b = T(2) - a;
-                return a < T(2) ? T(-0.5) * b * b * sg : T(0);
+                T const inner = T(-2) * t + T(1.5) * t * a, outer = T(-0.5) * b * b * sg;
+                return a < T(1) ? inner : (a < T(2) ? outer : T(0));
             }
         }
     };
@@ -147,12 +141,14 @@ namespace picgb::diff
     {
         using SH = DShape<SHAPE, T>;
         static constexpr int S = SH::supp;
-        int first[2][3];
+        uint32_t off[2][3][S]; // wrapped node index times the axis stride
         T w[2][3][S];
         T dw[2][3][S];
 
-        __device__ void compute(int const cell[3], T const pos[3])
+        __device__ void compute(int const cell[3], T const pos[3], DiffGrid<T> const& g)
         {
+            int const n3[3] = {g.nx, g.ny, g.nz};
+            uint32_t const stride[3] = {1u, uint32_t(g.nx), uint32_t(g.nx) * uint32_t(g.ny)};
 #pragma unroll
             for(int a = 0; a < 2; ++a)
 #pragma unroll
@@ -164,16 +160,40 @@ namespace picgb::diff
                         s = v >= T(-0.5) ? 0 : -1;
                     else
                         s = v >= T(0) ? 1 : 0;
-                    first[a][d] = cell[d] + s + SH::osBegin;
+                    int const first = cell[d] + s + SH::osBegin;
+#pragma unroll
+                    for(int t = 0; t < S; ++t)
+                        off[a][d][t] = uint32_t(wrapIdx(first + t, n3[d])) * stride[d];
                     SH::base(v - T(s) + T(0.5), w[a][d], dw[a][d]);
                 }
         }
 
-        // component COMP (0..2 E_x..E_z, 3..5 B_x..B_z) of field F
-        template<int COMP>
-        __device__ T value(T const* __restrict__ F, DiffGrid<T> const& g) const
+        // weights and node offsets of one axis for staggering a (0 or 1), without dynamic indexing
+        __device__ __forceinline__ void axis(int d, int a, T wt[S], T dwt[S], uint32_t o[S]) const
         {
-            constexpr int ax = stagger(COMP, 0), ay = stagger(COMP, 1), az = stagger(COMP, 2);
+#pragma unroll
+            for(int t = 0; t < S; ++t)
+            {
+                T const w0 = d == 0 ? w[0][0][t] : (d == 1 ? w[0][1][t] : w[0][2][t]);
+                T const w1 = d == 0 ? w[1][0][t] : (d == 1 ? w[1][1][t] : w[1][2][t]);
+                T const d0 = d == 0 ? dw[0][0][t] : (d == 1 ? dw[0][1][t] : dw[0][2][t]);
+                T const d1 = d == 0 ? dw[1][0][t] : (d == 1 ? dw[1][1][t] : dw[1][2][t]);
+                uint32_t const o0 = d == 0 ? off[0][0][t] : (d == 1 ? off[0][1][t] : off[0][2][t]);
+                uint32_t const o1 = d == 0 ? off[1][0][t] : (d == 1 ? off[1][1][t] : off[1][2][t]);
+                wt[t] = a ? w1 : w0;
+                dwt[t] = a ? d1 : d0;
+                o[t] = a ? o1 : o0;
+            }
+        }
+
+        // component comp (0..2 E_x..E_z, 3..5 B_x..B_z, a runtime value) of field F
+        __device__ T valueAt(T const* __restrict__ F, int comp) const
+        {
+            T wx[S], wy[S], wz[S], dx[S], dy[S], dz[S];
+            uint32_t ox[S], oy[S], oz[S];
+            axis(0, stagger(comp, 0), wx, dx, ox);
+            axis(1, stagger(comp, 1), wy, dy, oy);
+            axis(2, stagger(comp, 2), wz, dz, oz);
             T rz = T(0);
 #pragma unroll
             for(int z = 0; z < S; ++z)
@@ -185,23 +205,24 @@ namespace picgb::diff
                     T rx = T(0);
 #pragma unroll
                     for(int x = 0; x < S; ++x)
-                        rx += w[ax][0][x]
-                            * F[cellIndex(g, first[ax][0] + x, first[ay][1] + y, first[az][2] + z)];
-                    ry += w[ay][1][y] * rx;
+                        rx += wx[x] * F[oz[z] + oy[y] + ox[x]];
+                    ry += wy[y] * rx;
                 }
-                rz += w[az][2][z] * ry;
+                rz += wz[z] * ry;
             }
             return rz;
         }
 
-        // adjoint of value(): lam * weights scattered into lamF, and the position gradient
-        template<int COMP>
-        __device__ void adjoint(T const* __restrict__ F, T* __restrict__ lamF, DiffGrid<T> const& g, T lam, T gpos[3])
-            const
+        // adjoint of valueAt(): lam * weights scattered into lamF, and the position gradient
+        __device__ void adjointAt(T const* __restrict__ F, T* __restrict__ lamF, int comp, T lam, T gpos[3]) const
         {
-            constexpr int ax = stagger(COMP, 0), ay = stagger(COMP, 1), az = stagger(COMP, 2);
             if(lam == T(0))
                 return;
+            T wx[S], wy[S], wz[S], dx[S], dy[S], dz[S];
+            uint32_t ox[S], oy[S], oz[S];
+            axis(0, stagger(comp, 0), wx, dx, ox);
+            axis(1, stagger(comp, 1), wy, dy, oy);
+            axis(2, stagger(comp, 2), wz, dz, oz);
 #pragma unroll
             for(int z = 0; z < S; ++z)
 #pragma unroll
@@ -209,13 +230,12 @@ namespace picgb::diff
 #pragma unroll
                     for(int x = 0; x < S; ++x)
                     {
-                        size_t const i = cellIndex(g, first[ax][0] + x, first[ay][1] + y, first[az][2] + z);
-                        T const wx = w[ax][0][x], wy = w[ay][1][y], wz = w[az][2][z];
-                        atomicAdd(lamF + i, lam * wx * wy * wz);
+                        uint32_t const i = oz[z] + oy[y] + ox[x];
+                        atomicAdd(lamF + i, lam * wx[x] * wy[y] * wz[z]);
                         T const f = F[i] * lam;
-                        gpos[0] += f * dw[ax][0][x] * wy * wz;
-                        gpos[1] += f * wx * dw[ay][1][y] * wz;
-                        gpos[2] += f * wx * wy * dw[az][2][z];
+                        gpos[0] += f * dx[x] * wy[y] * wz[z];
+                        gpos[1] += f * wx[x] * dy[y] * wz[z];
+                        gpos[2] += f * wx[x] * wy[y] * dz[z];
                     }
         }
     };
@@ -320,22 +340,52 @@ namespace picgb::diff
             lp[d] += lv[d] / D - p[d] * pl / (c * c * D * D * D);
     }
 
+    // a[i] for a runtime axis i without dynamic register indexing
+    template<typename V>
+    __device__ __forceinline__ V sel3(V const a[3], int i)
+    {
+        return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]);
+    }
+
+    template<typename V>
+    __device__ __forceinline__ void add3(V a[3], int i, V v)
+    {
+        a[0] += i == 0 ? v : V(0);
+        a[1] += i == 1 ? v : V(0);
+        a[2] += i == 2 ? v : V(0);
+    }
+
+    // Rotations of the three current components: rotated axis r of component C is real axis rot(C, r)
+    // (J_x: i->y, j->z, k->x; J_y: i->z, j->x, k->y; J_z: i->x, j->y, k->z).
+    __host__ __device__ constexpr int rot(int C, int r)
+    {
+        return C == 0 ? (r == 0 ? 1 : (r == 1 ? 2 : 0)) : (C == 1 ? (r == 0 ? 2 : (r == 1 ? 0 : 1)) : r);
+    }
+
     // Esirkepov trajectory in the virtual grid: start q0 and end q1 relative to the
-    // origin cell (new cell + shift), and the per-axis leave flags.
+    // origin cell (new cell + shift), the per-axis leave flags, and the wrapped,
+    // strided offsets of the N = supp + 1 nodes per axis the deposit can touch.
     template<int SHAPE, typename T>
     struct DTrajectory
     {
+        using SH = DShape<SHAPE, T>;
+        static constexpr int B0 = SH::caBegin;
+        static constexpr int N = SH::caEnd - SH::caBegin + 1;
         T q0[3], q1[3];
-        int origin[3];
         int leave[3];
+        uint32_t node[3][N];
+        T s0[3][N], s1[3][N]; // S(node - q0), S(node - q1) per axis
 
-        __device__ void compute(int const newCell[3], T const pos[3], T const dp[3])
+        __device__ void compute(int const newCell[3], T const pos[3], T const dp[3], DiffGrid<T> const& g)
         {
+            int const n3[3] = {g.nx, g.ny, g.nz};
+            uint32_t const stride[3] = {1u, uint32_t(g.nx), uint32_t(g.nx) * uint32_t(g.ny)};
+#pragma unroll
             for(int d = 0; d < 3; ++d)
             {
                 T const p0 = pos[d] - dp[d], p1 = pos[d];
                 int iS, iE;
-                if constexpr(DShape<SHAPE, T>::even)
+                if constexpr(SH::even)
                 {
                     iS = int(floor(p0));
                     iE = int(floor(p1));
@@ -347,63 +397,199 @@ namespace picgb::diff
                 }
                 int const gs = iS < iE ? iS : iE;
                 leave[d] = iS != iE ? 1 : 0;
-                origin[d] = newCell[d] + gs;
                 q0[d] = p0 - T(gs);
                 q1[d] = p1 - T(gs);
+                int const o = newCell[d] + gs + B0;
+#pragma unroll
+                for(int t = 0; t < N; ++t)
+                {
+                    node[d][t] = uint32_t(wrapIdx(o + t, n3[d])) * stride[d];
+                    s0[d][t] = SH::ca(T(B0 + t) - q0[d]);
+                    s1[d][t] = SH::ca(T(B0 + t) - q1[d]);
+                }
+            }
+        }
+
+        // shape values at the N nodes of axis d for the start and end positions, and the node offsets
+        __device__ __forceinline__ void line(int d, T a0[], T a1[], uint32_t nd[]) const
+        {
+#pragma unroll
+            for(int t = 0; t < N; ++t)
+            {
+                a0[t] = d == 0 ? s0[0][t] : (d == 1 ? s0[1][t] : s0[2][t]);
+                a1[t] = d == 0 ? s1[0][t] : (d == 1 ? s1[1][t] : s1[2][t]);
+                nd[t] = d == 0 ? node[0][t] : (d == 1 ? node[1][t] : node[2][t]);
+            }
+        }
+
+        // derivatives S'(node - q) of axis d for the start and end positions
+        __device__ __forceinline__ void slope(int d, T a0[], T a1[]) const
+        {
+            T const u = sel3(q0, d), v = sel3(q1, d);
+#pragma unroll
+            for(int t = 0; t < N; ++t)
+            {
+                a0[t] = SH::dca(T(B0 + t) - u);
+                a1[t] = SH::dca(T(B0 + t) - v);
             }
         }
     };
 
-    // Rotations of the three current components: rotated axis r of component C is real axis rot(C, r)
-    // (J_x: i->y, j->z, k->x; J_y: i->z, j->x, k->y; J_z: i->x, j->y, k->z).
-    __host__ __device__ constexpr int rot(int C, int r)
-    {
-        return C == 0 ? (r == 0 ? 1 : (r == 1 ? 2 : 0)) : (C == 1 ? (r == 0 ? 2 : (r == 1 ? 0 : 1)) : r);
-    }
-
-    // Esirkepov deposit of one particle (all three components) into J with atomics.
+    // One rotated component C of the Esirkepov deposit (cptCurrent1D, Esirkepov.hpp:147-242):
+    // loops with fixed extents and the leave flags as predicates, so everything stays in registers.
     template<int SHAPE, typename T>
-    __device__ void esirkepovDeposit(
+    __device__ __forceinline__ void esirkepovComponent(
+        int const C,
         DTrajectory<SHAPE, T> const& tr,
-        T qvdt, // charge * weighting / (V dt)
+        T qvdt,
         DiffGrid<T> const& g,
         T* __restrict__ J)
     {
-        using SH = DShape<SHAPE, T>;
-        constexpr int B0 = SH::caBegin, E0 = SH::caEnd;
-        size_t const nc = size_t(g.nx) * g.ny * g.nz;
-        for(int C = 0; C < 3; ++C)
-        {
-            int const ai = rot(C, 0), aj = rot(C, 1), ak = rot(C, 2);
-            if(tr.q0[ak] == tr.q1[ak])
-                continue;
-            T const csd = qvdt * cellSize(g, ak);
-            int const ei = E0 + tr.leave[ai], ej = E0 + tr.leave[aj], ek = E0 + tr.leave[ak] - 1;
-            for(int i = B0; i < ei; ++i)
+        using TR = DTrajectory<SHAPE, T>;
+        constexpr int N = TR::N;
+        int const ai = rot(C, 0), aj = rot(C, 1), ak = rot(C, 2);
+        if(sel3(tr.q0, ak) == sel3(tr.q1, ak))
+            return;
+        T const csd = qvdt * cellSize(g, ak);
+        T s0i[N], s1i[N], s0j[N], s1j[N], s0k[N], s1k[N];
+        uint32_t ndi[N], ndj[N], ndk[N];
+        tr.line(ai, s0i, s1i, ndi);
+        tr.line(aj, s0j, s1j, ndj);
+        tr.line(ak, s0k, s1k, ndk);
+        // node counts: N - 1 without the leave node; the running sum along k has one node less
+        int const ni = N - 1 + sel3(tr.leave, ai), nj = N - 1 + sel3(tr.leave, aj), nk = N - 2 + sel3(tr.leave, ak);
+        T* const Jc = J + size_t(C) * g.nx * g.ny * g.nz;
+#pragma unroll
+        for(int i = 0; i < N; ++i)
+#pragma unroll
+            for(int j = 0; j < N; ++j)
             {
-                T const s0i = SH::ca(T(i) - tr.q0[ai]), s1i = SH::ca(T(i) - tr.q1[ai]);
-                for(int j = B0; j < ej; ++j)
-                {
-                    T const s0j = SH::ca(T(j) - tr.q0[aj]), s1j = SH::ca(T(j) - tr.q1[aj]);
-                    // -csd (S0i S0j / 3 + S1i S0j / 6 + S0i S1j / 6 + S1i S1j / 3) (Esirkepov.hpp:214-215)
-                    T const tmp = -csd
-                        * (s0i * s0j / T(3) + (s1i * s0j + s0i * s1j) / T(6) + s1i * s1j / T(3));
-                    T run = T(0);
-                    for(int k = B0; k < ek; ++k)
+                if(i >= ni || j >= nj)
+                    continue;
+                // -csd (S0i S0j / 3 + S1i S0j / 6 + S0i S1j / 6 + S1i S1j / 3) (Esirkepov.hpp:214-215)
+                T const tmp = -csd
+                    * (s0i[i] * s0j[j] / T(3) + (s1i[i] * s0j[j] + s0i[i] * s1j[j]) / T(6) + s1i[i] * s1j[j] / T(3));
+                T run = T(0);
+                uint32_t const base = ndi[i] + ndj[j];
+#pragma unroll
+                for(int k = 0; k < N - 1; ++k)
+                    if(k < nk)
                     {
-                        run += (SH::ca(T(k) - tr.q1[ak]) - SH::ca(T(k) - tr.q0[ak])) * tmp;
-                        int n[3];
-                        n[ai] = tr.origin[ai] + i;
-                        n[aj] = tr.origin[aj] + j;
-                        n[ak] = tr.origin[ak] + k;
-                        atomicAdd(J + C * nc + cellIndex(g, n[0], n[1], n[2]), run);
+                        run += (s1k[k] - s0k[k]) * tmp;
+                        atomicAdd(Jc + base + ndk[k], run);
                     }
-                }
             }
-        }
     }
 
-    // Adjoint of esirkepovDeposit: given lamJ, the gradients with respect to q0 and q1 (real axes).
+    template<int SHAPE, typename T>
+    __device__ void esirkepovDeposit(DTrajectory<SHAPE, T> const& tr, T qvdt, DiffGrid<T> const& g, T* __restrict__ J)
+    {
+#pragma unroll 1
+        for(int C = 0; C < 3; ++C)
+            esirkepovComponent(C, tr, qvdt, g, J);
+    }
+
+    // Adjoint of esirkepovComponent: with J(i, j, k) = tmp(i, j) D_k, D_k = sum_{k' <= k} dS_k',
+    // tmp = -csd (S0i S0j / 3 + S1i S0j / 6 + S0i S1j / 6 + S1i S1j / 3), the gradients of the
+    // loss with respect to the rotated start/end positions are accumulated in gq0, gq1
+    // (real axes) through dS(n - q)/dq = -S'(n - q).
+    template<int SHAPE, typename T>
+    __device__ __forceinline__ void esirkepovComponentAdjoint(
+        int const C,
+        DTrajectory<SHAPE, T> const& tr,
+        T qvdt,
+        DiffGrid<T> const& g,
+        T const* __restrict__ lamJ,
+        T gq0[3],
+        T gq1[3])
+    {
+        using TR = DTrajectory<SHAPE, T>;
+        using SH = DShape<SHAPE, T>;
+        constexpr int N = TR::N;
+        int const ai = rot(C, 0), aj = rot(C, 1), ak = rot(C, 2);
+        if(sel3(tr.q0, ak) == sel3(tr.q1, ak))
+            return;
+        T const csd = qvdt * cellSize(g, ak);
+        T s0i[N], s1i[N], s0j[N], s1j[N], s0k[N], s1k[N];
+        uint32_t ndi[N], ndj[N], ndk[N];
+        tr.line(ai, s0i, s1i, ndi);
+        tr.line(aj, s0j, s1j, ndj);
+        tr.line(ak, s0k, s1k, ndk);
+        int const ni = N - 1 + sel3(tr.leave, ai), nj = N - 1 + sel3(tr.leave, aj), nk = N - 2 + sel3(tr.leave, ak);
+        T const* const Lc = lamJ + size_t(C) * g.nx * g.ny * g.nz;
+        T ls0i[N], ls1i[N], ls0j[N], ls1j[N], lds[N];
+#pragma unroll
+        for(int t = 0; t < N; ++t)
+            ls0i[t] = ls1i[t] = ls0j[t] = ls1j[t] = lds[t] = T(0);
+#pragma unroll
+        for(int i = 0; i < N; ++i)
+#pragma unroll
+            for(int j = 0; j < N; ++j)
+            {
+                if(i >= ni || j >= nj)
+                    continue;
+                T const tmp = -csd
+                    * (s0i[i] * s0j[j] / T(3) + (s1i[i] * s0j[j] + s0i[i] * s1j[j]) / T(6) + s1i[i] * s1j[j] / T(3));
+                uint32_t const base = ndi[i] + ndj[j];
+                // ltmp = sum_k lam_k D_k; dL/d(dS_k') = sum_{k >= k'} lam_k tmp
+                T ltmp = T(0), D = T(0), lamk[N];
+#pragma unroll
+                for(int k = 0; k < N - 1; ++k)
+                {
+                    lamk[k] = T(0);
+                    if(k < nk)
+                    {
+                        D += s1k[k] - s0k[k];
+                        T const lam = Lc[base + ndk[k]];
+                        ltmp += lam * D;
+                        lamk[k] = lam * tmp;
+                    }
+                }
+                T acc = T(0);
+#pragma unroll
+                for(int k = N - 2; k >= 0; --k)
+                {
+                    acc += lamk[k];
+                    lds[k] += acc;
+                }
+                T const lt = -csd * ltmp;
+                ls0i[i] += lt * (s0j[j] / T(3) + s1j[j] / T(6));
+                ls1i[i] += lt * (s0j[j] / T(6) + s1j[j] / T(3));
+                ls0j[j] += lt * (s0i[i] / T(3) + s1i[i] / T(6));
+                ls1j[j] += lt * (s0i[i] / T(6) + s1i[i] / T(3));
+            }
+        T g0i = T(0), g1i = T(0), g0j = T(0), g1j = T(0), g0k = T(0), g1k = T(0);
+        T d0[N], d1[N];
+        tr.slope(ai, d0, d1);
+#pragma unroll
+        for(int t = 0; t < N; ++t)
+        {
+            g0i -= ls0i[t] * d0[t];
+            g1i -= ls1i[t] * d1[t];
+        }
+        tr.slope(aj, d0, d1);
+#pragma unroll
+        for(int t = 0; t < N; ++t)
+        {
+            g0j -= ls0j[t] * d0[t];
+            g1j -= ls1j[t] * d1[t];
+        }
+        tr.slope(ak, d0, d1);
+#pragma unroll
+        for(int t = 0; t < N; ++t)
+        {
+            // dS_k = S1_k - S0_k
+            g1k -= lds[t] * d1[t];
+            g0k += lds[t] * d0[t];
+        }
+        add3(gq0, ai, g0i);
+        add3(gq1, ai, g1i);
+        add3(gq0, aj, g0j);
+        add3(gq1, aj, g1j);
+        add3(gq0, ak, g0k);
+        add3(gq1, ak, g1k);
+    }
+
     template<int SHAPE, typename T>
     __device__ void esirkepovAdjoint(
         DTrajectory<SHAPE, T> const& tr,
@@ -413,72 +599,9 @@ namespace picgb::diff
         T gq0[3],
         T gq1[3])
     {
-        using SH = DShape<SHAPE, T>;
-        constexpr int B0 = SH::caBegin, E0 = SH::caEnd;
-        constexpr int N = E0 - B0 + 1; // nodes per axis with the leave node
-        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+#pragma unroll 1
         for(int C = 0; C < 3; ++C)
-        {
-            int const ai = rot(C, 0), aj = rot(C, 1), ak = rot(C, 2);
-            if(tr.q0[ak] == tr.q1[ak])
-                continue;
-            T const csd = qvdt * cellSize(g, ak);
-            int const ei = E0 + tr.leave[ai], ej = E0 + tr.leave[aj], ek = E0 + tr.leave[ak] - 1;
-            T s0k[N], s1k[N], lds[N];
-            for(int k = B0; k < ek; ++k)
-            {
-                s0k[k - B0] = SH::ca(T(k) - tr.q0[ak]);
-                s1k[k - B0] = SH::ca(T(k) - tr.q1[ak]);
-                lds[k - B0] = T(0);
-            }
-            for(int i = B0; i < ei; ++i)
-            {
-                T const s0i = SH::ca(T(i) - tr.q0[ai]), s1i = SH::ca(T(i) - tr.q1[ai]);
-                T ls0i = T(0), ls1i = T(0);
-                for(int j = B0; j < ej; ++j)
-                {
-                    T const s0j = SH::ca(T(j) - tr.q0[aj]), s1j = SH::ca(T(j) - tr.q1[aj]);
-                    T const tmp = -csd
-                        * (s0i * s0j / T(3) + (s1i * s0j + s0i * s1j) / T(6) + s1i * s1j / T(3));
-                    // J(k) = tmp * D_k with D_k = sum_{k' <= k} ds_k'
-                    T ltmp = T(0), D = T(0);
-                    T lamk[N];
-                    for(int k = B0; k < ek; ++k)
-                    {
-                        D += s1k[k - B0] - s0k[k - B0];
-                        int n[3];
-                        n[ai] = tr.origin[ai] + i;
-                        n[aj] = tr.origin[aj] + j;
-                        n[ak] = tr.origin[ak] + k;
-                        T const lam = lamJ[C * nc + cellIndex(g, n[0], n[1], n[2])];
-                        ltmp += lam * D;
-                        lamk[k - B0] = lam * tmp;
-                    }
-                    // dL/d(ds_k') = sum_{k >= k'} lam_k tmp
-                    T acc = T(0);
-                    for(int k = ek - 1; k >= B0; --k)
-                    {
-                        acc += lamk[k - B0];
-                        lds[k - B0] += acc;
-                    }
-                    T const lt = -csd * ltmp;
-                    ls0i += lt * (s0j / T(3) + s1j / T(6));
-                    ls1i += lt * (s0j / T(6) + s1j / T(3));
-                    T const ls0j = lt * (s0i / T(3) + s1i / T(6));
-                    T const ls1j = lt * (s0i / T(6) + s1i / T(3));
-                    // S(j - q): d/dq = -ca'(j - q)
-                    gq0[aj] -= ls0j * SH::dca(T(j) - tr.q0[aj]);
-                    gq1[aj] -= ls1j * SH::dca(T(j) - tr.q1[aj]);
-                }
-                gq0[ai] -= ls0i * SH::dca(T(i) - tr.q0[ai]);
-                gq1[ai] -= ls1i * SH::dca(T(i) - tr.q1[ai]);
-            }
-            for(int k = B0; k < ek; ++k)
-            {
-                // ds_k = S1_k - S0_k
-                gq1[ak] -= lds[k - B0] * SH::dca(T(k) - tr.q1[ak]);
-                gq0[ak] += lds[k - B0] * SH::dca(T(k) - tr.q0[ak]);
-            }
-        }
+            esirkepovComponentAdjoint(C, tr, qvdt, g, lamJ, gq0, gq1);
     }
+
 } // namespace picgb::diff
