@@ -225,13 +225,35 @@ extern "C"
     /* fieldSolver.update_afterCurrent (FDTD.hpp:95; FDTDBase.hpp:151-183): B half step */
     int picgb_stage_field_after(picgb_sim* sim, uint32_t step);
 
+    /* Incident field (fields/incidentField/Solver.hpp:500-533 with profiles/GaussianPulse.hpp):
+     * a Gaussian pulse enters through the total-field/scattered-field surface between the E
+     * plane y = surface (total side) and the B plane below it; the field solver stages add the
+     * incident E (B half steps, at times step*dt and (step+1)*dt) and the incident B (E step,
+     * at (step+1/2)*dt) on that surface.  The pulse travels along +y (axis 1, the only axis
+     * supported), polarised along x (0) or z (1):
+     *   E = E0 exp(-r^2/waist^2) exp(-(tau - t_center)^2 / (2 sigma^2)) sin(omega (tau - t_center) + phase),
+     *   tau = t - (y - surface*dy)/c, r the distance from (center_x, center_z) in cells,
+     *   omega = 2 pi c / wavelength, E0 = a0 omega c / e_over_m, sigma = duration_fwhm / (2 sqrt(ln 2))
+     * (duration_fwhm of the intensity).  There is no focusing: the waist is the same at every y.
+     * enabled = 0 switches it off. */
+    typedef struct picgb_incident_field
+    {
+        int32_t enabled;
+        int32_t axis;
+        int32_t surface;
+        int32_t polarisation;
+        float a0, e_over_m, wavelength, waist, duration_fwhm, t_center, center_x, center_z, phase;
+    } picgb_incident_field;
+    int picgb_set_incident_field(picgb_sim* sim, const picgb_incident_field* field);
+
     /* ------------------------------------------------------------ diagnostics */
     /* out[0] = field energy of E, out[1] = of B, out[2 + s] = kinetic energy of species s;
      * FP64 sums (EnergyFields.x.cpp:211-225, EnergyParticles.x.cpp:58-160, KinEnergy.hpp:43-66).
      * Synchronises the stream.  len = entries available in out. */
     int picgb_energies(picgb_sim* sim, double* out, size_t len);
-    /* Charge conservation (ChargeConservation.tpp:181-260): deposits rho of all species with a
-     * current into "FieldTmp0", returns max|eps0 div E - rho| and max|rho|.  Synchronises. */
+    /* Charge conservation (ChargeConservation.tpp:181-260): deposits rho of all charged species
+     * (immobile ones included) into "FieldTmp0", returns max|eps0 div E - rho| and max|rho|.
+     * Synchronises. */
     int picgb_charge_residual(picgb_sim* sim, double* max_residual, double* max_rho);
 
     /* Charge-conservation residual without any device allocation.  No counterpart in the

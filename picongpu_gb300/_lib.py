@@ -57,6 +57,12 @@ class PlasmaInit(ctypes.Structure):
                 ("position_seed", c_uint64)]
 
 
+class IncidentField(ctypes.Structure):
+    _fields_ = [("enabled", c_int), ("axis", c_int), ("surface", c_int), ("polarisation", c_int), ("a0", c_float),
+                ("e_over_m", c_float), ("wavelength", c_float), ("waist", c_float), ("duration_fwhm", c_float),
+                ("t_center", c_float), ("center_x", c_float), ("center_z", c_float), ("phase", c_float)]
+
+
 class EnsembleConfig(ctypes.Structure):
     _fields_ = [("grid", GridConfig), ("nbox", c_int), ("dims", P(c_int)), ("threads", c_int)]
 
@@ -106,6 +112,7 @@ SIGNATURES = [
     ("picgb_stage_deposit", c_int, [c_void_p, c_uint32]),
     ("picgb_stage_add_current", c_int, [c_void_p]),
     ("picgb_stage_field_after", c_int, [c_void_p, c_uint32]),
+    ("picgb_set_incident_field", c_int, [c_void_p, P(IncidentField)]),
     ("picgb_energies", c_int, [c_void_p, P(c_double), ctypes.c_size_t]),
     ("picgb_charge_residual", c_int, [c_void_p, P(c_double), P(c_double)]),
     ("picgb_set_stream", c_int, [c_void_p, c_void_p]),

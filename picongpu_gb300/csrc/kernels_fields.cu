@@ -100,6 +100,66 @@ namespace picgb
             yeeEAt(B, E, J, coeff, g, x, blockIdx.y, blockIdx.z);
     }
 
+    // ------------------------------------------------------------ incident field (TF/SF)
+    // Incident pulse value at (x, y, z) in cell units and time t (see IncidentParams).
+    __device__ __forceinline__ float incidentValue(IncidentParams const& p, GridParams const& g, float x, float y, float z, float t)
+    {
+        float const rx = (x - p.cx) * g.dx, rz = (z - p.cz) * g.dz;
+        float const tau = t - (y - float(p.j0)) * g.dy / g.c - p.tc;
+        float const env = expf(-(rx * rx + rz * rz) / (p.w0 * p.w0)) * expf(-(tau * tau) / (2.0f * p.sigma * p.sigma));
+        return p.E0 * env * sinf(p.omega * tau + p.phase);
+    }
+
+    // After B -= dt/2 curl E: the B plane j0 - 1 (scattered side) used the total E of plane j0;
+    // removing the incident part gives B_x += dt/2 E_z,inc / dy and B_z -= dt/2 E_x,inc / dy.
+    __global__ void kIncidentB(float* __restrict__ B, GridParams g, IncidentParams p, float t)
+    {
+        int const i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+        if(i >= g.nx)
+            return;
+        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+        size_t const idx = size_t(i) + size_t(g.nx) * (size_t(p.j0 - 1) + size_t(g.ny) * k);
+        float const h = 0.5f * g.dt / g.dy;
+        if(p.pol == 0) // E_x at (i + 1/2, j0, k)
+            B[2 * nc + idx] -= h * incidentValue(p, g, i + 0.5f, float(p.j0), float(k), t);
+        else // E_z at (i, j0, k + 1/2)
+            B[idx] += h * incidentValue(p, g, float(i), float(p.j0), k + 0.5f, t);
+    }
+
+    // After E += c^2 dt curl B: the E plane j0 (total side) used the scattered B of plane j0 - 1;
+    // adding the incident part gives E_x -= c^2 dt B_z,inc / dy and E_z += c^2 dt B_x,inc / dy,
+    // with B_z,inc = -E_x,inc / c (pol 0) and B_x,inc = E_z,inc / c (pol 1) for a wave along +y.
+    __global__ void kIncidentE(float* __restrict__ E, GridParams g, IncidentParams p, float t)
+    {
+        int const i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+        if(i >= g.nx)
+            return;
+        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+        size_t const idx = size_t(i) + size_t(g.nx) * (size_t(p.j0) + size_t(g.ny) * k);
+        float const h = g.c * g.c * g.dt / g.dy;
+        float const yb = float(p.j0) - 0.5f;
+        if(p.pol == 0) // B_z at (i + 1/2, j0 - 1/2, k)
+            E[idx] -= h * (-incidentValue(p, g, i + 0.5f, yb, float(k), t) / g.c);
+        else // B_x at (i, j0 - 1/2, k + 1/2)
+            E[2 * nc + idx] += h * (incidentValue(p, g, float(i), yb, k + 0.5f, t) / g.c);
+    }
+
+    cudaError_t launchIncidentB(float* B, GridParams const& g, IncidentParams const& inc, float t, cudaStream_t stream)
+    {
+        if(!inc.enabled)
+            return cudaSuccess;
+        kIncidentB<<<dim3((g.nx + 127) / 128, g.nz), 128, 0, stream>>>(B, g, inc, t);
+        return cudaGetLastError();
+    }
+
+    cudaError_t launchIncidentE(float* E, GridParams const& g, IncidentParams const& inc, float t, cudaStream_t stream)
+    {
+        if(!inc.enabled)
+            return cudaSuccess;
+        kIncidentE<<<dim3((g.nx + 127) / 128, g.nz), 128, 0, stream>>>(E, g, inc, t);
+        return cudaGetLastError();
+    }
+
     // ------------------------------------------------------------ ensemble of boxes
     // Block b of a batched field launch covers kBatchFieldThreads consecutive
     // cells of box blockBox[b]; returns false for threads past the box's end.

@@ -873,17 +873,20 @@ extern "C"
         return PICGB_OK;
     }
 
-    int picgb_stage_field_before(picgb_sim* s, uint32_t)
+    int picgb_stage_field_before(picgb_sim* s, uint32_t step)
     {
         if(int r = checkSim(s))
             return r;
+        float const t = float(double(step) * s->cfg.dt);
         CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_B, [&] { return launchYeeBHalf(s->E, s->B, s->g, s->stream); }));
+        CUDA_TRY(launchIncidentB(s->B, s->g, s->inc, t, s->stream)); // incident E at t (Solver.hpp:500-533)
         // with the fused deposit J is complete here: E += curl B c^2 dt and E += coeff J in one pass
         float const* J = s->cfg.fuse_deposit ? s->J : nullptr;
         CUDA_TRY(timedLaunch(
             s,
             PICGB_KERNEL_YEE_E,
             [&] { return launchYeeE(s->B, s->E, J, s->coeffJ(), s->g, s->stream); }));
+        CUDA_TRY(launchIncidentE(s->E, s->g, s->inc, t + 0.5f * s->cfg.dt, s->stream)); // incident B at t + dt/2
         return PICGB_OK;
     }
 
@@ -919,11 +922,45 @@ extern "C"
         return PICGB_OK;
     }
 
-    int picgb_stage_field_after(picgb_sim* s, uint32_t)
+    int picgb_stage_field_after(picgb_sim* s, uint32_t step)
     {
         if(int r = checkSim(s))
             return r;
         CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_B, [&] { return launchYeeBHalf(s->E, s->B, s->g, s->stream); }));
+        CUDA_TRY(launchIncidentB(s->B, s->g, s->inc, float(double(step + 1) * s->cfg.dt), s->stream)); // E at t + dt
+        return PICGB_OK;
+    }
+
+    int picgb_set_incident_field(picgb_sim* s, const picgb_incident_field* f)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(!f || !f->enabled)
+        {
+            s->inc = IncidentParams{};
+            return PICGB_OK;
+        }
+        if(f->axis != 1)
+            return fail(PICGB_ERR_UNSUPPORTED, "the incident field enters along +y (axis 1) only");
+        if(f->surface < 1 || f->surface >= s->cfg.ny)
+            return fail(PICGB_ERR_INVALID, "incident-field surface %d outside 1..%d", int(f->surface), int(s->cfg.ny) - 1);
+        if(!(f->wavelength > 0.0f && f->waist > 0.0f && f->duration_fwhm > 0.0f) || (f->polarisation != 0 && f->polarisation != 1))
+            return fail(PICGB_ERR_INVALID, "incident field needs positive wavelength, waist, duration and polarisation 0 or 1");
+        IncidentParams p{};
+        p.enabled = 1;
+        p.j0 = f->surface;
+        p.pol = f->polarisation;
+        double const omega = 2.0 * 3.14159265358979323846 * s->cfg.c / f->wavelength;
+        // a0 = q E0 / (m c omega) with the species' units given by the caller through e_over_m = q / m
+        p.E0 = float(f->a0 * omega * s->cfg.c / f->e_over_m);
+        p.omega = float(omega);
+        p.w0 = f->waist;
+        p.sigma = float(f->duration_fwhm / (2.0 * std::sqrt(std::log(2.0)))); // intensity FWHM -> field sigma
+        p.tc = f->t_center;
+        p.cx = f->center_x;
+        p.cz = f->center_z;
+        p.phase = f->phase;
+        s->inc = p;
         return PICGB_OK;
     }
 
@@ -1001,7 +1038,8 @@ extern "C"
         float const V = s->cellVolume();
         for(auto& sp : s->species)
         {
-            if(!sp->allocated || !hasCurrent(*sp))
+            // every charged species, immobile ones included (their density is part of rho)
+            if(!sp->allocated || sp->cfg.charge == 0.0f)
                 continue;
             CUDA_TRY(launchChargeDensity(sp->cfg.shape, s->cfg.supercell, sp->dev, s->rho, s->g, sp->cfg.charge, V, s->stream));
             ++s->launches;

@@ -75,6 +75,19 @@ namespace picgb
         JFixed jf; // fixed-point format of the J tile (used when built with PICGB_J_FIXED)
     };
 
+    // Incident Gaussian pulse entering through the total-field/scattered-field surface
+    // y = j0 (fields/incidentField/Solver.hpp:500-533, profiles/GaussianPulse.hpp): the
+    // field at (x, y, z, t) is E0 exp(-r^2 / w0^2) exp(-(tau - tc)^2 / (2 sigma^2))
+    // sin(omega (tau - tc) + phase), tau = t - (y - j0 dy) / c, r the distance from the
+    // axis (cx, cz), polarised along x (pol 0) or z (pol 1), travelling along +y.
+    struct IncidentParams
+    {
+        int enabled;
+        int j0; // first E plane of the total-field region
+        int pol;
+        float E0, omega, w0, sigma, tc, cx, cz, phase;
+    };
+
     // ---- launchers (kernels_*.cu); all asynchronous on `stream`
     // shape: 1 CIC, 2 TSC, 3 PQS; scId: 0 -> 8x8x4, 1 -> 4x4x4, 2 -> 8x8x8
     cudaError_t launchPush(
@@ -147,6 +160,10 @@ namespace picgb
     cudaError_t launchYeeBHalf(float const* E, float* B, GridParams const& g, cudaStream_t stream);
     cudaError_t launchYeeE(float const* B, float* E, float const* J, float coeff, GridParams const& g, cudaStream_t stream);
     cudaError_t launchAddCurrent(float* E, float const* J, float coeff, size_t ncell, cudaStream_t stream);
+    // TF/SF corrections after a B half step (incident E at time t, coefficient dt/2) and
+    // after the E step (incident B at time t, coefficient c^2 dt)
+    cudaError_t launchIncidentB(float* B, GridParams const& g, IncidentParams const& inc, float t, cudaStream_t stream);
+    cudaError_t launchIncidentE(float* E, GridParams const& g, IncidentParams const& inc, float t, cudaStream_t stream);
     cudaError_t launchFieldEnergy(float const* F, size_t ncell, double* out3, cudaStream_t stream);
     cudaError_t launchChargeResidual(
         float const* E,

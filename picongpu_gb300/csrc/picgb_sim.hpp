@@ -133,6 +133,7 @@ struct picgb_sim
     cudaStream_t stream = nullptr;
     bool ownStream = false;
     bool inEnsemble = false; // owned by a picgb_ensemble: not destroyed through picgb_destroy
+    picgb::IncidentParams inc{}; // incident pulse (TF/SF surface), disabled by default
     uint64_t launches = 0;
     std::vector<std::unique_ptr<picgb::host::Species>> species;
     std::map<std::string, picgb::host::Entry> registry;

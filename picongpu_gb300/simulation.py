@@ -244,6 +244,20 @@ class Simulation:
         return a
 
     # ------------------------------------------------------------ stepping
+    def set_incident_field(self, a0: float, wavelength: float, waist: float, duration_fwhm: float, t_center: float,
+                           surface: int, polarisation: int = 0, center=None, phase: float = 0.0,
+                           e_over_m: float = 1.0) -> None:
+        """Gaussian pulse entering along +y through the TF/SF surface y = surface
+        (fields/incidentField/Solver.hpp); see picgb_set_incident_field."""
+        cx, cz = center if center is not None else (self.grid.nx / 2.0, self.grid.nz / 2.0)
+        f = L.IncidentField(1, 1, surface, polarisation, a0, e_over_m, wavelength, waist, duration_fwhm, t_center, cx, cz,
+                            phase)
+        L.call("picgb_set_incident_field", self.handle, ctypes.byref(f))
+
+    def clear_incident_field(self) -> None:
+        f = L.IncidentField()
+        L.call("picgb_set_incident_field", self.handle, ctypes.byref(f))
+
     def step(self) -> None:
         L.call("picgb_step", self.handle, self.current_step)
         self.current_step += 1

@@ -54,7 +54,8 @@ def test_struct_sizes_match_header():
 #include "picgb.h"
 int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), sizeof(picgb_species_config),
  sizeof(picgb_particles), sizeof(picgb_buffer_desc), sizeof(picgb_plasma_init), sizeof(picgb_ensemble_config));
- printf("%zu %zu %zu\n", sizeof(picgb_diff_config), sizeof(picgb_diff_species), sizeof(picgb_diff_state));
+ printf("%zu %zu %zu %zu\n", sizeof(picgb_diff_config), sizeof(picgb_diff_species), sizeof(picgb_diff_state),
+ sizeof(picgb_incident_field));
  return 0;}
 """
     with tempfile.TemporaryDirectory() as d:
@@ -65,7 +66,7 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), si
         sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     mine = [ctypes.sizeof(t) for t in (_lib.GridConfig, _lib.SpeciesConfig, _lib.Particles, _lib.BufferDesc,
                                        _lib.PlasmaInit, _lib.EnsembleConfig, _lib.DiffConfig, _lib.DiffSpecies,
-                                       _lib.DiffState)]
+                                       _lib.DiffState, _lib.IncidentField)]
     assert mine == sizes
 
 
