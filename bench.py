@@ -374,6 +374,50 @@ def run_ensemble(args, local_rank):
     return out
 
 
+# ---------------------------------------------------------------------- laser-driven wake
+def run_laser_wake(args, local_rank):
+    """128 x 1024 x 128 cells, a Gaussian pulse (a0 = 2, waist 8, 10 dt FWHM, wavelength 16)
+    entering through the TF/SF surface y = 8 into an electron gas at n/n_c = 0.01 (8 ppc) over
+    immobile ions; PQS, Boris, Esirkepov, Yee.  A bounded number of steps is timed."""
+    import torch
+
+    import picongpu_gb300 as pg
+
+    n = (128, 1024, 128)
+    lam = 16.0
+    omega = 2 * np.pi / lam
+    dens = 0.01 * omega * omega  # n_c = omega^2 eps0 m / q^2 with eps0 = m = q = 1
+    g = pg.Grid(*n, dt=DT, supercell=(8, 8, 4), device=local_rank)
+    with pg.Simulation(g) as sim:
+        sim.add_species(pg.Species("e", -1.0, 1.0, shape="PQS"))
+        sim.add_species(pg.Species("i", 1.0, MASS_P, pusher=None, shape="PQS", current=None))
+        sim.init_plasma("e", 8, dens, 0.0, seed=21, position_seed=22)
+        sim.init_plasma("i", 8, dens, 0.0, seed=23, position_seed=22)
+        fwhm = 10 * DT
+        sigma = fwhm / (2 * np.sqrt(np.log(2)))
+        sim.set_incident_field(a0=2.0, wavelength=lam, waist=8.0, duration_fwhm=fwhm, t_center=4 * sigma, surface=8)
+        npart = sim.particle_count("e")
+        for _ in range(args.warmup):
+            sim.step()
+        sim.synchronize()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.laser_steps):
+            sim.step()
+        sim.synchronize()
+        dt_wall = time.perf_counter() - t0
+        en = sim.energies()
+        res, rho = sim.charge_residual()
+    return {"workload": "laser-driven wake: 128x1024x128 cells, e 8 ppc at n/n_c = 0.01 over immobile ions, "
+                        "Gaussian pulse a0 = 2, waist 8, 10 dt FWHM, wavelength 16, TF/SF surface y = 8, PQS, "
+                        "Boris, Esirkepov, Yee, fp32",
+            "steps": args.laser_steps, "after_steps": args.warmup + args.laser_steps, "particles_pushed": npart,
+            "value": npart * args.laser_steps / dt_wall, "unit": "particle-steps/s",
+            "ms_per_step": 1e3 * dt_wall / args.laser_steps, "field_energy": en["E"] + en["B"],
+            "electron_energy": en["e"], "charge_residual_over_electron_density": res / dens,
+            "timing": "host clock around the steps, stream synchronised on both sides"}
+
+
 # ---------------------------------------------------------------------- differentiable run
 def adjoint_case(A, n, ppc, precision, checkpoint_every):
     dens = (0.1 / DT) ** 2
@@ -476,6 +520,8 @@ def main():
     ap.add_argument("--ensemble-boxes", type=int, default=512)
     ap.add_argument("--ensemble-steps", type=int, default=10)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-laser", action="store_true")
+    ap.add_argument("--laser-steps", type=int, default=40)
     ap.add_argument("--adjoint-steps", type=int, default=300)
     ap.add_argument("--adjoint-fd-steps", type=int, default=20)
     args = ap.parse_args()
@@ -523,6 +569,9 @@ def main():
     adjoint = None
     if not args.no_adjoint:
         adjoint = run_adjoint(args)
+    laser = None
+    if not args.no_laser:
+        laser = run_laser_wake(args, local_rank)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         val, cores, sample = cpu_sample_rate(wl, 10, 1, budget_s=20.0)
@@ -531,7 +580,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded device init)", "config": config,
             "particles": r["npart"], "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"],
-            "clocks": r["clocks"], "gpu_launches": r["launches"], "batched": batched, "adjoint": adjoint}
+            "clocks": r["clocks"], "gpu_launches": r["launches"], "batched": batched, "adjoint": adjoint,
+            "laser_wake": laser}
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch
