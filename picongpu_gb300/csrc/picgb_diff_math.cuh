@@ -20,6 +20,18 @@
 
 namespace picgb::diff
 {
+    // constant factors as multiplications (a division by a constant is a full IEEE divide)
+    template<typename T>
+    __host__ __device__ constexpr T third()
+    {
+        return T(1.0 / 3.0);
+    }
+    template<typename T>
+    __host__ __device__ constexpr T sixth()
+    {
+        return T(1.0 / 6.0);
+    }
+
     template<typename T>
     struct DiffGrid
     {
@@ -75,9 +87,9 @@ namespace picgb::diff
             else
             {
                 T const a = T(1) - x, x2 = x * x;
-                s[0] = a * a * a / T(6);
-                s[1] = (T(4) - T(6) * x2 + T(3) * x2 * x) / T(6);
-                s[3] = x2 * x / T(6);
+                s[0] = a * a * a * sixth<T>();
+                s[1] = (T(4) - T(6) * x2 + T(3) * x2 * x) * sixth<T>();
+                s[3] = x2 * x * sixth<T>();
                 s[2] = T(1) - s[0] - s[1] - s[3];
                 ds[0] = T(-0.5) * a * a;
                 ds[1] = T(-2) * x + T(1.5) * x2;
@@ -102,7 +114,7 @@ namespace picgb::diff
             else
             {
                 T const b = T(2) - a;
-                T const inner = (T(4) - T(6) * t * t + T(3) * a * a * a) / T(6), outer = b * b * b / T(6);
+                T const inner = (T(4) - T(6) * t * t + T(3) * a * a * a) * sixth<T>(), outer = b * b * b * sixth<T>();
                 return a < T(1) ? inner : (a < T(2) ? outer : T(0));
             }
         }
@@ -223,20 +235,38 @@ namespace picgb::diff
             axis(0, stagger(comp, 0), wx, dx, ox);
             axis(1, stagger(comp, 1), wy, dy, oy);
             axis(2, stagger(comp, 2), wz, dz, oz);
+            // nested sums as in the gather: per row the value and its x-derivative, per plane
+            // the y-derivative, then z; the scattered value per node is (lam wy wz) wx
+            T gx = T(0), gy = T(0), gz = T(0);
 #pragma unroll
             for(int z = 0; z < S; ++z)
+            {
+                T pz = T(0), pdx = T(0), pdy = T(0);
 #pragma unroll
                 for(int y = 0; y < S; ++y)
+                {
+                    T const lyz = lam * wy[y] * wz[z];
+                    T sx = T(0), sdx = T(0);
 #pragma unroll
                     for(int x = 0; x < S; ++x)
                     {
                         uint32_t const i = oz[z] + oy[y] + ox[x];
-                        atomicAdd(lamF + i, lam * wx[x] * wy[y] * wz[z]);
-                        T const f = F[i] * lam;
-                        gpos[0] += f * dx[x] * wy[y] * wz[z];
-                        gpos[1] += f * wx[x] * dy[y] * wz[z];
-                        gpos[2] += f * wx[x] * wy[y] * dz[z];
+                        atomicAdd(lamF + i, lyz * wx[x]);
+                        T const f = F[i];
+                        sx += f * wx[x];
+                        sdx += f * dx[x];
                     }
+                    pz += wy[y] * sx;
+                    pdx += wy[y] * sdx;
+                    pdy += dy[y] * sx;
+                }
+                gx += wz[z] * pdx;
+                gy += wz[z] * pdy;
+                gz += dz[z] * pz;
+            }
+            gpos[0] += lam * gx;
+            gpos[1] += lam * gy;
+            gpos[2] += lam * gz;
         }
     };
 
@@ -468,7 +498,7 @@ namespace picgb::diff
                     continue;
                 // -csd (S0i S0j / 3 + S1i S0j / 6 + S0i S1j / 6 + S1i S1j / 3) (Esirkepov.hpp:214-215)
                 T const tmp = -csd
-                    * (s0i[i] * s0j[j] / T(3) + (s1i[i] * s0j[j] + s0i[i] * s1j[j]) / T(6) + s1i[i] * s1j[j] / T(3));
+                    * (s0i[i] * s0j[j] * third<T>() + (s1i[i] * s0j[j] + s0i[i] * s1j[j]) * sixth<T>() + s1i[i] * s1j[j] * third<T>());
                 T run = T(0);
                 uint32_t const base = ndi[i] + ndj[j];
 #pragma unroll
@@ -529,7 +559,7 @@ namespace picgb::diff
                 if(i >= ni || j >= nj)
                     continue;
                 T const tmp = -csd
-                    * (s0i[i] * s0j[j] / T(3) + (s1i[i] * s0j[j] + s0i[i] * s1j[j]) / T(6) + s1i[i] * s1j[j] / T(3));
+                    * (s0i[i] * s0j[j] * third<T>() + (s1i[i] * s0j[j] + s0i[i] * s1j[j]) * sixth<T>() + s1i[i] * s1j[j] * third<T>());
                 uint32_t const base = ndi[i] + ndj[j];
                 // ltmp = sum_k lam_k D_k; dL/d(dS_k') = sum_{k >= k'} lam_k tmp
                 T ltmp = T(0), D = T(0), lamk[N];
@@ -553,10 +583,10 @@ namespace picgb::diff
                     lds[k] += acc;
                 }
                 T const lt = -csd * ltmp;
-                ls0i[i] += lt * (s0j[j] / T(3) + s1j[j] / T(6));
-                ls1i[i] += lt * (s0j[j] / T(6) + s1j[j] / T(3));
-                ls0j[j] += lt * (s0i[i] / T(3) + s1i[i] / T(6));
-                ls1j[j] += lt * (s0i[i] / T(6) + s1i[i] / T(3));
+                ls0i[i] += lt * (s0j[j] * third<T>() + s1j[j] * sixth<T>());
+                ls1i[i] += lt * (s0j[j] * sixth<T>() + s1j[j] * third<T>());
+                ls0j[j] += lt * (s0i[i] * third<T>() + s1i[i] * sixth<T>());
+                ls1j[j] += lt * (s0i[i] * sixth<T>() + s1i[i] * third<T>());
             }
         T g0i = T(0), g1i = T(0), g0j = T(0), g1j = T(0), g0k = T(0), g1k = T(0);
         T d0[N], d1[N];
