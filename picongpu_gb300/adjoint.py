@@ -223,7 +223,8 @@ def gaussian_pulse(pic: DiffPIC, a0, waist, wavelength: float, length: float, ce
 
 
 def thermal_species(pic: DiffPIC, k: int, ppc: int, density: float, u_th: float, seed: int, position_seed=None):
-    """Seeded uniform plasma of species k: ppc particles per cell at uniform in-cell positions,
+    """Seeded uniform plasma of species k: ppc particles per cell (particle i in cell i mod ncell)
+    at uniform in-cell positions,
     momenta u_th * N(0,1) * m w c per component, weighting density * V / ppc."""
     import torch
 
@@ -233,7 +234,9 @@ def thermal_species(pic: DiffPIC, k: int, ppc: int, density: float, u_th: float,
         raise ValueError(f"species {k} was declared with {pic.species[k].n} particles, {n} needed")
     gpos = torch.Generator(device="cuda").manual_seed(seed if position_seed is None else position_seed)
     gmom = torch.Generator(device="cuda").manual_seed(seed + 7919)
-    cells = torch.arange(nx * ny * nz, device="cuda", dtype=torch.int64).repeat_interleave(ppc)
+    # cell of particle k = k mod ncell: the 32 particles of a warp sit in 32 different cells, so
+    # the atomics of one instruction (deposit, gather transpose) never hit the same address
+    cells = torch.arange(nx * ny * nz, device="cuda", dtype=torch.int64).repeat(ppc)
     cell = torch.stack([cells % nx, (cells // nx) % ny, cells // (nx * ny)]).to(torch.int32).contiguous()
     pos = torch.rand((3, n), generator=gpos, device="cuda", dtype=torch.float64).to(pic.dtype).contiguous()
     dx, dy, dz = pic.cell
