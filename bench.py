@@ -162,6 +162,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+# ---------------------------------------------------------------------- replicas
+def max_over_ranks(x: float, device: str) -> float:
+    """Largest value over the ranks of the default process group (the slowest replica's time)."""
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(npart_per_rank: int, steps: int, ms: float, world: int) -> float:
+    """Whole-job particle-steps/s of `world` independent replicas that each advanced npart_per_rank
+    particles by `steps` steps, timed by the slowest replica (ms)."""
+    return world * npart_per_rank * steps / (ms / 1e3)
+
+
 # ---------------------------------------------------------------------- GPU arm
 def build_sim(pg, wl, device):
     g = pg.Grid(*wl["n"], dt=DT, supercell=(8, 8, 4), device=device)
@@ -231,11 +247,9 @@ def run_gpu(args, wl, rank, world, local_rank):
     kinds = sim.deposit_kinds()
     sim.profile(False)
     if dist:
-        t = torch.tensor([ms], device=f"cuda:{local_rank}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, f"cuda:{local_rank}")
         torch.distributed.barrier()
-    value = world * npart * args.steps / (ms / 1e3)
+    value = replica_rate(npart, args.steps, ms, world)
 
     # roofline of the fused push kernel (dominant kernel)
     push_ms, push_n = kt["push"]
@@ -299,9 +313,7 @@ def run_e2e(args, wl, sim, pg, torch, local_rank, world):
     t1 = time.perf_counter()
     dt = t1 - t0
     if world > 1:
-        t = torch.tensor([dt], device=f"cuda:{local_rank}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dt = float(t.item())
+        dt = max_over_ranks(dt, f"cuda:{local_rank}")
     d2h += args.steps * 8 * (2 + 2)
     sim2.close()
     del keep
