@@ -354,8 +354,12 @@ def run_ensemble(args, local_rank):
     dims, ppc, u_th, dens = ensemble_boxes(args.ensemble_boxes)
     ntune = min(64, len(dims))
     g = pg.Grid(8, 8, 4, dt=DT, device=local_rank)
-    sc, th, rates = pg.autotune(dims[:ntune], species, ensemble_inits(pg, ppc[:ntune], u_th[:ntune], dens[:ntune]),
-                                grid=g, warmup=2, steps=3)
+    if args.no_ensemble_tune:
+        sc, th, rates = (8, 8, 4), 256, {}
+    else:
+        sc, th, rates = pg.autotune(dims[:ntune], species,
+                                    ensemble_inits(pg, ppc[:ntune], u_th[:ntune], dens[:ntune]), grid=g, warmup=2,
+                                    steps=3)
     g = pg.Grid(8, 8, 4, dt=DT, supercell=sc, device=local_rank)
     out = {"workload": f"{len(dims)} periodic boxes, edges from {list(EDGES)} per axis, 4-16 ppc per species, "
                        f"u_th in [0.005, 0.05], omega_p dt in [0.05, 0.2], {shape}, Boris, Esirkepov, Yee, fp32",
@@ -531,6 +535,7 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-boxes", type=int, default=512)
     ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--no-ensemble-tune", action="store_true", help="8x8x4 supercells, 256 threads, no autotuning")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-laser", action="store_true")
     ap.add_argument("--laser-steps", type=int, default=40)
