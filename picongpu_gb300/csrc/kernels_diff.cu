@@ -31,7 +31,14 @@ namespace picgb::diff
         DBoris<T> boris;
         DTrajectory<SHAPE, T> traj;
 
-        __device__ void run(DiffParticles<T> const& sp, uint64_t p, T const* E, T const* B, DiffGrid<T> const& g)
+        // gathered: the six field values of this particle from an earlier pass ([6][n]), or null
+        __device__ void run(
+            DiffParticles<T> const& sp,
+            uint64_t p,
+            T const* E,
+            T const* B,
+            DiffGrid<T> const& g,
+            T const* gathered = nullptr)
         {
             size_t const nc = size_t(g.nx) * g.ny * g.nz;
             for(int d = 0; d < 3; ++d)
@@ -45,12 +52,20 @@ namespace picgb::diff
             mw = sp.mass * w;
             // the gather weights are not kept: the adjoint recomputes them at its end, which keeps
             // them out of the registers during the deposit adjoint
-            DGather<SHAPE, T> gw;
-            gw.compute(cell, pos, g);
             T f6[6];
+            if(gathered)
+            {
+                for(int comp = 0; comp < 6; ++comp)
+                    f6[comp] = gathered[comp * sp.n + p];
+            }
+            else
+            {
+                DGather<SHAPE, T> gw;
+                gw.compute(cell, pos, g);
 #pragma unroll 1
-            for(int comp = 0; comp < 6; ++comp)
-                f6[comp] = gw.valueAt(comp < 3 ? E + comp * nc : B + (comp - 3) * nc, comp);
+                for(int comp = 0; comp < 6; ++comp)
+                    f6[comp] = gw.valueAt(comp < 3 ? E + comp * nc : B + (comp - 3) * nc, comp);
+            }
             for(int d = 0; d < 3; ++d)
             {
                 Ef[d] = f6[d];
@@ -80,13 +95,25 @@ namespace picgb::diff
 
     template<int SHAPE, typename T>
     __global__ void __launch_bounds__(kDiffThreads)
-        kDiffPush(DiffParticles<T> sp, T const* __restrict__ E, T const* __restrict__ B, T* __restrict__ J, DiffGrid<T> g)
+        kDiffPush(
+            DiffParticles<T> sp,
+            T const* __restrict__ E,
+            T const* __restrict__ B,
+            T* __restrict__ J,
+            DiffGrid<T> g,
+            T* __restrict__ gathered)
     {
         uint64_t const p = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
         if(p >= sp.n)
             return;
         ParticleStep<SHAPE, T> st;
         st.run(sp, p, E, B, g);
+        if(gathered) // kept for the adjoint of this step
+            for(int d = 0; d < 3; ++d)
+            {
+                gathered[d * sp.n + p] = st.Ef[d];
+                gathered[(3 + d) * sp.n + p] = st.Bf[d];
+            }
         esirkepovDeposit(st.traj, st.qvdt(g), g, J);
         for(int d = 0; d < 3; ++d)
         {
@@ -109,14 +136,15 @@ namespace picgb::diff
         T* __restrict__ lamB,
         T* __restrict__ lamPos,
         T* __restrict__ lamMom,
-        DiffGrid<T> g)
+        DiffGrid<T> g,
+        T const* __restrict__ gathered)
     {
         uint64_t const p = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
         if(p >= sp.n)
             return;
         size_t const nc = size_t(g.nx) * g.ny * g.nz;
         ParticleStep<SHAPE, T> st;
-        st.run(sp, p, E, B, g);
+        st.run(sp, p, E, B, g, gathered);
         T lpos[3], lmom[3];
         for(int d = 0; d < 3; ++d)
         {
@@ -229,7 +257,14 @@ namespace picgb::diff
     inline unsigned blocksFor(uint64_t n, int threads) { return unsigned((n + threads - 1) / threads); }
 
     template<typename T, int SHAPE>
-    cudaError_t pushT(DiffSpeciesPtr const& s, void const* E, void const* B, void* J, DiffGridDesc const& g, cudaStream_t st)
+    cudaError_t pushT(
+        DiffSpeciesPtr const& s,
+        void const* E,
+        void const* B,
+        void* J,
+        void* gathered,
+        DiffGridDesc const& g,
+        cudaStream_t st)
     {
         if(s.n == 0)
             return cudaSuccess;
@@ -238,7 +273,8 @@ namespace picgb::diff
             static_cast<T const*>(E),
             static_cast<T const*>(B),
             static_cast<T*>(J),
-            grid<T>(g));
+            grid<T>(g),
+            static_cast<T*>(gathered));
         return cudaGetLastError();
     }
 
@@ -252,6 +288,7 @@ namespace picgb::diff
         void* lamB,
         void* lamPos,
         void* lamMom,
+        void const* gathered,
         DiffGridDesc const& g,
         cudaStream_t st)
     {
@@ -266,21 +303,30 @@ namespace picgb::diff
             static_cast<T*>(lamB),
             static_cast<T*>(lamPos),
             static_cast<T*>(lamMom),
-            grid<T>(g));
+            grid<T>(g),
+            static_cast<T const*>(gathered));
         return cudaGetLastError();
     }
 
     template<typename T>
-    cudaError_t dispatchPush(int shape, DiffSpeciesPtr const& s, void const* E, void const* B, void* J, DiffGridDesc const& g, cudaStream_t st)
+    cudaError_t dispatchPush(
+        int shape,
+        DiffSpeciesPtr const& s,
+        void const* E,
+        void const* B,
+        void* J,
+        void* gathered,
+        DiffGridDesc const& g,
+        cudaStream_t st)
     {
         switch(shape)
         {
         case 1:
-            return pushT<T, 1>(s, E, B, J, g, st);
+            return pushT<T, 1>(s, E, B, J, gathered, g, st);
         case 2:
-            return pushT<T, 2>(s, E, B, J, g, st);
+            return pushT<T, 2>(s, E, B, J, gathered, g, st);
         case 3:
-            return pushT<T, 3>(s, E, B, J, g, st);
+            return pushT<T, 3>(s, E, B, J, gathered, g, st);
         }
         return cudaErrorInvalidValue;
     }
@@ -296,17 +342,18 @@ namespace picgb::diff
         void* lamB,
         void* lamPos,
         void* lamMom,
+        void const* gathered,
         DiffGridDesc const& g,
         cudaStream_t st)
     {
         switch(shape)
         {
         case 1:
-            return adjointT<T, 1>(s, E, B, lamJ, lamE, lamB, lamPos, lamMom, g, st);
+            return adjointT<T, 1>(s, E, B, lamJ, lamE, lamB, lamPos, lamMom, gathered, g, st);
         case 2:
-            return adjointT<T, 2>(s, E, B, lamJ, lamE, lamB, lamPos, lamMom, g, st);
+            return adjointT<T, 2>(s, E, B, lamJ, lamE, lamB, lamPos, lamMom, gathered, g, st);
         case 3:
-            return adjointT<T, 3>(s, E, B, lamJ, lamE, lamB, lamPos, lamMom, g, st);
+            return adjointT<T, 3>(s, E, B, lamJ, lamE, lamB, lamPos, lamMom, gathered, g, st);
         }
         return cudaErrorInvalidValue;
     }
@@ -318,11 +365,12 @@ namespace picgb::diff
         void const* E,
         void const* B,
         void* J,
+        void* gathered,
         DiffGridDesc const& g,
         cudaStream_t st)
     {
-        return precision == 8 ? dispatchPush<double>(shape, s, E, B, J, g, st)
-                              : dispatchPush<float>(shape, s, E, B, J, g, st);
+        return precision == 8 ? dispatchPush<double>(shape, s, E, B, J, gathered, g, st)
+                              : dispatchPush<float>(shape, s, E, B, J, gathered, g, st);
     }
 
     cudaError_t launchDiffAdjoint(
@@ -336,11 +384,13 @@ namespace picgb::diff
         void* lamB,
         void* lamPos,
         void* lamMom,
+        void const* gathered,
         DiffGridDesc const& g,
         cudaStream_t st)
     {
-        return precision == 8 ? dispatchAdjoint<double>(shape, s, E, B, lamJ, lamE, lamB, lamPos, lamMom, g, st)
-                              : dispatchAdjoint<float>(shape, s, E, B, lamJ, lamE, lamB, lamPos, lamMom, g, st);
+        return precision == 8
+            ? dispatchAdjoint<double>(shape, s, E, B, lamJ, lamE, lamB, lamPos, lamMom, gathered, g, st)
+            : dispatchAdjoint<float>(shape, s, E, B, lamJ, lamE, lamB, lamPos, lamMom, gathered, g, st);
     }
 
     template<typename T>

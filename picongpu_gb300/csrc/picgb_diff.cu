@@ -46,6 +46,7 @@ struct picgb_diff
     size_t blobBytes = 0;
     std::vector<void*> ckpts; // state at steps 0, K, 2K, ...
     std::vector<void*> seg; // states of one segment during the backward pass
+    std::vector<void*> gathered; // per step of a segment: the particles' gathered E, B ([6][n] per species)
     void* work = nullptr;
     uint32_t nsteps = 0;
     bool haveForward = false;
@@ -86,6 +87,25 @@ struct picgb_diff
         return off;
     }
 
+    size_t gatheredBytes() const
+    {
+        size_t b = 0;
+        for(auto const& sp : species)
+            b += (6 * sp.n * esz + 255) / 256 * 256;
+        return b;
+    }
+
+    // species k's part of a gathered-field buffer, or null
+    void* gatheredPtr(void* buf, size_t k) const
+    {
+        if(!buf)
+            return nullptr;
+        size_t off = 0;
+        for(size_t i = 0; i < k; ++i)
+            off += (6 * species[i].n * esz + 255) / 256 * 256;
+        return static_cast<char*>(buf) + off;
+    }
+
     DiffSpeciesPtr speciesPtr(StatePtrs const& s, size_t k) const
     {
         return DiffSpeciesPtr{s.cell[k], s.pos[k], s.mom[k], weights[k], species[k].n, species[k].charge, species[k].mass};
@@ -122,13 +142,23 @@ namespace
         return PICGB_OK;
     }
 
-    // One forward step in place (Simulation::runOneStep with the fused deposit).
-    int stepForward(picgb_diff* d, StatePtrs const& s, cudaStream_t st)
+    // One forward step in place (Simulation::runOneStep with the fused deposit); the particles'
+    // gathered fields go to `gathered` when it is not null.
+    int stepForward(picgb_diff* d, StatePtrs const& s, cudaStream_t st, void* gathered = nullptr)
     {
         double const dt = d->g.dt, c2 = d->g.c * d->g.c;
         CUDA_TRY(cudaMemsetAsync(d->J, 0, d->fieldBytes(), st));
         for(size_t k = 0; k < d->species.size(); ++k)
-            CUDA_TRY(launchDiffPush(d->prec, d->cfg.shape, d->speciesPtr(s, k), s.E, s.B, d->J, d->g, st));
+            CUDA_TRY(launchDiffPush(
+                d->prec,
+                d->cfg.shape,
+                d->speciesPtr(s, k),
+                s.E,
+                s.B,
+                d->J,
+                d->gatheredPtr(gathered, k),
+                d->g,
+                st));
         CUDA_TRY(launchDiffCurlAdd(d->prec, s.B, s.E, -0.5 * dt, true, d->g, st));
         CUDA_TRY(launchDiffCurlAdd(d->prec, s.E, s.B, c2 * dt, false, d->g, st));
         CUDA_TRY(launchDiffAxpby(d->prec, s.E, -dt / d->g.eps0, d->J, 1.0, 3 * d->nc, st));
@@ -137,7 +167,8 @@ namespace
     }
 
     // Adjoint of the step that started in state s; lam holds dL/d(state after) on entry.
-    int stepAdjoint(picgb_diff* d, StatePtrs const& s, StatePtrs const& lam, cudaStream_t st)
+    // gathered: the particles' fields kept by the replay of this step, or null.
+    int stepAdjoint(picgb_diff* d, StatePtrs const& s, StatePtrs const& lam, cudaStream_t st, void* gathered)
     {
         double const dt = d->g.dt, c2 = d->g.c * d->g.c;
         CUDA_TRY(launchDiffCurlAdd(d->prec, lam.E, lam.B, -0.5 * dt, false, d->g, st));
@@ -157,6 +188,7 @@ namespace
                 lam.B,
                 lam.pos[k],
                 lam.mom[k],
+                d->gatheredPtr(gathered, k),
                 d->g,
                 st));
         return PICGB_OK;
@@ -176,6 +208,12 @@ namespace
             void* p = nullptr;
             CUDA_TRY(cudaMalloc(&p, d->blobBytes));
             d->seg.push_back(p);
+        }
+        while(d->gathered.size() < K)
+        {
+            void* p = nullptr;
+            CUDA_TRY(cudaMalloc(&p, d->gatheredBytes()));
+            d->gathered.push_back(p);
         }
         if(!d->work)
             CUDA_TRY(cudaMalloc(&d->work, d->blobBytes));
@@ -251,6 +289,8 @@ extern "C"
             cudaFree(p);
         for(void* p : d->seg)
             cudaFree(p);
+        for(void* p : d->gathered)
+            cudaFree(p);
         if(d->work)
             cudaFree(d->work);
         if(d->J)
@@ -315,11 +355,12 @@ extern "C"
                 if(int r = copyState(d, d->blobPtrs(d->seg[i - a]), work, st))
                     return r;
                 if(i + 1 < b)
-                    if(int r = stepForward(d, work, st))
+                    if(int r = stepForward(d, work, st, d->gathered[i - a]))
                         return r;
             }
+            // the last step of the segment was not replayed: its adjoint gathers the fields itself
             for(size_t i = b; i-- > a;)
-                if(int r = stepAdjoint(d, d->blobPtrs(d->seg[i - a]), lam, st))
+                if(int r = stepAdjoint(d, d->blobPtrs(d->seg[i - a]), lam, st, i + 1 < b ? d->gathered[i - a] : nullptr))
                     return r;
         }
         return PICGB_OK;

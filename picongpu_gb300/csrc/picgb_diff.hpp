@@ -33,6 +33,7 @@ namespace picgb::diff
         void const* E,
         void const* B,
         void* J,
+        void* gathered, // [6][n] gathered E and B of each particle are stored here, or null
         DiffGridDesc const& g,
         cudaStream_t st);
     cudaError_t launchDiffAdjoint(
@@ -46,6 +47,7 @@ namespace picgb::diff
         void* lamB,
         void* lamPos,
         void* lamMom,
+        void const* gathered, // [6][n] from launchDiffPush of the same step, or null (gathered again)
         DiffGridDesc const& g,
         cudaStream_t st);
     // A += alpha * curl(F) (3-component SoA fields), forward or backward differences
