@@ -18,6 +18,9 @@ namespace picgb::diff
         T const* w; // [n]
         uint64_t n;
         T charge, mass;
+        int32_t* cellOut; // new state (may equal the inputs)
+        T* posOut;
+        T* momOut;
     };
 
     // Everything one particle's step computes from its start state and the fields.
@@ -117,9 +120,9 @@ namespace picgb::diff
         esirkepovDeposit(st.traj, st.qvdt(g), g, J);
         for(int d = 0; d < 3; ++d)
         {
-            sp.cell[d * sp.n + p] = st.newCell[d];
-            sp.pos[d * sp.n + p] = st.newPos[d];
-            sp.mom[d * sp.n + p] = st.newMom[d];
+            sp.cellOut[d * sp.n + p] = st.newCell[d];
+            sp.posOut[d * sp.n + p] = st.newPos[d];
+            sp.momOut[d * sp.n + p] = st.newMom[d];
         }
     }
 
@@ -245,7 +248,10 @@ namespace picgb::diff
             static_cast<T const*>(s.w),
             s.n,
             T(s.charge),
-            T(s.mass)};
+            T(s.mass),
+            s.cellOut ? s.cellOut : s.cell,
+            static_cast<T*>(s.posOut ? s.posOut : s.pos),
+            static_cast<T*>(s.momOut ? s.momOut : s.mom)};
     }
 
     template<typename T>

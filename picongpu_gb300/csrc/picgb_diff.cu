@@ -47,7 +47,6 @@ struct picgb_diff
     std::vector<void*> ckpts; // state at steps 0, K, 2K, ...
     std::vector<void*> seg; // states of one segment during the backward pass
     std::vector<void*> gathered; // per step of a segment: the particles' gathered E, B ([6][n] per species)
-    void* work = nullptr;
     uint32_t nsteps = 0;
     bool haveForward = false;
 
@@ -142,27 +141,31 @@ namespace
         return PICGB_OK;
     }
 
-    // One forward step in place (Simulation::runOneStep with the fused deposit); the particles'
-    // gathered fields go to `gathered` when it is not null.
-    int stepForward(picgb_diff* d, StatePtrs const& s, cudaStream_t st, void* gathered = nullptr)
+    // One forward step (Simulation::runOneStep with the fused deposit) from state s into state
+    // o (o == s: in place; otherwise s is left unchanged); the particles' gathered fields go to
+    // `gathered` when it is not null.
+    int stepForward(picgb_diff* d, StatePtrs const& s, StatePtrs const& o, cudaStream_t st, void* gathered = nullptr)
     {
         double const dt = d->g.dt, c2 = d->g.c * d->g.c;
         CUDA_TRY(cudaMemsetAsync(d->J, 0, d->fieldBytes(), st));
         for(size_t k = 0; k < d->species.size(); ++k)
-            CUDA_TRY(launchDiffPush(
-                d->prec,
-                d->cfg.shape,
-                d->speciesPtr(s, k),
-                s.E,
-                s.B,
-                d->J,
-                d->gatheredPtr(gathered, k),
-                d->g,
-                st));
-        CUDA_TRY(launchDiffCurlAdd(d->prec, s.B, s.E, -0.5 * dt, true, d->g, st));
-        CUDA_TRY(launchDiffCurlAdd(d->prec, s.E, s.B, c2 * dt, false, d->g, st));
-        CUDA_TRY(launchDiffAxpby(d->prec, s.E, -dt / d->g.eps0, d->J, 1.0, 3 * d->nc, st));
-        CUDA_TRY(launchDiffCurlAdd(d->prec, s.B, s.E, -0.5 * dt, true, d->g, st));
+        {
+            DiffSpeciesPtr sp = d->speciesPtr(s, k);
+            sp.cellOut = o.cell[k];
+            sp.posOut = o.pos[k];
+            sp.momOut = o.mom[k];
+            CUDA_TRY(launchDiffPush(d->prec, d->cfg.shape, sp, s.E, s.B, d->J, d->gatheredPtr(gathered, k), d->g, st));
+        }
+        if(o.E != s.E)
+        {
+            CUDA_TRY(cudaMemcpyAsync(o.E, s.E, d->fieldBytes(), cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(cudaMemcpyAsync(o.B, s.B, d->fieldBytes(), cudaMemcpyDeviceToDevice, st));
+        }
+        StatePtrs const& s2 = o; // the field update runs on the output fields
+        CUDA_TRY(launchDiffCurlAdd(d->prec, s2.B, s2.E, -0.5 * dt, true, d->g, st));
+        CUDA_TRY(launchDiffCurlAdd(d->prec, s2.E, s2.B, c2 * dt, false, d->g, st));
+        CUDA_TRY(launchDiffAxpby(d->prec, s2.E, -dt / d->g.eps0, d->J, 1.0, 3 * d->nc, st));
+        CUDA_TRY(launchDiffCurlAdd(d->prec, s2.B, s2.E, -0.5 * dt, true, d->g, st));
         return PICGB_OK;
     }
 
@@ -215,8 +218,6 @@ namespace
             CUDA_TRY(cudaMalloc(&p, d->gatheredBytes()));
             d->gathered.push_back(p);
         }
-        if(!d->work)
-            CUDA_TRY(cudaMalloc(&d->work, d->blobBytes));
         return PICGB_OK;
     }
 
@@ -291,8 +292,6 @@ extern "C"
             cudaFree(p);
         for(void* p : d->gathered)
             cudaFree(p);
-        if(d->work)
-            cudaFree(d->work);
         if(d->J)
             cudaFree(d->J);
         if(d->lamJ)
@@ -321,7 +320,7 @@ extern "C"
             if(i % K == 0)
                 if(int r = copyState(d, d->blobPtrs(d->ckpts[i / K]), s, st))
                     return r;
-            if(int r = stepForward(d, s, st))
+            if(int r = stepForward(d, s, s, st))
                 return r;
         }
         d->nsteps = nsteps;
@@ -344,20 +343,15 @@ extern "C"
         size_t const N = d->nsteps;
         if(N == 0)
             return PICGB_OK;
-        StatePtrs const work = d->blobPtrs(d->work);
         for(size_t sidx = (N + K - 1) / K; sidx-- > 0;)
         {
             size_t const a = sidx * K, b = std::min(N, a + K);
-            if(int r = copyState(d, work, d->blobPtrs(d->ckpts[sidx]), st))
+            // replay the segment: each step reads the state of step i and writes that of step i + 1
+            if(int r = copyState(d, d->blobPtrs(d->seg[0]), d->blobPtrs(d->ckpts[sidx]), st))
                 return r;
-            for(size_t i = a; i < b; ++i)
-            {
-                if(int r = copyState(d, d->blobPtrs(d->seg[i - a]), work, st))
+            for(size_t i = a; i + 1 < b; ++i)
+                if(int r = stepForward(d, d->blobPtrs(d->seg[i - a]), d->blobPtrs(d->seg[i - a + 1]), st, d->gathered[i - a]))
                     return r;
-                if(i + 1 < b)
-                    if(int r = stepForward(d, work, st, d->gathered[i - a]))
-                        return r;
-            }
             // the last step of the segment was not replayed: its adjoint gathers the fields itself
             for(size_t i = b; i-- > a;)
                 if(int r = stepAdjoint(d, d->blobPtrs(d->seg[i - a]), lam, st, i + 1 < b ? d->gathered[i - a] : nullptr))

@@ -23,6 +23,10 @@ namespace picgb::diff
         void const* w;
         uint64_t n;
         double charge, mass; // per real particle
+        // where the push writes the new cell, pos, mom (null: in place)
+        int32_t* cellOut = nullptr;
+        void* posOut = nullptr;
+        void* momOut = nullptr;
     };
 
     // precision: 4 (float) or 8 (double); shape: 1 CIC, 2 TSC, 3 PQS
