@@ -8,6 +8,8 @@
 namespace picgb::diff
 {
     constexpr int kDiffThreads = 128;
+    // rows per particle of the fields kept by the replay: 6 values and 6 x 3 position gradients
+    constexpr int kGatherRows = 24;
 
     template<typename T>
     struct DiffParticles
@@ -34,14 +36,16 @@ namespace picgb::diff
         DBoris<T> boris;
         DTrajectory<SHAPE, T> traj;
 
-        // gathered: the six field values of this particle from an earlier pass ([6][n]), or null
+        // gathered: this particle's six field values and their position gradients from an
+        // earlier pass ([kGatherRows][n]), or null
         __device__ void run(
             DiffParticles<T> const& sp,
             uint64_t p,
             T const* E,
             T const* B,
             DiffGrid<T> const& g,
-            T const* gathered = nullptr)
+            T const* gathered = nullptr,
+            T* keep = nullptr)
         {
             size_t const nc = size_t(g.nx) * g.ny * g.nz;
             for(int d = 0; d < 3; ++d)
@@ -60,6 +64,21 @@ namespace picgb::diff
             {
                 for(int comp = 0; comp < 6; ++comp)
                     f6[comp] = gathered[comp * sp.n + p];
+            }
+            else if(keep)
+            {
+                // the fields and their gradients, kept for the adjoint of this step
+                DGather<SHAPE, T> gw;
+                gw.compute(cell, pos, g);
+#pragma unroll 1
+                for(int comp = 0; comp < 6; ++comp)
+                {
+                    T gr[3];
+                    f6[comp] = gw.valueGradAt(comp < 3 ? E + comp * nc : B + (comp - 3) * nc, comp, gr);
+                    keep[comp * sp.n + p] = f6[comp];
+                    for(int d = 0; d < 3; ++d)
+                        keep[(6 + 3 * comp + d) * sp.n + p] = gr[d];
+                }
             }
             else
             {
@@ -110,13 +129,7 @@ namespace picgb::diff
         if(p >= sp.n)
             return;
         ParticleStep<SHAPE, T> st;
-        st.run(sp, p, E, B, g);
-        if(gathered) // kept for the adjoint of this step
-            for(int d = 0; d < 3; ++d)
-            {
-                gathered[d * sp.n + p] = st.Ef[d];
-                gathered[(3 + d) * sp.n + p] = st.Bf[d];
-            }
+        st.run(sp, p, E, B, g, nullptr, gathered);
         esirkepovDeposit(st.traj, st.qvdt(g), g, J);
         for(int d = 0; d < 3; ++d)
         {
@@ -177,7 +190,15 @@ namespace picgb::diff
         {
             size_t const o = size_t(comp % 3) * nc;
             T const lam = comp == 0 ? l6[0] : comp == 1 ? l6[1] : comp == 2 ? l6[2] : comp == 3 ? l6[3] : comp == 4 ? l6[4] : l6[5];
-            gw.adjointAt(comp < 3 ? E + o : B + o, comp < 3 ? lamE + o : lamB + o, comp, lam, gpos);
+            if(gathered)
+            {
+                // position gradient from the kept field gradients; only the scatter remains
+                for(int d = 0; d < 3; ++d)
+                    gpos[d] += lam * gathered[(6 + 3 * comp + d) * sp.n + p];
+                gw.scatterAt(comp < 3 ? lamE + o : lamB + o, comp, lam);
+            }
+            else
+                gw.adjointAt(comp < 3 ? E + o : B + o, comp < 3 ? lamE + o : lamB + o, comp, lam, gpos);
         }
         for(int d = 0; d < 3; ++d)
         {

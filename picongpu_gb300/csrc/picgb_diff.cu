@@ -46,7 +46,7 @@ struct picgb_diff
     size_t blobBytes = 0;
     std::vector<void*> ckpts; // state at steps 0, K, 2K, ...
     std::vector<void*> seg; // states of one segment during the backward pass
-    std::vector<void*> gathered; // per step of a segment: the particles' gathered E, B ([6][n] per species)
+    std::vector<void*> gathered; // per step of a segment: the particles' gathered E, B and gradients ([24][n])
     uint32_t nsteps = 0;
     bool haveForward = false;
 
@@ -90,7 +90,7 @@ struct picgb_diff
     {
         size_t b = 0;
         for(auto const& sp : species)
-            b += (6 * sp.n * esz + 255) / 256 * 256;
+            b += (24 * sp.n * esz + 255) / 256 * 256;
         return b;
     }
 
@@ -101,7 +101,7 @@ struct picgb_diff
             return nullptr;
         size_t off = 0;
         for(size_t i = 0; i < k; ++i)
-            off += (6 * species[i].n * esz + 255) / 256 * 256;
+            off += (24 * species[i].n * esz + 255) / 256 * 256;
         return static_cast<char*>(buf) + off;
     }
 

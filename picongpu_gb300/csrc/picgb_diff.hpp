@@ -37,7 +37,7 @@ namespace picgb::diff
         void const* E,
         void const* B,
         void* J,
-        void* gathered, // [6][n] gathered E and B of each particle are stored here, or null
+        void* gathered, // [24][n]: gathered E, B and their position gradients are stored here, or null
         DiffGridDesc const& g,
         cudaStream_t st);
     cudaError_t launchDiffAdjoint(
@@ -51,7 +51,7 @@ namespace picgb::diff
         void* lamB,
         void* lamPos,
         void* lamMom,
-        void const* gathered, // [6][n] from launchDiffPush of the same step, or null (gathered again)
+        void const* gathered, // [24][n] from launchDiffPush of the same step, or null (gathered again)
         DiffGridDesc const& g,
         cudaStream_t st);
     // A += alpha * curl(F) (3-component SoA fields), forward or backward differences

@@ -225,6 +225,67 @@ namespace picgb::diff
             return rz;
         }
 
+        // valueAt() and its gradient with respect to the particle position (nested sums)
+        __device__ T valueGradAt(T const* __restrict__ F, int comp, T grad[3]) const
+        {
+            T wx[S], wy[S], wz[S], dx[S], dy[S], dz[S];
+            uint32_t ox[S], oy[S], oz[S];
+            axis(0, stagger(comp, 0), wx, dx, ox);
+            axis(1, stagger(comp, 1), wy, dy, oy);
+            axis(2, stagger(comp, 2), wz, dz, oz);
+            T v = T(0), gx = T(0), gy = T(0), gz = T(0);
+#pragma unroll
+            for(int z = 0; z < S; ++z)
+            {
+                T pz = T(0), pdx = T(0), pdy = T(0);
+#pragma unroll
+                for(int y = 0; y < S; ++y)
+                {
+                    T sx = T(0), sdx = T(0);
+#pragma unroll
+                    for(int x = 0; x < S; ++x)
+                    {
+                        T const f = F[oz[z] + oy[y] + ox[x]];
+                        sx += f * wx[x];
+                        sdx += f * dx[x];
+                    }
+                    pz += wy[y] * sx;
+                    pdx += wy[y] * sdx;
+                    pdy += dy[y] * sx;
+                }
+                v += wz[z] * pz;
+                gx += wz[z] * pdx;
+                gy += wz[z] * pdy;
+                gz += dz[z] * pz;
+            }
+            grad[0] = gx;
+            grad[1] = gy;
+            grad[2] = gz;
+            return v;
+        }
+
+        // scatter part of adjointAt() alone: lam * weights added into lamF
+        __device__ void scatterAt(T* __restrict__ lamF, int comp, T lam) const
+        {
+            if(lam == T(0))
+                return;
+            T wx[S], wy[S], wz[S], dx[S], dy[S], dz[S];
+            uint32_t ox[S], oy[S], oz[S];
+            axis(0, stagger(comp, 0), wx, dx, ox);
+            axis(1, stagger(comp, 1), wy, dy, oy);
+            axis(2, stagger(comp, 2), wz, dz, oz);
+#pragma unroll
+            for(int z = 0; z < S; ++z)
+#pragma unroll
+                for(int y = 0; y < S; ++y)
+                {
+                    T const lyz = lam * wy[y] * wz[z];
+#pragma unroll
+                    for(int x = 0; x < S; ++x)
+                        atomicAdd(lamF + oz[z] + oy[y] + ox[x], lyz * wx[x]);
+                }
+        }
+
         // adjoint of valueAt(): lam * weights scattered into lamF, and the position gradient
         __device__ void adjointAt(T const* __restrict__ F, T* __restrict__ lamF, int comp, T lam, T gpos[3]) const
         {
