@@ -281,43 +281,6 @@ namespace picgb
         }
     };
 
-    // FieldToParticleInterpolation (algorithms/FieldToParticleInterpolation.hpp:97-124) of one
-    // component with field position (fx, fy, fz).
-    template<typename SH, int TX, int TY>
-    __device__ __forceinline__ float gatherComponent(
-        float const* __restrict__ tile,
-        int lx,
-        int ly,
-        int lz,
-        float px,
-        float py,
-        float pz,
-        float fx,
-        float fy,
-        float fz)
-    {
-        constexpr int S = SH::supp;
-        float const pin[3] = {px, py, pz};
-        float const fp[3] = {fx, fy, fz};
-        int shift[3];
-        float p[3];
-#pragma unroll
-        for(int d = 0; d < 3; ++d)
-        {
-            float v = fs(fs(pin[d], fp[d]), 0.5f);
-            if constexpr(SH::even)
-                shift[d] = v >= -0.5f ? 0 : -1;
-            else
-                shift[d] = v >= 0.0f ? 1 : 0;
-            p[d] = fa(fs(v, float(shift[d])), 0.5f);
-        }
-        float sx[S], sy[S], sz[S];
-        SH::base(p[0], sx);
-        SH::base(p[1], sy);
-        SH::base(p[2], sz);
-        return interpolate<SH, TX, TY>(tile, lx, ly, lz, shift[0], shift[1], shift[2], sx, sy, sz);
-    }
-
     // ------------------------------------------------------------ push
     __device__ __forceinline__ float l2n2(float a, float b, float c) { return fa(fa(fm(a, a), fm(b, b)), fm(c, c)); }
 
