@@ -434,6 +434,34 @@ def run_laser_wake(args, local_rank):
             "timing": "host clock around the steps, stream synchronised on both sides"}
 
 
+def run_pushers(args, local_rank):
+    """The two-stream workload on 128^3 cells with each field pusher: Boris, HigueraCary and Vay
+    (the last two with their square-root stages in double, the reference's default).  Host clock
+    around the timed steps, stream synchronised on both sides."""
+    import picongpu_gb300 as pg
+
+    wl = dict(WORKLOADS["two_stream_256"], n=(128, 128, 128))
+    out = {"workload": "two-stream 128^3 cells, 2 species x 16 ppc, TSC, Esirkepov, Yee, fp32 (pusher square "
+                       "roots in fp64 for HigueraCary and Vay)", "steps": args.pusher_steps, "unit": "particle-steps/s"}
+    for pusher in ("Boris", "HigueraCary", "Vay"):
+        g = pg.Grid(*wl["n"], dt=DT, supercell=(8, 8, 4), device=local_rank)
+        with pg.Simulation(g) as sim:
+            sim.add_species(pg.Species("e", -1.0, 1.0, pusher=pusher, shape=wl["shape"]))
+            sim.add_species(pg.Species("i", 1.0, MASS_P, pusher=pusher, shape=wl["shape"]))
+            init_plasma(sim, wl)
+            npart = sim.particle_count("e") + sim.particle_count("i")
+            for _ in range(args.warmup):
+                sim.step()
+            sim.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.pusher_steps):
+                sim.step()
+            sim.synchronize()
+            dt_wall = time.perf_counter() - t0
+        out[pusher] = npart * args.pusher_steps / dt_wall
+    return out
+
+
 # ---------------------------------------------------------------------- differentiable run
 def adjoint_case(A, n, ppc, precision, checkpoint_every):
     dens = (0.1 / DT) ** 2
@@ -539,6 +567,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-laser", action="store_true")
     ap.add_argument("--laser-steps", type=int, default=40)
+    ap.add_argument("--no-pushers", action="store_true")
+    ap.add_argument("--pusher-steps", type=int, default=20)
     ap.add_argument("--adjoint-steps", type=int, default=300)
     ap.add_argument("--adjoint-fd-steps", type=int, default=20)
     args = ap.parse_args()
@@ -589,6 +619,9 @@ def main():
     laser = None
     if not args.no_laser:
         laser = run_laser_wake(args, local_rank)
+    pushers = None
+    if not args.no_pushers:
+        pushers = run_pushers(args, local_rank)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         val, cores, sample = cpu_sample_rate(wl, 10, 1, budget_s=20.0)
@@ -598,7 +631,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded device init)", "config": config,
             "particles": r["npart"], "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"],
             "clocks": r["clocks"], "gpu_launches": r["launches"], "batched": batched, "adjoint": adjoint,
-            "laser_wake": laser}
+            "laser_wake": laser, "pushers": pushers}
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch

@@ -56,7 +56,9 @@ extern "C"
     {
         PICGB_PUSHER_BORIS = 0, /* particles/pusher/particlePusherBoris.hpp */
         PICGB_PUSHER_FREE = 1, /* particles/pusher/particlePusherFree.hpp */
-        PICGB_PUSHER_NONE = 2 /* species without the particlePusher<> flag: not pushed (immobile) */
+        PICGB_PUSHER_NONE = 2, /* species without the particlePusher<> flag: not pushed (immobile) */
+        PICGB_PUSHER_HIGUERA_CARY = 3, /* particles/pusher/particlePusherHigueraCary.hpp, square roots in double */
+        PICGB_PUSHER_VAY = 4 /* particles/pusher/particlePusherVay.hpp, square roots in double */
     };
     enum picgb_shape
     {

@@ -4,7 +4,8 @@ The oracle is a plain C++ restatement (``pic_oracle.hpp``) of PIConGPU's
 reference algorithms for the electromagnetic PIC step: Yee field solver
 (fields/MaxwellSolver/FDTD/FDTDBase.kernel), form-factor gather
 (algorithms/FieldToParticleInterpolation.hpp), Boris push
-(particles/pusher/particlePusherBoris.hpp), moveParticle
+(particles/pusher/particlePusherBoris.hpp, particlePusherHigueraCary.hpp,
+particlePusherVay.hpp), moveParticle
 (particles/MoveParticle.hpp), Esirkepov deposition
 (fields/currentDeposition/Esirkepov/Esirkepov.hpp) and the energy and charge
 conservation diagnostics.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
@@ -62,10 +63,16 @@ class OrcParticles(ctypes.Structure):
     ]
 
 
+def _stale() -> bool:
+    t = os.path.getmtime(_LIB_PATH)
+    return any(os.path.getmtime(os.path.join(_HERE, f)) > t for f in ("oracle_capi.cpp", "pic_oracle.hpp", "Makefile"))
+
+
 def build(force: bool = False) -> str:
-    """Compile the oracle shared library with its Makefile (g++, OpenMP)."""
-    if force or not os.path.exists(_LIB_PATH):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the oracle shared library with its Makefile (g++, OpenMP); make rebuilds
+    it when a source is newer than the library."""
+    if force or not os.path.exists(_LIB_PATH) or _stale():
+        subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return _LIB_PATH
 
 

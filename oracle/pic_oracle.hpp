@@ -94,7 +94,9 @@ namespace orc
     enum Pusher
     {
         BORIS = 0,
-        FREE = 1
+        FREE = 1,
+        HIGUERA_CARY = 3,
+        VAY = 4
     };
 
     struct SpeciesParam
@@ -501,6 +503,105 @@ namespace orc
             pos[d] += (vel[d] * deltaT) / cs[d];
     }
 
+    template<typename T>
+    inline T dot3(T const a[3], T const b[3])
+    {
+        T r = a[0] * b[0];
+        r += a[1] * b[1];
+        r += a[2] * b[2];
+        return r;
+    }
+
+    // pmacc::math::cross (pmacc/math/vector/Vector.tpp:71-77)
+    template<typename T>
+    inline void cross3(T const a[3], T const b[3], T r[3])
+    {
+        r[0] = a[1] * b[2] - a[2] * b[1];
+        r[1] = a[2] * b[0] - a[0] * b[2];
+        r[2] = a[0] * b[1] - a[1] * b[0];
+    }
+
+    // Position update shared by the pushers: pos += vel dt / cellSize
+    template<typename T>
+    inline void advance(Grid const& g, T mass, T const mom[3], T pos[3])
+    {
+        T vel[3];
+        velocityOf(mom, mass, T(g.c), vel);
+        T const cs[3] = {T(g.dx), T(g.dy), T(g.dz)};
+        for(int d = 0; d < 3; ++d)
+            pos[d] += (vel[d] * T(g.dt)) / cs[d];
+    }
+
+    // HigueraCary (particles/pusher/particlePusherHigueraCary.hpp:85-135).  T is
+    // float_X; D is the precision of the square-root stages (param/pusher.param:65-72,
+    // precision64Bit by default).  Every cast sits where the reference's types put it.
+    template<typename T, typename D>
+    inline void higueraCaryPush(Grid const& g, T charge, T mass, T const E[3], T const B[3], T mom[3], T pos[3])
+    {
+        T const deltaT = T(g.dt);
+        T const c = T(g.c);
+        T mmT[3];
+        for(int d = 0; d < 3; ++d)
+            mmT[d] = mom[d] + T(0.5) * charge * E[d] * deltaT;
+        D const mm[3] = {D(mmT[0]), D(mmT[1]), D(mmT[2])};
+        D const gamma_minus = D(gammaOf(mmT, mass, c)); // Gamma<float_X> casts the momentum back
+        D tau[3];
+        for(int d = 0; d < 3; ++d)
+            tau[d] = D(T(0.5) * B[d] * charge * deltaT / mass);
+        D const sigma = gamma_minus * gamma_minus - l2norm2(tau);
+        D const u_star = dot3(mm, tau) / D(mass * c);
+        D const gamma_plus = std::sqrt(D(0.5) * (sigma + std::sqrt(sigma * sigma + D(4.0) * (l2norm2(tau) + u_star * u_star))));
+        D tv[3];
+        for(int d = 0; d < 3; ++d)
+            tv[d] = tau[d] / gamma_plus;
+        D const s = D(1.0) / (D(1.0) + l2norm2(tv));
+        D const mt = dot3(mm, tv);
+        D cr[3], mp[3], cr2[3];
+        cross3(mm, tv, cr);
+        for(int d = 0; d < 3; ++d)
+            mp[d] = s * (mm[d] + mt * tv[d] + cr[d]);
+        cross3(mp, tv, cr2);
+        for(int d = 0; d < 3; ++d)
+        {
+            T const diff = T(0.5) * charge * E[d] * deltaT + T(cr2[d]);
+            mom[d] = T(mp[d]) + diff;
+        }
+        advance(g, mass, mom, pos);
+    }
+
+    // Vay (particles/pusher/particlePusherVay.hpp:72-110), precisions as in higueraCaryPush.
+    template<typename T, typename D>
+    inline void vayPush(Grid const& g, T charge, T mass, T const E[3], T const B[3], T mom[3], T pos[3])
+    {
+        T const deltaT = T(g.dt);
+        T const c = T(g.c);
+        T const factor = T(0.5 * double(charge) * double(deltaT));
+        T v[3], cvb[3], mp[3];
+        velocityOf(mom, mass, c, v);
+        cross3(v, B, cvb);
+        for(int d = 0; d < 3; ++d)
+        {
+            T const atZero = mom[d] + factor * (E[d] + cvb[d]);
+            mp[d] = atZero + factor * E[d];
+        }
+        T const gamma_prime = gammaOf(mp, mass, c);
+        T const fom = factor / mass;
+        D const tau[3] = {D(fom * B[0]), D(fom * B[1]), D(fom * B[2])};
+        D const mpD[3] = {D(mp[0]), D(mp[1]), D(mp[2])};
+        D const u_star = dot3(mpD, tau) / D(c * mass);
+        D const sigma = D(gamma_prime * gamma_prime) - l2norm2(tau);
+        D const gamma_half = std::sqrt(D(0.5) * (sigma + std::sqrt(sigma * sigma + D(4.0) * (l2norm2(tau) + u_star * u_star))));
+        D const rg = D(T(1.0)) / gamma_half;
+        T const t[3] = {T(tau[0] * rg), T(tau[1] * rg), T(tau[2] * rg)};
+        T const s = T(1.0) / (T(1.0) + l2norm2(t));
+        T const mt = dot3(mp, t);
+        T cr[3];
+        cross3(mp, t, cr);
+        for(int d = 0; d < 3; ++d)
+            mom[d] = s * (mp[d] + mt * t[d] + cr[d]);
+        advance(g, mass, mom, pos);
+    }
+
     // Free streaming (particles/pusher/particlePusherFree.hpp:40-72)
     template<typename T>
     inline void freePush(Grid const& g, T mass, T const mom[3], T pos[3])
@@ -593,12 +694,17 @@ namespace orc
             T const w = P.w[k];
             T const mass = T(sp.mass) * w; // traits/attribute/GetMass.hpp:34-37
             T const charge = T(sp.charge) * w; // traits/attribute/GetCharge.hpp:46
-            if(sp.pusher == BORIS)
+            if(sp.pusher == BORIS || sp.pusher == HIGUERA_CARY || sp.pusher == VAY)
             {
                 T Bv[3], Ev[3];
                 gather(g, sp.shape, B, kPosB, cell, pos, Bv);
                 gather(g, sp.shape, E, kPosE, cell, pos, Ev);
-                borisPush(g, charge, mass, Ev, Bv, mom, pos);
+                if(sp.pusher == BORIS)
+                    borisPush(g, charge, mass, Ev, Bv, mom, pos);
+                else if(sp.pusher == HIGUERA_CARY)
+                    higueraCaryPush<T, double>(g, charge, mass, Ev, Bv, mom, pos);
+                else
+                    vayPush<T, double>(g, charge, mass, Ev, Bv, mom, pos);
             }
             else
                 freePush(g, mass, mom, pos);

@@ -200,8 +200,8 @@ namespace picgb
         scCoords(sc, g, scx, scy, scz);
         int const ox = scx * SX, oy = scy * SY, oz = scz * SZ;
         size_t const ncell = size_t(g.nx) * g.ny * g.nz;
-        bool const useBoris = (pp.pusher == 0);
-        if(useBoris)
+        bool const useFields = (pp.pusher != kPusherFree); // Boris, HigueraCary, Vay
+        if(useFields)
         {
             loadTile<TG::GX, TG::GY, TG::GT>(Es, E, ox - SH::gLo, oy - SH::gLo, oz - SH::gLo, g, ncell);
             loadTile<TG::GX, TG::GY, TG::GT>(Bs, B, ox - SH::gLo, oy - SH::gLo, oz - SH::gLo, g, ncell);
@@ -230,7 +230,7 @@ namespace picgb
                 float const mass = fm(pp.mass, w);
                 charge = fm(pp.charge, w);
                 float vel[3];
-                if(useBoris)
+                if(useFields)
                 {
                     float Ev[3], Bv[3];
                     GatherWeights<SH> gw;
@@ -242,7 +242,20 @@ namespace picgb
                     Ev[0] = gw.template gather<TG::GX, TG::GY, 1, 0, 0>(Es, lx, ly, lz);
                     Ev[1] = gw.template gather<TG::GX, TG::GY, 0, 1, 0>(Es + TG::GT, lx, ly, lz);
                     Ev[2] = gw.template gather<TG::GX, TG::GY, 0, 0, 1>(Es + 2 * TG::GT, lx, ly, lz);
-                    boris(charge, mass, Ev, Bv, pp.dt, pp.c2, pp.rc2, mom, vel);
+                    if(pp.pusher == kPusherBoris)
+                        boris(charge, mass, Ev, Bv, pp.dt, pp.c2, pp.rc2, mom, vel);
+                    else
+                    {
+                        float3 const e3 = make_float3(Ev[0], Ev[1], Ev[2]), b3 = make_float3(Bv[0], Bv[1], Bv[2]);
+                        float3 const m3 = make_float3(mom[0], mom[1], mom[2]);
+                        float3 const r = pp.pusher == kPusherHigueraCary
+                            ? higueraCary(charge, mass, e3, b3, pp.dt, pp.c, pp.c2, m3)
+                            : vay(charge, mass, e3, b3, pp.dt, pp.c, pp.c2, pp.rc2, m3);
+                        mom[0] = r.x;
+                        mom[1] = r.y;
+                        mom[2] = r.z;
+                        velocity(mom, mass, pp.rc2, vel);
+                    }
                 }
                 else
                     velocity(mom, mass, pp.rc2, vel);

@@ -42,6 +42,7 @@ PushParams picgb_sim::pushParams(Species const& s, bool deposit) const
     p.rc2 = 1.0f / (cfg.c * cfg.c);
     float const vdt = cellVolume() * cfg.dt;
     p.invVdt = 1.0f / vdt;
+    p.c = cfg.c;
     p.pusher = s.cfg.pusher;
     p.deposit = deposit ? 1 : 0;
     p.kindCount = prof ? kindCount : nullptr;
@@ -504,7 +505,7 @@ extern "C"
             return r;
         if(!cfg || !cfg->name || !cfg->name[0])
             return fail(PICGB_ERR_INVALID, "species needs a name");
-        if(cfg->pusher < 0 || cfg->pusher > 2)
+        if(cfg->pusher < PICGB_PUSHER_BORIS || cfg->pusher > PICGB_PUSHER_VAY)
             return fail(PICGB_ERR_INVALID, "unknown pusher %d", int(cfg->pusher));
         if(cfg->shape < PICGB_SHAPE_CIC || cfg->shape > PICGB_SHAPE_PQS)
             return fail(PICGB_ERR_UNSUPPORTED, "shape %d has no CUDA kernel (CIC, TSC, PQS are available)",

@@ -340,6 +340,94 @@ namespace picgb
         velocity(mom, mass, rc2, vel);
     }
 
+    // ---- HigueraCary and Vay.  Their square-root stages run in double, the
+    // reference's default (param/pusher.param:56-72, precision64Bit); the rest in
+    // float, with every float<->double cast where the reference's types put it.
+    __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+    __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+    __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+    __device__ __forceinline__ double ddv(double a, double b) { return __ddiv_rn(a, b); }
+    __device__ __forceinline__ double dsq(double a) { return __dsqrt_rn(a); }
+    __device__ __forceinline__ double dl2n2(double a, double b, double c) { return da(da(dm(a, a), dm(b, b)), dm(c, c)); }
+
+    // Gamma<float_X> (algorithms/Gamma.hpp:30-37)
+    __device__ __forceinline__ float gammaOf(float a, float b, float c, float mass, float c2)
+    {
+        float const m2_c2_reci = frcp(fm(fm(mass, mass), c2));
+        return fsq(fa(1.0f, fm(l2n2(a, b, c), m2_c2_reci)));
+    }
+
+    // HigueraCary (particles/pusher/particlePusherHigueraCary.hpp:85-135): the new
+    // momentum.  Kept out of line so the Boris kernels keep their register budget.
+    __device__ __noinline__ float3 higueraCary(float charge, float mass, float3 E, float3 B, float dt, float c, float c2, float3 mom)
+    {
+        float const hq = fm(0.5f, charge);
+        // mom_minus = mom + 0.5 q E dt (float), then held in double
+        float const mf[3] = {fa(mom.x, fm(fm(hq, E.x), dt)), fa(mom.y, fm(fm(hq, E.y), dt)), fa(mom.z, fm(fm(hq, E.z), dt))};
+        double const mm[3] = {mf[0], mf[1], mf[2]};
+        double const gm = gammaOf(mf[0], mf[1], mf[2], mass, c2);
+        // tau = 0.5 B q dt / m (float), then held in double
+        double const tau[3] = {fdv(fm(fm(fm(0.5f, B.x), charge), dt), mass), fdv(fm(fm(fm(0.5f, B.y), charge), dt), mass),
+                               fdv(fm(fm(fm(0.5f, B.z), charge), dt), mass)};
+        double const tau2 = dl2n2(tau[0], tau[1], tau[2]);
+        double const sigma = ds(dm(gm, gm), tau2);
+        double const ustar = ddv(da(da(dm(mm[0], tau[0]), dm(mm[1], tau[1])), dm(mm[2], tau[2])), double(fm(mass, c)));
+        double const gp = dsq(dm(0.5, da(sigma, dsq(da(dm(sigma, sigma), dm(4.0, da(tau2, dm(ustar, ustar))))))));
+        double const t[3] = {ddv(tau[0], gp), ddv(tau[1], gp), ddv(tau[2], gp)};
+        double const s = ddv(1.0, da(1.0, dl2n2(t[0], t[1], t[2])));
+        double const mt = da(da(dm(mm[0], t[0]), dm(mm[1], t[1])), dm(mm[2], t[2]));
+        double const cr[3] = {ds(dm(mm[1], t[2]), dm(mm[2], t[1])), ds(dm(mm[2], t[0]), dm(mm[0], t[2])),
+                              ds(dm(mm[0], t[1]), dm(mm[1], t[0]))};
+        double mp[3];
+#pragma unroll
+        for(int d = 0; d < 3; ++d)
+            mp[d] = dm(s, da(da(mm[d], dm(mt, t[d])), cr[d]));
+        // the second half acceleration plus the rotation term cross(mom_plus, t), summed in float
+        float const d2[3] = {__double2float_rn(ds(dm(mp[1], t[2]), dm(mp[2], t[1]))),
+                             __double2float_rn(ds(dm(mp[2], t[0]), dm(mp[0], t[2]))),
+                             __double2float_rn(ds(dm(mp[0], t[1]), dm(mp[1], t[0])))};
+        float3 r;
+        r.x = fa(__double2float_rn(mp[0]), fa(fm(fm(hq, E.x), dt), d2[0]));
+        r.y = fa(__double2float_rn(mp[1]), fa(fm(fm(hq, E.y), dt), d2[1]));
+        r.z = fa(__double2float_rn(mp[2]), fa(fm(fm(hq, E.z), dt), d2[2]));
+        return r;
+    }
+
+    // Vay (particles/pusher/particlePusherVay.hpp:72-103): the new momentum.
+    __device__ __noinline__ float3 vay(float charge, float mass, float3 E, float3 B, float dt, float c, float c2, float rc2, float3 mom)
+    {
+        float const factor = fm(fm(0.5f, charge), dt);
+        float const m[3] = {mom.x, mom.y, mom.z};
+        float v[3];
+        velocity(m, mass, rc2, v);
+        float const Ev[3] = {E.x, E.y, E.z}, Bv[3] = {B.x, B.y, B.z};
+        float const cvb[3] = {fs(fm(v[1], Bv[2]), fm(v[2], Bv[1])), fs(fm(v[2], Bv[0]), fm(v[0], Bv[2])),
+                              fs(fm(v[0], Bv[1]), fm(v[1], Bv[0]))};
+        float mp[3];
+#pragma unroll
+        for(int d = 0; d < 3; ++d)
+            mp[d] = fa(fa(m[d], fm(factor, fa(Ev[d], cvb[d]))), fm(factor, Ev[d])); // momentum_atZero, momentum_prime
+        float const gprime = gammaOf(mp[0], mp[1], mp[2], mass, c2);
+        float const fom = fdv(factor, mass);
+        double const tau[3] = {fm(fom, Bv[0]), fm(fom, Bv[1]), fm(fom, Bv[2])};
+        double const tau2 = dl2n2(tau[0], tau[1], tau[2]);
+        double const ustar = ddv(da(da(dm(mp[0], tau[0]), dm(mp[1], tau[1])), dm(mp[2], tau[2])), double(fm(c, mass)));
+        double const sigma = ds(double(fm(gprime, gprime)), tau2);
+        double const gph = dsq(dm(0.5, da(sigma, dsq(da(dm(sigma, sigma), dm(4.0, da(tau2, dm(ustar, ustar))))))));
+        double const rg = ddv(1.0, gph);
+        float const t[3] = {__double2float_rn(dm(tau[0], rg)), __double2float_rn(dm(tau[1], rg)),
+                            __double2float_rn(dm(tau[2], rg))};
+        float const s = frcp(fa(1.0f, l2n2(t[0], t[1], t[2])));
+        float const mt = fa(fa(fm(mp[0], t[0]), fm(mp[1], t[1])), fm(mp[2], t[2]));
+        float const cr[3] = {fs(fm(mp[1], t[2]), fm(mp[2], t[1])), fs(fm(mp[2], t[0]), fm(mp[0], t[2])),
+                             fs(fm(mp[0], t[1]), fm(mp[1], t[0]))};
+        float3 r;
+        r.x = fm(s, fa(fa(mp[0], fm(mt, t[0])), cr[0]));
+        r.y = fm(s, fa(fa(mp[1], fm(mt, t[1])), cr[1]));
+        r.z = fm(s, fa(fa(mp[2], fm(mt, t[2])), cr[2]));
+        return r;
+    }
+
     // moveParticle (particles/MoveParticle.hpp:48-160).  pos in [-1,2) on entry,
     // [0,1) on exit; mv = cell move per axis; returns the supercell leave
     // direction through dir (0 when the particle stays inside its supercell).

@@ -61,6 +61,12 @@ namespace picgb
         uint32_t spill_cap;
     };
 
+    // PushParams::pusher values (the C-ABI's enum picgb_pusher)
+    constexpr int kPusherBoris = 0;
+    constexpr int kPusherFree = 1;
+    constexpr int kPusherHigueraCary = 3;
+    constexpr int kPusherVay = 4;
+
     struct PushParams
     {
         float charge; // per real particle
@@ -69,7 +75,8 @@ namespace picgb
         float c2; // c * c
         float rc2; // 1 / (c * c)
         float invVdt; // 1 / (dx * dy * dz * dt)
-        int pusher; // 0 Boris, 1 Free (2 = not pushed, never launched)
+        float c; // speed of light (HigueraCary and Vay)
+        int pusher; // 0 Boris, 1 Free, 3 HigueraCary, 4 Vay (2 = not pushed, never launched)
         int deposit; // deposit the current inside the push kernel
         unsigned long long* kindCount; // profiling only: [0] deposits with the short footprint, [1] general; or nullptr
         JFixed jf; // fixed-point format of the J tile (used when built with PICGB_J_FIXED)

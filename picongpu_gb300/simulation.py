@@ -18,7 +18,8 @@ import numpy as np
 from . import _lib as L
 
 # .param policy names -> C-ABI enums (param/species.param:49-90, param/fieldSolver.param:57)
-PUSHERS = {"Boris": L.PUSHER_BORIS, "Free": L.PUSHER_FREE, None: L.PUSHER_NONE}
+PUSHERS = {"Boris": L.PUSHER_BORIS, "Free": L.PUSHER_FREE, "HigueraCary": L.PUSHER_HIGUERA_CARY,
+           "Vay": L.PUSHER_VAY, None: L.PUSHER_NONE}
 SHAPES = {"CIC": L.SHAPE_CIC, "TSC": L.SHAPE_TSC, "PQS": L.SHAPE_PQS}
 CURRENTS = {"Esirkepov": L.CURRENT_ESIRKEPOV, None: L.CURRENT_NONE}
 SOLVERS = {"Yee": L.SOLVER_YEE}
@@ -155,7 +156,9 @@ class Simulation:
 
     # ------------------------------------------------------------ species
     def add_species(self, sp: Species) -> int:
-        pusher = PUSHERS.get(sp.pusher, L.PUSHER_NONE)
+        if sp.pusher not in PUSHERS:
+            raise ValueError(f"unknown pusher {sp.pusher!r}; available: {[k for k in PUSHERS if k]} or None")
+        pusher = PUSHERS[sp.pusher]
         cfg = L.SpeciesConfig(sp.name.encode(), sp.charge, sp.mass, pusher, SHAPES[sp.shape],
                               CURRENTS[sp.current], sp.capacity, int(sp.with_ids))
         idx = ctypes.c_int32()

@@ -9,6 +9,8 @@ Contract (parity bar of the PIC hot path):
   different order than the oracle);
 * E after a full step (it absorbs J): |dE| <= 1e-6 * max|E|.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -82,13 +84,24 @@ def test_yee_bit_exact(orc):
 @pytest.mark.parametrize("sc", [(8, 8, 4), (4, 4, 4), (8, 8, 8)])
 def test_push_and_deposit_one_step(orc, shape, sc):
     """Gather + Boris + move + sort bit-exact; fused Esirkepov deposit within 1e-6."""
+    _push_and_deposit(orc, shape, sc, "Boris")
+
+
+@pytest.mark.parametrize("pusher", ["HigueraCary", "Vay"])
+@pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS"])
+def test_higuera_cary_and_vay_one_step(orc, pusher, shape):
+    """The HigueraCary and Vay pushers (square-root stages in double) bit-exact with the oracle."""
+    _push_and_deposit(orc, shape, (8, 8, 4), pusher, amp=0.3)
+
+
+def _push_and_deposit(orc, shape, sc, pusher, amp=0.05):
     g = make_grid((32, 32, 32) if sc != (8, 8, 8) else (32, 32, 16), sc=sc)
     gd = g.as_dict()
-    rng = np.random.default_rng(100 + len(shape) + sc[2])
+    rng = np.random.default_rng(100 + len(shape) + sc[2] + len(pusher))
     p = random_particles(gd, 4, rng, u_th=0.2, weight=0.01)  # hot: many cell and supercell crossings
-    E = random_field(gd, rng, amp=0.05)
-    B = random_field(gd, rng, amp=0.05)
-    sp = pg.Species("e", charge=-1.0, mass=1.0, shape=shape, with_ids=True)
+    E = random_field(gd, rng, amp=amp)
+    B = random_field(gd, rng, amp=amp)
+    sp = pg.Species("e", charge=-1.0, mass=1.0, pusher=pusher, shape=shape, with_ids=True)
     with pg.Simulation(g) as sim:
         sim.add_species(sp)
         sim.set_particles("e", p)
@@ -223,3 +236,8 @@ def test_invalid_configs_are_rejected():
         with pytest.raises(pg.PicError) as e:
             sim.set_particles("e", bad)
         assert e.value.code == pg._lib.ERR_INVALID
+        with pytest.raises(ValueError):
+            sim.add_species(pg.Species("x", -1.0, 1.0, pusher="Axel"))
+        cfg = pg._lib.SpeciesConfig(b"y", -1.0, 1.0, 5, pg._lib.SHAPE_TSC, 1, 0, 0)
+        idx = ctypes.c_int32()
+        assert pg.load().picgb_add_species(sim.handle, ctypes.byref(cfg), ctypes.byref(idx)) == pg._lib.ERR_INVALID

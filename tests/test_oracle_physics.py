@@ -1,6 +1,8 @@
-"""Analytic invariants of the oracle: Boris gyration (share/picongpu/tests/Pusher),
-discrete charge continuity of the Esirkepov deposit, and the Yee update against
-an independent numpy restatement."""
+"""Analytic invariants of the oracle: gyration of the Boris, HigueraCary and Vay
+pushers (share/picongpu/tests/Pusher), their phase-lag order
+(share/picongpu/tests/PusherScaling), the E x B drift that HigueraCary and Vay keep,
+discrete charge continuity of the Esirkepov deposit, and the Yee update against an
+independent numpy restatement."""
 import numpy as np
 import pytest
 
@@ -14,7 +16,11 @@ def _fit_circle(x, y):
     return s[0] / 2, s[1] / 2
 
 
-def test_boris_gyration(orc):
+PUSHERS = {"Boris": 0, "HigueraCary": 3, "Vay": 4}
+
+
+@pytest.mark.parametrize("pusher", list(PUSHERS))
+def test_gyration(orc, pusher):
     """Electron at 0.5c in uniform B_z, 50 steps per turn (Pusher/README.rst, MainTest.py:177,212):
     radius change per turn < 1e-5 (momentum) and < 5e-5 (position), phase change < 0.16 rad."""
     g = grid(n=(16, 16, 16), sc=(8, 8, 4), dt=0.5)
@@ -27,7 +33,7 @@ def test_boris_gyration(orc):
     p = dict(pos=np.full((3, 1), 0.5, np.float32), mom=np.array([[u], [0], [0]], np.float32),
              w=np.ones(1, np.float32), sc=np.array([1 + 2 * (1 + 2 * 2)], np.int32),
              lcell=np.array([0], np.uint16))
-    sp = dict(charge=-1.0, mass=1.0, shape=2, pusher=0, current=1)
+    sp = dict(charge=-1.0, mass=1.0, shape=2, pusher=PUSHERS[pusher], current=1)
     xs, ys, rp = [], [], []
     last = None
     off = np.zeros(2)
@@ -52,6 +58,61 @@ def test_boris_gyration(orc):
         assert abs(r[i1] - r[i0]) / r[i0] < 5e-5
         assert abs((ph[i1] - ph[i0]) % (2 * np.pi)) < 0.16 or abs((ph[i1] - ph[i0]) % (2 * np.pi) - 2 * np.pi) < 0.16
     assert abs(r.mean() - u / B0) / (u / B0) < 0.02  # radius p/(qB)
+
+
+def _single(g, mom, pusher):
+    p = dict(pos=np.full((3, 1), 0.5, np.float32), mom=np.array(mom, np.float32).reshape(3, 1),
+             w=np.ones(1, np.float32), sc=np.array([0], np.int32), lcell=np.array([0], np.uint16))
+    return p, dict(charge=-1.0, mass=1.0, shape=2, pusher=PUSHERS[pusher], current=1)
+
+
+def _phase_lag(orc, pusher, steps_per_turn, turns=4):
+    """|phase of the momentum after `turns` nominal periods - turns * 2 pi| (gyration at 0.5c)."""
+    g = grid(n=(16, 16, 16), sc=(8, 8, 4), dt=0.5)
+    gamma = 1.0 / np.sqrt(1 - 0.25)
+    B0 = 2 * np.pi * gamma / (steps_per_turn * g["dt"])
+    E = np.zeros((3, 16, 16, 16), np.float32)
+    B = np.zeros_like(E)
+    B[2] = np.float32(B0)
+    p, sp = _single(g, [gamma * 0.5, 0, 0], pusher)
+    ang = [0.0]
+    for _ in range(steps_per_turn * turns):
+        orc.push(g, sp, p, E, B)
+        ang.append(np.arctan2(p["mom"][1, 0], p["mom"][0, 0]))
+    return abs(abs(np.unwrap(np.array(ang))[-1]) - 2 * np.pi * turns)
+
+
+@pytest.mark.parametrize("pusher", list(PUSHERS))
+def test_phase_lag_is_second_order(orc, pusher):
+    """PusherScaling/README.rst: with 10, 20, 40, 80 and 160 steps per turn the phase lag falls
+    by 2^x per halving of dt with x within 0.1 of 2 and a standard deviation of x below 0.05."""
+    lags = np.array([_phase_lag(orc, pusher, n) for n in (10, 20, 40, 80, 160)])
+    x = np.log2(lags[:-1] / lags[1:])
+    assert abs(x.mean() - 2.0) < 0.1, x
+    assert x.std() < 0.05, x
+
+
+def test_exb_drift_kept_by_higuera_cary_and_vay(orc):
+    """A particle at the relativistic E x B drift velocity (0.9c) feels no force: HigueraCary and
+    Vay keep its momentum to float rounding over 200 steps (the property both were built for);
+    Boris does not (its velocity average is not the drift), the reason they exist."""
+    g = grid(n=(16, 16, 16), sc=(8, 8, 4), dt=0.5)
+    vd = 0.9
+    E = np.zeros((3, 16, 16, 16), np.float32)
+    B = np.zeros_like(E)
+    E[1] = np.float32(vd)  # E x B / B^2 = vd x-hat for B = z-hat
+    B[2] = 1.0
+    dev = {}
+    for pusher in PUSHERS:
+        p, sp = _single(g, [vd / np.sqrt(1 - vd * vd), 0, 0], pusher)
+        m0 = p["mom"].copy()
+        worst = 0.0
+        for _ in range(200):
+            orc.push(g, sp, p, E, B)
+            worst = max(worst, float(np.abs(p["mom"] - m0).max() / np.abs(m0).max()))
+        dev[pusher] = worst
+    assert dev["HigueraCary"] < 1e-5 and dev["Vay"] < 1e-5, dev
+    assert dev["Boris"] > 1e-2, dev
 
 
 @pytest.mark.parametrize("shape", [1, 2, 3])
