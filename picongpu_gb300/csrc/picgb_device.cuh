@@ -1,5 +1,5 @@
 // Device-side math of the PIC hot path: assignment shapes, form-factor gather,
-// Boris push, moveParticle and the Esirkepov deposit.
+// Boris, HigueraCary and Vay pushes, moveParticle and the Esirkepov deposit.
 //
 // Operations that decide particle positions (shapes, gather, push, move) use
 // the explicit round-to-nearest intrinsics (__fmul_rn, __fadd_rn, __fmaf_rn,
@@ -359,7 +359,7 @@ namespace picgb
 
     // HigueraCary (particles/pusher/particlePusherHigueraCary.hpp:85-135): the new
     // momentum.  Kept out of line so the Boris kernels keep their register budget.
-    __device__ __noinline__ float3 higueraCary(float charge, float mass, float3 E, float3 B, float dt, float c, float c2, float3 mom)
+    static __device__ __noinline__ float3 higueraCary(float charge, float mass, float3 E, float3 B, float dt, float c, float c2, float3 mom)
     {
         float const hq = fm(0.5f, charge);
         // mom_minus = mom + 0.5 q E dt (float), then held in double
@@ -394,7 +394,7 @@ namespace picgb
     }
 
     // Vay (particles/pusher/particlePusherVay.hpp:72-103): the new momentum.
-    __device__ __noinline__ float3 vay(float charge, float mass, float3 E, float3 B, float dt, float c, float c2, float rc2, float3 mom)
+    static __device__ __noinline__ float3 vay(float charge, float mass, float3 E, float3 B, float dt, float c, float c2, float rc2, float3 mom)
     {
         float const factor = fm(fm(0.5f, charge), dt);
         float const m[3] = {mom.x, mom.y, mom.z};
