@@ -17,7 +17,7 @@ namespace picgb
         return THREADS >= 256 ? PICGB_PUSH_MIN_BLOCKS : 2 * PICGB_PUSH_MIN_BLOCKS;
     }
 
-    template<int SHAPE, int SX, int SY, int SZ, int THREADS>
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT>
     __global__ void __launch_bounds__(THREADS, batchMinBlocks<THREADS>()) kPushBatch(
         BatchSpecies const* __restrict__ table,
         uint32_t const* __restrict__ items,
@@ -44,7 +44,7 @@ namespace picgb
             for(int i = threadIdx.x; i < kWords; i += THREADS)
                 reinterpret_cast<uint32_t*>(&s_box)[i] = __ldg(src + i);
             __syncthreads();
-            pushSupercell<SHAPE, SX, SY, SZ, THREADS>(
+            pushSupercell<SHAPE, SX, SY, SZ, THREADS, ALT>(
                 s_box.sp,
                 s_box.E,
                 s_box.B,
@@ -59,7 +59,7 @@ namespace picgb
         }
     }
 
-    template<int SHAPE, int SX, int SY, int SZ, int THREADS>
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT>
     cudaError_t launchPushBatchT(
         BatchSpecies const* table,
         uint32_t const* items,
@@ -69,7 +69,7 @@ namespace picgb
         cudaStream_t stream)
     {
         using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>, THREADS>;
-        auto k = kPushBatch<SHAPE, SX, SY, SZ, THREADS>;
+        auto k = kPushBatch<SHAPE, SX, SY, SZ, THREADS, ALT>;
         size_t const smem = TG::pushSmem;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if(e != cudaSuccess)
@@ -90,39 +90,28 @@ namespace picgb
         return cudaGetLastError();
     }
 
-    template<int SHAPE, int SX, int SY, int SZ, int THREADS>
-    int pushBatchOccupancyT()
-    {
-        using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>, THREADS>;
-        auto k = kPushBatch<SHAPE, SX, SY, SZ, THREADS>;
-        if(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TG::pushSmem)) != cudaSuccess)
-            return 0;
-        int occ = 0;
-        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, THREADS, TG::pushSmem) != cudaSuccess)
-            return 0;
-        return occ;
-    }
-
-// Instantiates the batched launchers of one shape for the supercell sizes
-// 8x8x4, 4x4x4, 8x8x8 and 128 or 256 threads per supercell.
-#define PICGB_BATCH_CASES(F, SHAPE, ...)                                                                              \
+// Instantiates the batched launcher of one shape and pusher variant (ALT: HigueraCary
+// and Vay) for the supercell sizes 8x8x4, 4x4x4, 8x8x8 and 128 or 256 threads per
+// supercell.  Each (shape, variant) pair has its own translation unit, so the
+// heaviest instantiations compile in parallel.
+#define PICGB_BATCH_CASES(F, SHAPE, ALT, ...)                                                                         \
     switch(scId * 2 + (threads == 128 ? 0 : 1))                                                                       \
     {                                                                                                                 \
     case 0:                                                                                                           \
-        return F<SHAPE, 8, 8, 4, 128>(__VA_ARGS__);                                                                   \
+        return F<SHAPE, 8, 8, 4, 128, ALT>(__VA_ARGS__);                                                              \
     case 1:                                                                                                           \
-        return F<SHAPE, 8, 8, 4, 256>(__VA_ARGS__);                                                                   \
+        return F<SHAPE, 8, 8, 4, 256, ALT>(__VA_ARGS__);                                                              \
     case 2:                                                                                                           \
-        return F<SHAPE, 4, 4, 4, 128>(__VA_ARGS__);                                                                   \
+        return F<SHAPE, 4, 4, 4, 128, ALT>(__VA_ARGS__);                                                              \
     case 3:                                                                                                           \
-        return F<SHAPE, 4, 4, 4, 256>(__VA_ARGS__);                                                                   \
+        return F<SHAPE, 4, 4, 4, 256, ALT>(__VA_ARGS__);                                                              \
     case 4:                                                                                                           \
-        return F<SHAPE, 8, 8, 8, 128>(__VA_ARGS__);                                                                   \
+        return F<SHAPE, 8, 8, 8, 128, ALT>(__VA_ARGS__);                                                              \
     case 5:                                                                                                           \
-        return F<SHAPE, 8, 8, 8, 256>(__VA_ARGS__);                                                                   \
+        return F<SHAPE, 8, 8, 8, 256, ALT>(__VA_ARGS__);                                                              \
     }
 
-#define PICGB_BATCH_LAUNCHERS(SHAPE, NAME)                                                                            \
+#define PICGB_BATCH_LAUNCHERS(SHAPE, NAME, ALT)                                                                       \
     cudaError_t launchPushBatch##NAME(                                                                                \
         int scId,                                                                                                     \
         int threads,                                                                                                  \
@@ -135,14 +124,7 @@ namespace picgb
     {                                                                                                                 \
         if(threads != 128 && threads != 256)                                                                          \
             return cudaErrorInvalidValue;                                                                             \
-        PICGB_BATCH_CASES(launchPushBatchT, SHAPE, table, items, nitems, counter, status, stream)                     \
+        PICGB_BATCH_CASES(launchPushBatchT, SHAPE, ALT, table, items, nitems, counter, status, stream)                \
         return cudaErrorInvalidValue;                                                                                 \
-    }                                                                                                                 \
-    int pushBatchOccupancy##NAME(int scId, int threads)                                                               \
-    {                                                                                                                 \
-        if(threads != 128 && threads != 256)                                                                          \
-            return 0;                                                                                                 \
-        PICGB_BATCH_CASES(pushBatchOccupancyT, SHAPE)                                                                 \
-        return 0;                                                                                                     \
     }
 } // namespace picgb

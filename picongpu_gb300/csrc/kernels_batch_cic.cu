@@ -1,7 +1,7 @@
-// Batched (ensemble) push kernels instantiated for the CIC shape.
+// Batched (ensemble) push kernels instantiated for the CIC shape, Boris and Free pushers.
 #include "kernels_batch.cuh"
 
 namespace picgb
 {
-    PICGB_BATCH_LAUNCHERS(1, CIC)
+    PICGB_BATCH_LAUNCHERS(1, CIC, false)
 } // namespace picgb

@@ -1,7 +1,7 @@
-// Batched (ensemble) push kernels instantiated for the TSC shape.
+// Batched (ensemble) push kernels instantiated for the TSC shape, Boris and Free pushers.
 #include "kernels_batch.cuh"
 
 namespace picgb
 {
-    PICGB_BATCH_LAUNCHERS(2, TSC)
+    PICGB_BATCH_LAUNCHERS(2, TSC, false)
 } // namespace picgb

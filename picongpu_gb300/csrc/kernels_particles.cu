@@ -10,7 +10,9 @@
 namespace picgb
 {
 #define PICGB_DECL_SHAPE(NAME)                                                                                        \
-    cudaError_t launchPushBatch##NAME(                                                                                \
+    cudaError_t launchPushBatch##NAME(int, int, BatchSpecies const*, uint32_t const*, uint32_t, uint32_t*, unsigned*, \
+                                      cudaStream_t);                                                                  \
+    cudaError_t launchPushBatch##NAME##Alt(                                                                           \
         int,                                                                                                          \
         int,                                                                                                          \
         BatchSpecies const*,                                                                                          \
@@ -19,7 +21,6 @@ namespace picgb
         uint32_t*,                                                                                                    \
         unsigned*,                                                                                                    \
         cudaStream_t);                                                                                                \
-    int pushBatchOccupancy##NAME(int, int);                                                                           \
     cudaError_t launchPush##NAME(                                                                                     \
         int,                                                                                                          \
         SpeciesDev const&,                                                                                            \
@@ -71,6 +72,7 @@ namespace picgb
         int shape,
         int scId,
         int threads,
+        int pusher,
         BatchSpecies const* table,
         uint32_t const* items,
         uint32_t nitems,
@@ -78,30 +80,23 @@ namespace picgb
         unsigned* status,
         cudaStream_t stream)
     {
-        switch(shape)
+        bool const alt = pusher == kPusherHigueraCary || pusher == kPusherVay;
+        switch(shape * 2 + (alt ? 1 : 0))
         {
-        case 1:
-            return launchPushBatchCIC(scId, threads, table, items, nitems, counter, status, stream);
         case 2:
-            return launchPushBatchTSC(scId, threads, table, items, nitems, counter, status, stream);
+            return launchPushBatchCIC(scId, threads, table, items, nitems, counter, status, stream);
         case 3:
+            return launchPushBatchCICAlt(scId, threads, table, items, nitems, counter, status, stream);
+        case 4:
+            return launchPushBatchTSC(scId, threads, table, items, nitems, counter, status, stream);
+        case 5:
+            return launchPushBatchTSCAlt(scId, threads, table, items, nitems, counter, status, stream);
+        case 6:
             return launchPushBatchPQS(scId, threads, table, items, nitems, counter, status, stream);
+        case 7:
+            return launchPushBatchPQSAlt(scId, threads, table, items, nitems, counter, status, stream);
         }
         return cudaErrorInvalidValue;
-    }
-
-    int pushBatchOccupancy(int shape, int scId, int threads)
-    {
-        switch(shape)
-        {
-        case 1:
-            return pushBatchOccupancyCIC(scId, threads);
-        case 2:
-            return pushBatchOccupancyTSC(scId, threads);
-        case 3:
-            return pushBatchOccupancyPQS(scId, threads);
-        }
-        return 0;
     }
 
     cudaError_t launchDeposit(

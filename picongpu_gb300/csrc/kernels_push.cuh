@@ -162,8 +162,9 @@ namespace picgb
     // general footprint.  Without the split every warp would pay, through
     // divergence, the largest footprint of any of its lanes.  `smem` holds
     // TileGeom::pushSmem bytes; the block must be synchronised before a second
-    // call reuses it.
-    template<int SHAPE, int SX, int SY, int SZ, int THREADS>
+    // call reuses it.  ALT: the kernel variant for the HigueraCary and Vay pushers;
+    // the other variant serves Boris and Free, so neither carries the other's code.
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT>
     __device__ __forceinline__ void pushSupercell(
         SpeciesDev const& sp,
         float const* __restrict__ E,
@@ -242,7 +243,7 @@ namespace picgb
                     Ev[0] = gw.template gather<TG::GX, TG::GY, 1, 0, 0>(Es, lx, ly, lz);
                     Ev[1] = gw.template gather<TG::GX, TG::GY, 0, 1, 0>(Es + TG::GT, lx, ly, lz);
                     Ev[2] = gw.template gather<TG::GX, TG::GY, 0, 0, 1>(Es + 2 * TG::GT, lx, ly, lz);
-                    if(pp.pusher == kPusherBoris)
+                    if constexpr(!ALT)
                         boris(charge, mass, Ev, Bv, pp.dt, pp.c2, pp.rc2, mom, vel);
                     else
                     {
@@ -385,7 +386,7 @@ namespace picgb
     }
 
     // Fused push kernel of one box: one block per supercell.
-    template<int SHAPE, int SX, int SY, int SZ>
+    template<int SHAPE, int SX, int SY, int SZ, bool ALT>
     __global__ void __launch_bounds__(kPushThreads, PICGB_PUSH_MIN_BLOCKS) kPush(
         SpeciesDev sp,
         float const* __restrict__ E,
@@ -397,7 +398,7 @@ namespace picgb
     {
         extern __shared__ __align__(16) float smem[];
         __shared__ unsigned s_nhole;
-        pushSupercell<SHAPE, SX, SY, SZ, kPushThreads>(sp, E, B, J, g, pp, status, blockIdx.x, smem, s_nhole);
+        pushSupercell<SHAPE, SX, SY, SZ, kPushThreads, ALT>(sp, E, B, J, g, pp, status, blockIdx.x, smem, s_nhole);
     }
 
     // Deposit-only kernel over the sorted particles (the reference's separate
@@ -505,7 +506,8 @@ namespace picgb
         cudaStream_t stream)
     {
         using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>>;
-        auto k = kPush<SHAPE, SX, SY, SZ>;
+        bool const alt = pp.pusher == kPusherHigueraCary || pp.pusher == kPusherVay;
+        auto k = alt ? kPush<SHAPE, SX, SY, SZ, true> : kPush<SHAPE, SX, SY, SZ, false>;
         size_t const smem = TG::pushSmem;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if(e != cudaSuccess)

@@ -46,14 +46,13 @@ namespace picgb
         int shape,
         int scId,
         int threads,
+        int pusher, // selects the kernel variant (Boris/Free or HigueraCary/Vay)
         BatchSpecies const* table,
         uint32_t const* items,
         uint32_t nitems,
         uint32_t* counter,
         unsigned* status,
         cudaStream_t stream);
-    // Resident blocks per SM of the batched push kernel (0 if the variant does not exist).
-    int pushBatchOccupancy(int shape, int scId, int threads);
     cudaError_t launchCompactBatch(
         BatchSpecies const* boxes,
         uint32_t const* items,

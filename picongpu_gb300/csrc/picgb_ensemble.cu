@@ -229,11 +229,12 @@ namespace
         for(size_t k = 0; k < nspec; ++k)
             if(pushed[k])
             {
-                int const shape = e->boxes[0]->species[k]->cfg.shape;
+                auto const& cfg = e->boxes[0]->species[k]->cfg;
                 launch(launchPushBatch(
-                    shape,
+                    cfg.shape,
                     scId,
                     e->threads,
+                    cfg.pusher,
                     e->dSpecies + k * nbox,
                     e->dItems,
                     e->nitems,
