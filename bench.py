@@ -462,6 +462,43 @@ def run_pushers(args, local_rank):
     return out
 
 
+def run_checkpoint(args, local_rank):
+    """openPMD checkpoint write and restart read of the two-stream workload on 64^3 cells
+    (E, B and 2 x 4.2e6 particles) to a temporary directory, timed with the host clock
+    around the C-ABI calls (device copies and file IO included)."""
+    import shutil
+    import tempfile
+
+    import picongpu_gb300 as pg
+
+    wl = WORKLOADS["two_stream_64"]
+    d = tempfile.mkdtemp(prefix="picgb_ckpt_")
+    try:
+        sim = build_sim(pg, wl, local_rank)
+        with sim:
+            init_plasma(sim, wl)
+            sim.run(2)
+            sim.synchronize()
+            t0 = time.perf_counter()
+            it = sim.write_checkpoint(d)
+            t_write = time.perf_counter() - t0
+            nbytes = sum(os.path.getsize(os.path.join(it, f)) for f in os.listdir(it))
+            npart = sim.particle_count("e") + sim.particle_count("i")
+        sim2 = build_sim(pg, wl, local_rank)
+        with sim2:
+            t0 = time.perf_counter()
+            sim2.read_checkpoint(d, 2)
+            sim2.synchronize()
+            t_read = time.perf_counter() - t0
+            same = sim2.particle_count("e") + sim2.particle_count("i") == npart
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {"workload": "two-stream 64^3 cells, 2 species x 16 ppc (E, B, positions, cell offsets, momenta, "
+                        "weightings)", "bytes": nbytes, "particles": npart, "write_s": t_write, "read_s": t_read,
+            "write_GBps": nbytes / t_write / 1e9, "read_GBps": nbytes / t_read / 1e9, "restored_all": bool(same),
+            "timing": "host clock around picgb_checkpoint_write / picgb_checkpoint_read"}
+
+
 # ---------------------------------------------------------------------- differentiable run
 def adjoint_case(A, n, ppc, precision, checkpoint_every):
     dens = (0.1 / DT) ** 2
@@ -568,6 +605,7 @@ def main():
     ap.add_argument("--no-laser", action="store_true")
     ap.add_argument("--laser-steps", type=int, default=40)
     ap.add_argument("--no-pushers", action="store_true")
+    ap.add_argument("--no-checkpoint", action="store_true")
     ap.add_argument("--pusher-steps", type=int, default=20)
     ap.add_argument("--adjoint-steps", type=int, default=300)
     ap.add_argument("--adjoint-fd-steps", type=int, default=20)
@@ -622,6 +660,9 @@ def main():
     pushers = None
     if not args.no_pushers:
         pushers = run_pushers(args, local_rank)
+    checkpoint = None
+    if not args.no_checkpoint:
+        checkpoint = run_checkpoint(args, local_rank)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         val, cores, sample = cpu_sample_rate(wl, 10, 1, budget_s=20.0)
@@ -631,7 +672,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded device init)", "config": config,
             "particles": r["npart"], "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"],
             "clocks": r["clocks"], "gpu_launches": r["launches"], "batched": batched, "adjoint": adjoint,
-            "laser_wake": laser, "pushers": pushers}
+            "laser_wake": laser, "pushers": pushers, "checkpoint": checkpoint}
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch

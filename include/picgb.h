@@ -46,7 +46,8 @@ extern "C"
         PICGB_ERR_DUPLICATE = 5, /* id already registered (DataConnector::share throws) */
         PICGB_ERR_TIMEOUT = 6, /* a bounded device wait gave up */
         PICGB_ERR_UNSUPPORTED = 7, /* policy combination without a kernel */
-        PICGB_ERR_LOST = 8 /* particles were dropped: overflow beyond the spill buffer */
+        PICGB_ERR_LOST = 8, /* particles were dropped: overflow beyond the spill buffer */
+        PICGB_ERR_IO = 9 /* a checkpoint file could not be written or read, or its index is malformed */
     };
 
     /* ------------------------------------------------------------ policies
@@ -419,6 +420,66 @@ extern "C"
     /* Sum over the species' particles of (gamma - 1) m w c^2, in FP64 (KinEnergy.hpp:43-66
      * without the low-energy branch); synchronises the stream. */
     int picgb_diff_kinetic_energy(picgb_diff* d, const picgb_diff_state* state, int32_t species, double* out, void* stream);
+
+    /* ------------------------------------------------------------ openPMD checkpoints
+     * The reference's Checkpoint and openPMD plugins (plugins/Checkpoint.x.cpp,
+     * plugins/openPMD/openPMDWriter.hpp) write E, B and every species in the openPMD 1.1.0
+     * layout with the ED-PIC extension.  One iteration here is the directory
+     * <dir>/simData_<step>/ holding the series index simData_<step>.json (the openPMD tree in
+     * the attribute/dataset form of openPMD-api's JSON backend: small datasets inline under
+     * "data", large ones as raw little-endian C-order files named by "external") and those
+     * files.  Meshes: E, B (dataOrder C, axisLabels z,y,x, Yee staggering in "position").
+     * Particles: position (in-cell, unitSI = cell edge), positionOffset (int32 cell index),
+     * momentum (macro-weighted), weighting, id (when kept), constant charge and mass records,
+     * one particle patch.  Values are in the simulation's own unit system (unitSI 1). */
+    typedef struct picgb_openpmd_species
+    {
+        const char* name; /* DataConnector id; letters, digits, '_' and '-' only */
+        float charge; /* per real particle */
+        float mass; /* per real particle */
+        int32_t pusher; /* enum picgb_pusher, recorded as the ED-PIC particlePush attribute */
+        int32_t shape; /* enum picgb_shape, recorded as particleShape */
+        int32_t current; /* enum picgb_current, recorded as currentDeposition */
+        picgb_particles particles; /* host arrays in the exchange format (sc, lcell for grid->supercell) */
+    } picgb_openpmd_species;
+
+    /* Host-side writer (no device work): the iteration directory from host arrays.  E and B
+     * are 3 host arrays of nx*ny*nz floats each, x fastest. */
+    int picgb_openpmd_write(
+        const char* dir,
+        uint32_t step,
+        const picgb_grid_config* grid,
+        const float* const* E,
+        const float* const* B,
+        int32_t nspecies,
+        const picgb_openpmd_species* species);
+    /* Particle count of species `name` in iteration `step` (PICGB_ERR_NOT_FOUND if absent). */
+    int picgb_openpmd_species_count(const char* dir, uint32_t step, const char* name, uint64_t* n);
+    /* Reads species `name` into host arrays of at least `host->n` particles; sc and lcell are
+     * computed for grid->supercell, so a restart may change the supercell size.  The id array
+     * is filled when host->id is not NULL and the file holds ids (else PICGB_ERR_NOT_FOUND). */
+    int picgb_openpmd_read_species(
+        const char* dir,
+        uint32_t step,
+        const char* name,
+        const picgb_grid_config* grid,
+        picgb_particles* host);
+    /* Reads mesh "E" or "B" (3 host arrays of nx*ny*nz floats). */
+    int picgb_openpmd_read_mesh(
+        const char* dir,
+        uint32_t step,
+        const char* name,
+        const picgb_grid_config* grid,
+        float* const* host);
+
+    /* Checkpoint of a simulation (Checkpoint::notify): E, B and every species with a
+     * particle array, as iteration `step` under `dir`.  Iteration s is the state after s
+     * steps, at time s * dt. */
+    int picgb_checkpoint_write(picgb_sim* sim, const char* dir, uint32_t step);
+    /* Restart (Simulation::restart -> checkpoint read): E and B, and every species of the
+     * simulation by name; J is zeroed.  The grid must match the file's; the caller's next
+     * step index is `step`. */
+    int picgb_checkpoint_read(picgb_sim* sim, const char* dir, uint32_t step);
 
 #ifdef __cplusplus
 }

@@ -16,9 +16,9 @@ c_int, c_uint32, c_uint64, c_float, c_double, c_void_p, c_char_p = (
 P = ctypes.POINTER
 
 # status codes (enum picgb_status)
-OK, ERR_INVALID, ERR_CUDA, ERR_OVERFLOW, ERR_NOT_FOUND, ERR_DUPLICATE, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_LOST = range(9)
+OK, ERR_INVALID, ERR_CUDA, ERR_OVERFLOW, ERR_NOT_FOUND, ERR_DUPLICATE, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_LOST, ERR_IO = range(10)
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "OVERFLOW", 4: "NOT_FOUND", 5: "DUPLICATE", 6: "TIMEOUT",
-                7: "UNSUPPORTED", 8: "LOST"}
+                7: "UNSUPPORTED", 8: "LOST", 9: "IO"}
 
 PUSHER_BORIS, PUSHER_FREE, PUSHER_NONE, PUSHER_HIGUERA_CARY, PUSHER_VAY = 0, 1, 2, 3, 4
 SHAPE_NGP, SHAPE_CIC, SHAPE_TSC, SHAPE_PQS, SHAPE_PCS = range(5)
@@ -43,6 +43,11 @@ class SpeciesConfig(ctypes.Structure):
 class Particles(ctypes.Structure):
     _fields_ = [("n", c_uint64), ("pos", c_void_p * 3), ("mom", c_void_p * 3), ("w", c_void_p), ("sc", c_void_p),
                 ("lcell", c_void_p), ("id", c_void_p)]
+
+
+class OpenPMDSpecies(ctypes.Structure):
+    _fields_ = [("name", c_char_p), ("charge", c_float), ("mass", c_float), ("pusher", c_int), ("shape", c_int),
+                ("current", c_int), ("particles", Particles)]
 
 
 class BufferDesc(ctypes.Structure):
@@ -138,6 +143,13 @@ SIGNATURES = [
     ("picgb_ensemble_autotune", c_int,
      [P(EnsembleConfig), c_int, P(SpeciesConfig), P(PlasmaInit), c_uint32, c_uint32, P(c_int), P(c_int),
       P(c_double)]),
+    ("picgb_openpmd_write", c_int, [c_char_p, c_uint32, P(GridConfig), P(c_void_p), P(c_void_p), c_int,
+                                    P(OpenPMDSpecies)]),
+    ("picgb_openpmd_species_count", c_int, [c_char_p, c_uint32, c_char_p, P(c_uint64)]),
+    ("picgb_openpmd_read_species", c_int, [c_char_p, c_uint32, c_char_p, P(GridConfig), P(Particles)]),
+    ("picgb_openpmd_read_mesh", c_int, [c_char_p, c_uint32, c_char_p, P(GridConfig), P(c_void_p)]),
+    ("picgb_checkpoint_write", c_int, [c_void_p, c_char_p, c_uint32]),
+    ("picgb_checkpoint_read", c_int, [c_void_p, c_char_p, c_uint32]),
     ("picgb_diff_create", c_int, [P(DiffConfig), c_int, P(DiffSpecies), P(c_void_p)]),
     ("picgb_diff_destroy", c_int, [c_void_p]),
     ("picgb_diff_forward", c_int, [c_void_p, P(DiffState), c_uint32, c_void_p]),

@@ -11,6 +11,7 @@ CUDA library libpicgb.so through its C-ABI.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -41,6 +42,12 @@ class Grid:
     solver: str = "Yee"
     fuse_deposit: bool = True
     device: int = 0
+
+    def config(self) -> L.GridConfig:
+        """The C-ABI picgb_grid_config of this grid."""
+        return L.GridConfig(self.nx, self.ny, self.nz, SUPERCELLS[tuple(self.supercell)], self.dx, self.dy, self.dz,
+                            self.dt, self.c, self.eps0, SOLVERS[self.solver], int(bool(self.fuse_deposit)),
+                            self.device)
 
     @property
     def sx(self):
@@ -112,9 +119,7 @@ class DataConnector:
 class Simulation:
     def __init__(self, grid: Grid):
         self.grid = grid
-        cfg = L.GridConfig(grid.nx, grid.ny, grid.nz, SUPERCELLS[tuple(grid.supercell)], grid.dx, grid.dy, grid.dz,
-                           grid.dt, grid.c, grid.eps0, SOLVERS[grid.solver], int(bool(grid.fuse_deposit)),
-                           grid.device)
+        cfg = grid.config()
         h = ctypes.c_void_p()
         L.call("picgb_create", ctypes.byref(cfg), ctypes.byref(h))
         self._init_handle(h, grid, owned=True)
@@ -245,6 +250,20 @@ class Simulation:
         ptrs = (ctypes.c_void_p * a.shape[0])(*[a[c].ctypes.data for c in range(a.shape[0])])
         L.call("picgb_field_get", self.handle, name.encode(), ptrs)
         return a
+
+    # ------------------------------------------------------------ checkpoints
+    def write_checkpoint(self, directory: str, step: int | None = None) -> str:
+        """openPMD checkpoint of E, B and every species as iteration ``step`` (default: the
+        current step, i.e. the state after that many steps); returns the iteration directory."""
+        step = self.current_step if step is None else int(step)
+        L.call("picgb_checkpoint_write", self.handle, os.fsencode(directory), step)
+        return os.path.join(directory, f"simData_{step}")
+
+    def read_checkpoint(self, directory: str, step: int) -> None:
+        """Restart from iteration ``step``: E, B and the species of this simulation (by name);
+        J is zeroed and the next step index becomes ``step``."""
+        L.call("picgb_checkpoint_read", self.handle, os.fsencode(directory), int(step))
+        self.current_step = int(step)
 
     # ------------------------------------------------------------ stepping
     def set_incident_field(self, a0: float, wavelength: float, waist: float, duration_fwhm: float, t_center: float,
