@@ -72,7 +72,8 @@ extern "C"
     enum picgb_current
     {
         PICGB_CURRENT_NONE = 0, /* species without the current<> flag */
-        PICGB_CURRENT_ESIRKEPOV = 1 /* fields/currentDeposition/Esirkepov/Esirkepov.hpp */
+        PICGB_CURRENT_ESIRKEPOV = 1, /* fields/currentDeposition/Esirkepov/Esirkepov.hpp */
+        PICGB_CURRENT_EMZ = 2 /* fields/currentDeposition/EmZ/EmZ.hpp (Esirkepov meets ZigZag); single-box path */
     };
     enum picgb_field_solver
     {

@@ -96,6 +96,7 @@ def lib() -> ctypes.CDLL:
         L.orc_push.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), P(OrcField), P(OrcField)]
         L.orc_deposit.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), P(OrcField), ctypes.c_int]
         L.orc_esirkepov_one.argtypes = [P(OrcGrid), ctypes.c_int, vp, vp, vp, ctypes.c_float, P(OrcField)]
+        L.orc_emz_one.argtypes = [P(OrcGrid), ctypes.c_int, vp, vp, vp, ctypes.c_float, P(OrcField)]
         L.orc_step.argtypes = [
             P(OrcGrid),
             ctypes.c_int,
@@ -189,6 +190,13 @@ def esirkepov_one(g, shape, cell, pos, vel, charge, J):
     pos = np.ascontiguousarray(pos, dtype=np.float32)
     vel = np.ascontiguousarray(vel, dtype=np.float32)
     lib().orc_esirkepov_one(grid(g), int(shape), _ptr(cell), _ptr(pos), _ptr(vel), float(charge), field(J))
+
+
+def emz_one(g, shape, cell, pos, vel, charge, J):
+    cell = np.ascontiguousarray(cell, dtype=np.int32)
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    vel = np.ascontiguousarray(vel, dtype=np.float32)
+    lib().orc_emz_one(grid(g), int(shape), _ptr(cell), _ptr(pos), _ptr(vel), float(charge), field(J))
 
 
 def step(g, species_list, plist, E, B, J, threads: int = 1):

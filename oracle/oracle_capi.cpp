@@ -172,6 +172,21 @@ extern "C"
         orc::esirkepov(G, shape, cell, pos, vel, charge, acc);
     }
 
+    void orc_emz_one(
+        orc_grid const* g,
+        int shape,
+        int const* cell,
+        float const* pos,
+        float const* vel,
+        float charge,
+        orc_field* J)
+    {
+        orc::Grid G = toGrid(g);
+        auto Jf = toF(J);
+        orc::JAccess<float> acc{&G, &Jf};
+        orc::emz(G, shape, cell, pos, vel, charge, acc);
+    }
+
     void orc_step(
         orc_grid const* g,
         int nspecies,

@@ -105,8 +105,9 @@ namespace orc
         float mass; // mass of one real particle (macro mass = mass * w)
         int shape; // Shape
         int pusher; // Pusher
-        int current; // 1 = Esirkepov deposit, 0 = no current
+        int current; // 1 = Esirkepov deposit, 2 = EmZ, 0 = no current
     };
+    constexpr int EMZ_CURRENT = 2;
 
     // ---------------------------------------------------------------- shapes
     // particles/shapes/{NGP,CIC,TSC,PQS,PCS}.hpp.  support = order + 1.
@@ -864,6 +865,136 @@ namespace orc
         }
     }
 
+    // ---------------------------------------------------------------- EmZ
+    // One rotated 1D current of an EmZ virtual particle (EmZ/DepositCurrent.hpp:76-126):
+    // on-support shapes, Jit for the outer loop and Cached for the middle and inner loops
+    // (Strategy.def:44-61), loops [begin, begin + supp) and [begin, begin + supp - 1).
+    template<typename T, typename Acc>
+    void emzCurrent1D(
+        int shape,
+        T const p0[3],
+        T const p1[3],
+        int const base[3],
+        int const perm[3],
+        int comp,
+        T currentSurfaceDensity,
+        Acc& acc)
+    {
+        if(p0[2] == p1[2])
+            return;
+        int const supp = support(shape);
+        int const begin = ShapeFn<T>::osBegin(shape);
+        int const end = begin + supp;
+        T sj0[6] = {}, sj1[6] = {}, sk0[6] = {}, sk1[6] = {};
+        ShapeFn<T>::baseArray(shape, p0[1], sj0);
+        ShapeFn<T>::baseArray(shape, p1[1], sj1);
+        ShapeFn<T>::baseArray(shape, p0[2], sk0);
+        ShapeFn<T>::baseArray(shape, p1[2], sk1);
+        for(int i = begin; i < end; ++i)
+        {
+            T const s0i = ShapeFn<T>::os(shape, T(i) - p0[0]);
+            T const dsi = ShapeFn<T>::os(shape, T(i) - p1[0]) - s0i;
+            for(int j = begin; j < end; ++j)
+            {
+                T const s0j = sj0[j - begin];
+                T const dsj = sj1[j - begin] - s0j;
+                T tmp = -currentSurfaceDensity
+                    * (s0i * s0j + T(0.5) * (dsi * s0j + s0i * dsj) + (T(1.0) / T(3.0)) * dsj * dsi);
+                T accumulated_J = T(0.0);
+                for(int k = begin; k < end - 1; ++k)
+                {
+                    T const W = (sk1[k - begin] - sk0[k - begin]) * tmp;
+                    accumulated_J += W;
+                    int r[3] = {i, j, k};
+                    int node[3];
+                    for(int a = 0; a < 3; ++a)
+                        node[perm[a]] = base[perm[a]] + r[a];
+                    acc.add(comp, node[0], node[1], node[2], accumulated_J);
+                }
+            }
+        }
+    }
+
+    // One EmZ virtual particle from p0 to p1 in the frame of cell `base`
+    // (EmZ/DepositCurrent.hpp:38-63): the three rotated calls.
+    template<typename T, typename Acc>
+    void emzVirtual(Grid const& g, int shape, T const p0[3], T const p1[3], int const base[3], T chargeDensity, Acc& acc)
+    {
+        T const cs[3] = {T(g.dx), T(g.dy), T(g.dz)};
+        T const dt = T(g.dt);
+        {
+            T const q0[3] = {p0[1], p0[2], p0[0]}, q1[3] = {p1[1], p1[2], p1[0]};
+            int const perm[3] = {1, 2, 0};
+            emzCurrent1D(shape, q0, q1, base, perm, 0, cs[0] * chargeDensity / dt, acc);
+        }
+        {
+            T const q0[3] = {p0[2], p0[0], p0[1]}, q1[3] = {p1[2], p1[0], p1[1]};
+            int const perm[3] = {2, 0, 1};
+            emzCurrent1D(shape, q0, q1, base, perm, 1, cs[1] * chargeDensity / dt, acc);
+        }
+        {
+            int const perm[3] = {0, 1, 2};
+            emzCurrent1D(shape, p0, p1, base, perm, 2, cs[2] * chargeDensity / dt, acc);
+        }
+    }
+
+    // EmZ::operator() (fields/currentDeposition/EmZ/EmZ.hpp:72-120): the trajectory is
+    // split at the relay point (relayPoint.hpp:48-64) into at most two virtual particles,
+    // each on support.  Arguments as for esirkepov().
+    template<typename T, typename Acc>
+    void emz(Grid const& g, int shape, int const cell[3], T const pos[3], T const vel[3], T charge, Acc& acc)
+    {
+        int const supp = support(shape);
+        bool const isEven = (supp % 2) == 0;
+        T const cs[3] = {T(g.dx), T(g.dy), T(g.dz)};
+        T posStart[3], relay[3];
+        int shiftStart[3], shiftEnd[3];
+        bool two = false;
+        for(int d = 0; d < 3; ++d)
+        {
+            T const deltaPos = (vel[d] * T(g.dt)) / cs[d];
+            posStart[d] = pos[d] - deltaPos;
+            relayPoint(isEven, shiftStart[d], shiftEnd[d], posStart[d], pos[d]);
+            if(shiftStart[d] == shiftEnd[d])
+                relay[d] = pos[d];
+            else if(isEven)
+                relay[d] = T(std::max(shiftStart[d], shiftEnd[d]));
+            else
+                relay[d] = T(shiftStart[d] + shiftEnd[d]) / T(2.0);
+            two |= shiftStart[d] != shiftEnd[d];
+        }
+        T const chargeDensity = charge / (cs[0] * cs[1] * cs[2]);
+        T a0[3], a1[3];
+        int base[3];
+        for(int d = 0; d < 3; ++d)
+        {
+            a0[d] = posStart[d] - T(shiftStart[d]);
+            a1[d] = relay[d] - T(shiftStart[d]);
+            base[d] = cell[d] + shiftStart[d];
+        }
+        emzVirtual(g, shape, a0, a1, base, chargeDensity, acc);
+        if(two)
+        {
+            for(int d = 0; d < 3; ++d)
+            {
+                a1[d] = pos[d] - T(shiftEnd[d]);
+                a0[d] = relay[d] - T(shiftEnd[d]);
+                base[d] = cell[d] + shiftEnd[d];
+            }
+            emzVirtual(g, shape, a0, a1, base, chargeDensity, acc);
+        }
+    }
+
+    // The species' current solver (param/species.param: UsedParticleCurrentSolver).
+    template<typename T, typename Acc>
+    void depositOne(Grid const& g, SpeciesParam const& sp, int const cell[3], T const pos[3], T const vel[3], T charge, Acc& acc)
+    {
+        if(sp.current == EMZ_CURRENT)
+            emz(g, sp.shape, cell, pos, vel, charge, acc);
+        else
+            esirkepov(g, sp.shape, cell, pos, vel, charge, acc);
+    }
+
     // Deposit all particles of one species into J (FieldJ.kernel:52-142; the guard
     // add of CurrentInterpolationAndAdditionToEMF.hpp:110 is the periodic wrap here).
     // Single-threaded in particle order so that the result is reproducible.
@@ -881,7 +1012,7 @@ namespace orc
             T const charge = T(sp.charge) * w;
             T vel[3];
             velocityOf(mom, T(sp.mass) * w, T(g.c), vel);
-            esirkepov(g, sp.shape, cell, pos, vel, charge, acc);
+            depositOne(g, sp, cell, pos, vel, charge, acc);
         }
     }
 
@@ -918,7 +1049,7 @@ namespace orc
                 T const w = P.w[k];
                 T vel[3];
                 velocityOf(mom, T(sp.mass) * w, T(g.c), vel);
-                esirkepov(g, sp.shape, cell, pos, vel, T(sp.charge) * w, acc);
+                depositOne(g, sp, cell, pos, vel, T(sp.charge) * w, acc);
             }
         }
 #pragma omp parallel for schedule(static)

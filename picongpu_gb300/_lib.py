@@ -22,7 +22,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "OVERFLOW", 4: "NOT_FOUND",
 
 PUSHER_BORIS, PUSHER_FREE, PUSHER_NONE, PUSHER_HIGUERA_CARY, PUSHER_VAY = 0, 1, 2, 3, 4
 SHAPE_NGP, SHAPE_CIC, SHAPE_TSC, SHAPE_PQS, SHAPE_PCS = range(5)
-CURRENT_NONE, CURRENT_ESIRKEPOV = 0, 1
+CURRENT_NONE, CURRENT_ESIRKEPOV, CURRENT_EMZ = 0, 1, 2
 SOLVER_YEE = 0
 SUPERCELL_8x8x4, SUPERCELL_4x4x4, SUPERCELL_8x8x8 = 0, 1, 2
 SUPERCELL_SIZES = {0: (8, 8, 4), 1: (4, 4, 4), 2: (8, 8, 8)}

@@ -44,7 +44,7 @@ namespace picgb
             for(int i = threadIdx.x; i < kWords; i += THREADS)
                 reinterpret_cast<uint32_t*>(&s_box)[i] = __ldg(src + i);
             __syncthreads();
-            pushSupercell<SHAPE, SX, SY, SZ, THREADS, ALT>(
+            pushSupercell<SHAPE, SX, SY, SZ, THREADS, ALT, false>(
                 s_box.sp,
                 s_box.E,
                 s_box.B,

@@ -31,6 +31,16 @@ namespace picgb
         PushParams const&,                                                                                            \
         unsigned*,                                                                                                    \
         cudaStream_t);                                                                                                \
+    cudaError_t launchPush##NAME##Alt(                                                                                \
+        int,                                                                                                          \
+        SpeciesDev const&,                                                                                            \
+        float const*,                                                                                                 \
+        float const*,                                                                                                 \
+        float*,                                                                                                       \
+        GridParams const&,                                                                                            \
+        PushParams const&,                                                                                            \
+        unsigned*,                                                                                                    \
+        cudaStream_t);                                                                                                \
     cudaError_t launchDeposit##NAME(                                                                                  \
         int,                                                                                                          \
         SpeciesDev const&,                                                                                            \
@@ -56,14 +66,21 @@ namespace picgb
         unsigned* status,
         cudaStream_t stream)
     {
-        switch(shape)
+        bool const alt = pp.pusher == kPusherHigueraCary || pp.pusher == kPusherVay;
+        switch(shape * 2 + (alt ? 1 : 0))
         {
-        case 1:
-            return launchPushCIC(scId, sp, E, B, J, g, pp, status, stream);
         case 2:
-            return launchPushTSC(scId, sp, E, B, J, g, pp, status, stream);
+            return launchPushCIC(scId, sp, E, B, J, g, pp, status, stream);
         case 3:
+            return launchPushCICAlt(scId, sp, E, B, J, g, pp, status, stream);
+        case 4:
+            return launchPushTSC(scId, sp, E, B, J, g, pp, status, stream);
+        case 5:
+            return launchPushTSCAlt(scId, sp, E, B, J, g, pp, status, stream);
+        case 6:
             return launchPushPQS(scId, sp, E, B, J, g, pp, status, stream);
+        case 7:
+            return launchPushPQSAlt(scId, sp, E, B, J, g, pp, status, stream);
         }
         return cudaErrorInvalidValue;
     }

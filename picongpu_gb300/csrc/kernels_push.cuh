@@ -164,7 +164,9 @@ namespace picgb
     // TileGeom::pushSmem bytes; the block must be synchronised before a second
     // call reuses it.  ALT: the kernel variant for the HigueraCary and Vay pushers;
     // the other variant serves Boris and Free, so neither carries the other's code.
-    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT>
+    // EMZ: the EmZ deposit (each particle's first virtual particle at once, the second,
+    // for the particles that change cell, through the warp's queue) instead of Esirkepov.
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT, bool EMZ>
     __device__ __forceinline__ void pushSupercell(
         SpeciesDev const& sp,
         float const* __restrict__ E,
@@ -219,7 +221,9 @@ namespace picgb
             uint32_t const k = c0 + threadIdx.x;
             int kind = -1; // 0: stays in its assignment cell, 1: crosses a cell boundary
             float p0[3], p1[3], charge = 0.0f;
-            int stat[3], org = 0;
+            int stat[3] = {0, 0, 0}, org = 0;
+            float b0[3], b1[3]; // EmZ: the second virtual particle
+            int orgB = 0;
             if(k < n)
             {
                 size_t const slot = base + k;
@@ -266,7 +270,23 @@ namespace picgb
                 int nlc = lc;
                 int mv[3], dir[3];
                 bool const leave = moveParticle<SC>(pos, nlc, mv, dir);
-                if(pp.deposit)
+                if constexpr(EMZ)
+                {
+                    int sS[3], sE[3];
+                    bool two;
+                    if(pp.deposit && !ES::prepareEmZ(pos, vel, g, p0, p1, sS, b0, b1, sE, two))
+                        atomicOr(status, ST_BAD_CELL);
+                    else if(pp.deposit)
+                    {
+                        // tile indices of the two virtual particles' cells
+                        org = (lx + mv[0] + sS[0] + SH::jLo)
+                            + TG::JX * ((ly + mv[1] + sS[1] + SH::jLo) + TG::JY * (lz + mv[2] + sS[2] + SH::jLo));
+                        orgB = (lx + mv[0] + sE[0] + SH::jLo)
+                            + TG::JX * ((ly + mv[1] + sE[1] + SH::jLo) + TG::JY * (lz + mv[2] + sE[2] + SH::jLo));
+                        kind = two ? 1 : 0;
+                    }
+                }
+                else if(pp.deposit)
                 {
                     int gs[3];
                     if(!ES::prepare(pos, vel, g, p0, p1, gs, stat))
@@ -339,8 +359,14 @@ namespace picgb
             }
             if(!pp.deposit)
                 continue;
-            // particles that stay in their cell: deposit now with the short footprint
-            if(kind == 0)
+            // particles that stay in their cell: deposit now with the short footprint (EmZ:
+            // every particle's first virtual particle)
+            if constexpr(EMZ)
+            {
+                if(kind >= 0)
+                    ES::runEmZ(Tile{Js, org, pp.jf}, p0, p1, charge, g);
+            }
+            else if(kind == 0)
                 ES::template run<false>(Tile{Js, org, pp.jf}, p0, p1, stat, charge, g, pp.invVdt);
             // the others: into the warp's queue, drained 32 at a time
             unsigned const crossing = __ballot_sync(0xffffffffu, kind == 1);
@@ -354,7 +380,12 @@ namespace picgb
                 }
             }
             if(kind == 1)
-                queue.put(queued + __popc(crossing & laneMaskLt()), p0, p1, charge, org, stat);
+            {
+                if constexpr(EMZ)
+                    queue.put(queued + __popc(crossing & laneMaskLt()), b0, b1, charge, orgB, stat);
+                else
+                    queue.put(queued + __popc(crossing & laneMaskLt()), p0, p1, charge, org, stat);
+            }
             queued += __popc(crossing);
             __syncwarp();
             if(queued >= 32)
@@ -362,7 +393,10 @@ namespace picgb
                 float q0[3], q1[3], qc;
                 int qo, qs[3];
                 queue.get(lane, q0, q1, qc, qo, qs);
-                ES::template run<true>(Tile{Js, qo, pp.jf}, q0, q1, qs, qc, g, pp.invVdt);
+                if constexpr(EMZ)
+                    ES::runEmZ(Tile{Js, qo, pp.jf}, q0, q1, qc, g);
+                else
+                    ES::template run<true>(Tile{Js, qo, pp.jf}, q0, q1, qs, qc, g, pp.invVdt);
                 __syncwarp();
                 if(lane < queued - 32)
                     queue.move(32 + lane, lane);
@@ -376,7 +410,10 @@ namespace picgb
             float q0[3], q1[3], qc;
             int qo, qs[3];
             queue.get(lane, q0, q1, qc, qo, qs);
-            ES::template run<true>(Tile{Js, qo, pp.jf}, q0, q1, qs, qc, g, pp.invVdt);
+            if constexpr(EMZ)
+                ES::runEmZ(Tile{Js, qo, pp.jf}, q0, q1, qc, g);
+            else
+                ES::template run<true>(Tile{Js, qo, pp.jf}, q0, q1, qs, qc, g, pp.invVdt);
         }
         __syncthreads(); // every hole is recorded and every deposit done
         if(threadIdx.x == 0)
@@ -386,7 +423,7 @@ namespace picgb
     }
 
     // Fused push kernel of one box: one block per supercell.
-    template<int SHAPE, int SX, int SY, int SZ, bool ALT>
+    template<int SHAPE, int SX, int SY, int SZ, bool ALT, bool EMZ>
     __global__ void __launch_bounds__(kPushThreads, PICGB_PUSH_MIN_BLOCKS) kPush(
         SpeciesDev sp,
         float const* __restrict__ E,
@@ -398,12 +435,12 @@ namespace picgb
     {
         extern __shared__ __align__(16) float smem[];
         __shared__ unsigned s_nhole;
-        pushSupercell<SHAPE, SX, SY, SZ, kPushThreads, ALT>(sp, E, B, J, g, pp, status, blockIdx.x, smem, s_nhole);
+        pushSupercell<SHAPE, SX, SY, SZ, kPushThreads, ALT, EMZ>(sp, E, B, J, g, pp, status, blockIdx.x, smem, s_nhole);
     }
 
     // Deposit-only kernel over the sorted particles (the reference's separate
     // CurrentDeposition stage, simulation/stage/CurrentDeposition.x.cpp:105).
-    template<int SHAPE, int SX, int SY, int SZ>
+    template<int SHAPE, int SX, int SY, int SZ, bool EMZ>
     __global__ void __launch_bounds__(kPushThreads)
         kDeposit(SpeciesDev sp, float* __restrict__ J, GridParams g, PushParams pp, unsigned* __restrict__ status)
     {
@@ -435,6 +472,40 @@ namespace picgb
             velocity(mom, fm(pp.mass, w), pp.rc2, vel);
             float p0[3], p1[3];
             int gs[3], stat[3];
+            if constexpr(EMZ)
+            {
+                float b0[3], b1[3];
+                int sE[3];
+                bool two;
+                if(!Esirkepov<SH>::prepareEmZ(pos, vel, g, p0, p1, gs, b0, b1, sE, two))
+                {
+                    atomicOr(status, ST_BAD_CELL);
+                    continue;
+                }
+                float const q = fm(pp.charge, w);
+                Esirkepov<SH>::runEmZ(
+                    TileJ<TG::JX, TG::JY, TG::JT>{
+                        Js,
+                        (cellRel[0] + gs[0] + SH::jLo)
+                            + TG::JX * ((cellRel[1] + gs[1] + SH::jLo) + TG::JY * (cellRel[2] + gs[2] + SH::jLo)),
+                        pp.jf},
+                    p0,
+                    p1,
+                    q,
+                    g);
+                if(two)
+                    Esirkepov<SH>::runEmZ(
+                        TileJ<TG::JX, TG::JY, TG::JT>{
+                            Js,
+                            (cellRel[0] + sE[0] + SH::jLo)
+                                + TG::JX * ((cellRel[1] + sE[1] + SH::jLo) + TG::JY * (cellRel[2] + sE[2] + SH::jLo)),
+                            pp.jf},
+                        b0,
+                        b1,
+                        q,
+                        g);
+                continue;
+            }
             if(!Esirkepov<SH>::prepare(pos, vel, g, p0, p1, gs, stat))
             {
                 atomicOr(status, ST_BAD_CELL);
@@ -494,7 +565,7 @@ namespace picgb
         }
     }
 
-    template<int SHAPE, int SX, int SY, int SZ>
+    template<int SHAPE, int SX, int SY, int SZ, bool ALT>
     cudaError_t launchPushT(
         SpeciesDev const& sp,
         float const* E,
@@ -506,8 +577,7 @@ namespace picgb
         cudaStream_t stream)
     {
         using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>>;
-        bool const alt = pp.pusher == kPusherHigueraCary || pp.pusher == kPusherVay;
-        auto k = alt ? kPush<SHAPE, SX, SY, SZ, true> : kPush<SHAPE, SX, SY, SZ, false>;
+        auto k = pp.current == kCurrentEmZ ? kPush<SHAPE, SX, SY, SZ, ALT, true> : kPush<SHAPE, SX, SY, SZ, ALT, false>;
         size_t const smem = TG::pushSmem;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if(e != cudaSuccess)
@@ -527,7 +597,7 @@ namespace picgb
         cudaStream_t stream)
     {
         using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>>;
-        auto k = kDeposit<SHAPE, SX, SY, SZ>;
+        auto k = pp.current == kCurrentEmZ ? kDeposit<SHAPE, SX, SY, SZ, true> : kDeposit<SHAPE, SX, SY, SZ, false>;
         size_t const smem = TG::depositSmem;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if(e != cudaSuccess)
@@ -551,8 +621,10 @@ namespace picgb
         return cudaGetLastError();
     }
 
-// Instantiates the three launchers of one shape for the supported supercell sizes.
-#define PICGB_SHAPE_LAUNCHERS(SHAPE, NAME)                                                                            \
+// Instantiates the push launcher of one shape and pusher variant (ALT: HigueraCary and
+// Vay) for the supported supercell sizes; each (shape, variant) pair has its own
+// translation unit, so the heaviest instantiations compile in parallel.
+#define PICGB_PUSH_LAUNCHER(SHAPE, NAME, ALT)                                                                         \
     cudaError_t launchPush##NAME(                                                                                     \
         int scId,                                                                                                     \
         SpeciesDev const& sp,                                                                                         \
@@ -567,14 +639,18 @@ namespace picgb
         switch(scId)                                                                                                  \
         {                                                                                                             \
         case 0:                                                                                                       \
-            return launchPushT<SHAPE, 8, 8, 4>(sp, E, B, J, g, pp, status, stream);                                   \
+            return launchPushT<SHAPE, 8, 8, 4, ALT>(sp, E, B, J, g, pp, status, stream);                              \
         case 1:                                                                                                       \
-            return launchPushT<SHAPE, 4, 4, 4>(sp, E, B, J, g, pp, status, stream);                                   \
+            return launchPushT<SHAPE, 4, 4, 4, ALT>(sp, E, B, J, g, pp, status, stream);                              \
         case 2:                                                                                                       \
-            return launchPushT<SHAPE, 8, 8, 8>(sp, E, B, J, g, pp, status, stream);                                   \
+            return launchPushT<SHAPE, 8, 8, 8, ALT>(sp, E, B, J, g, pp, status, stream);                              \
         }                                                                                                             \
         return cudaErrorInvalidValue;                                                                                 \
-    }                                                                                                                 \
+    }
+
+// Instantiates the deposit and charge-density launchers of one shape for the supported
+// supercell sizes.
+#define PICGB_SHAPE_LAUNCHERS(SHAPE, NAME)                                                                            \
     cudaError_t launchDeposit##NAME(                                                                                  \
         int scId,                                                                                                     \
         SpeciesDev const& sp,                                                                                         \

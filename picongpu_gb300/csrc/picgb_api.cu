@@ -44,6 +44,7 @@ PushParams picgb_sim::pushParams(Species const& s, bool deposit) const
     p.invVdt = 1.0f / vdt;
     p.c = cfg.c;
     p.pusher = s.cfg.pusher;
+    p.current = s.cfg.current;
     p.deposit = deposit ? 1 : 0;
     p.kindCount = prof ? kindCount : nullptr;
     // Fixed-point format of the J tile (kernels built with PICGB_J_FIXED).  A
@@ -370,7 +371,10 @@ namespace picgb::host
         return PICGB_OK;
     }
 
-    bool hasCurrent(Species const& sp) { return sp.cfg.current == PICGB_CURRENT_ESIRKEPOV; }
+    bool hasCurrent(Species const& sp)
+    {
+        return sp.cfg.current == PICGB_CURRENT_ESIRKEPOV || sp.cfg.current == PICGB_CURRENT_EMZ;
+    }
 } // namespace
 
 extern "C"
@@ -510,7 +514,7 @@ extern "C"
         if(cfg->shape < PICGB_SHAPE_CIC || cfg->shape > PICGB_SHAPE_PQS)
             return fail(PICGB_ERR_UNSUPPORTED, "shape %d has no CUDA kernel (CIC, TSC, PQS are available)",
                         int(cfg->shape));
-        if(cfg->current < 0 || cfg->current > 1)
+        if(cfg->current < PICGB_CURRENT_NONE || cfg->current > PICGB_CURRENT_EMZ)
             return fail(PICGB_ERR_INVALID, "unknown current solver %d", int(cfg->current));
         if(!(cfg->mass > 0.0f))
             return fail(PICGB_ERR_INVALID, "species mass must be positive");

@@ -700,6 +700,81 @@ namespace picgb
             }
             cpt1D<2, kGeneral>(acc, stat, p0, p1, fm(fm(qv, g.dz), u));
         }
+
+        // ---- EmZ (fields/currentDeposition/EmZ/EmZ.hpp:72-120): the trajectory is split at
+        // the relay point (relayPoint.hpp:48-64) into at most two virtual particles, each
+        // on support, so each deposits with the short footprint of cpt1D<C, false>
+        // (EmZ/DepositCurrent.hpp:76-126: on-support shapes, loops [begin, begin + supp)).
+        // a0 -> a1 in the frame of cell shift sS, b0 -> b1 in the frame of sE; returns
+        // false when a shift is out of range, which valid inputs (|v| dt < cell) never give.
+        __device__ __forceinline__ static bool prepareEmZ(
+            float const pos[3],
+            float const vel[3],
+            GridParams const& g,
+            float a0[3],
+            float a1[3],
+            int sS[3],
+            float b0[3],
+            float b1[3],
+            int sE[3],
+            bool& two)
+        {
+            two = false;
+            bool ok = true;
+#pragma unroll
+            for(int d = 0; d < 3; ++d)
+            {
+                float const x2 = pos[d];
+                float const x1 = fs(x2, divCell(fm(vel[d], g.dt), d, g));
+                int i1, i2;
+                float relay;
+                if constexpr(SH::even)
+                {
+                    i1 = int(floorf(x1));
+                    i2 = int(floorf(x2));
+                    relay = i1 == i2 ? x2 : float(i1 > i2 ? i1 : i2);
+                }
+                else
+                {
+                    i1 = int(floorf(fa(x1, 0.5f)));
+                    i2 = int(floorf(fa(x2, 0.5f)));
+                    relay = i1 == i2 ? x2 : fdv(float(i1 + i2), 2.0f);
+                }
+                sS[d] = i1;
+                sE[d] = i2;
+                a0[d] = fs(x1, float(i1));
+                a1[d] = fs(relay, float(i1));
+                b0[d] = fs(relay, float(i2));
+                b1[d] = fs(x2, float(i2));
+                two |= (i1 != i2);
+                ok &= (i1 >= -1 && i1 <= (SH::even ? 1 : 2) && i2 >= 0 && i2 <= (SH::even ? 0 : 1));
+            }
+            return ok;
+        }
+
+        // One EmZ virtual particle (EmZ/DepositCurrent.hpp:38-63): chargeDensity = q / V and
+        // currentSurfaceDensity = cellEdge * chargeDensity / dt, in the reference's order.
+        template<typename Acc>
+        __device__ __forceinline__ static void runEmZ(
+            Acc const& acc,
+            float const p0[3],
+            float const p1[3],
+            float charge,
+            GridParams const& g)
+        {
+            int const st[3] = {kInCell, kInCell, kInCell};
+            float const rho = fdv(charge, fm(fm(g.dx, g.dy), g.dz));
+            float const u = acc.unit();
+            {
+                float const a0[3] = {p0[1], p0[2], p0[0]}, a1[3] = {p1[1], p1[2], p1[0]};
+                cpt1D<0, false>(acc, st, a0, a1, fm(fdv(fm(g.dx, rho), g.dt), u));
+            }
+            {
+                float const a0[3] = {p0[2], p0[0], p0[1]}, a1[3] = {p1[2], p1[0], p1[1]};
+                cpt1D<1, false>(acc, st, a0, a1, fm(fdv(fm(g.dy, rho), g.dt), u));
+            }
+            cpt1D<2, false>(acc, st, p0, p1, fm(fdv(fm(g.dz, rho), g.dt), u));
+        }
     };
 
 } // namespace picgb

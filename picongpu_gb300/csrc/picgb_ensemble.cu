@@ -407,6 +407,8 @@ extern "C"
     {
         if(int r = checkEns(e))
             return r;
+        if(cfg && cfg->current == PICGB_CURRENT_EMZ)
+            return fail(PICGB_ERR_UNSUPPORTED, "the batched push deposits with Esirkepov only; EmZ runs on the single-box path");
         for(auto* b : e->boxes)
             if(int r = picgb_add_species(b, cfg, index))
                 return r;

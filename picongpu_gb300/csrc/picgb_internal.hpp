@@ -66,6 +66,10 @@ namespace picgb
     constexpr int kPusherFree = 1;
     constexpr int kPusherHigueraCary = 3;
     constexpr int kPusherVay = 4;
+    // PushParams::current values (the C-ABI's enum picgb_current)
+    constexpr int kCurrentNone = 0;
+    constexpr int kCurrentEsirkepov = 1;
+    constexpr int kCurrentEmZ = 2;
 
     struct PushParams
     {
@@ -77,6 +81,7 @@ namespace picgb
         float invVdt; // 1 / (dx * dy * dz * dt)
         float c; // speed of light (HigueraCary and Vay)
         int pusher; // 0 Boris, 1 Free, 3 HigueraCary, 4 Vay (2 = not pushed, never launched)
+        int current; // 1 Esirkepov, 2 EmZ (0: no current, the deposit is off)
         int deposit; // deposit the current inside the push kernel
         unsigned long long* kindCount; // profiling only: [0] deposits with the short footprint, [1] general; or nullptr
         JFixed jf; // fixed-point format of the J tile (used when built with PICGB_J_FIXED)

@@ -306,7 +306,9 @@ namespace
             std::string const pre = std::string("particles_") + sp.name + "_";
             Value& ps = child(particles, sp.name);
             attr(ps, "particleShape", double(sp.shape), "FLOAT");
-            attr(ps, "currentDeposition", sp.current == PICGB_CURRENT_ESIRKEPOV ? "Esirkepov" : "none", "STRING");
+            attr(ps, "currentDeposition",
+                 sp.current == PICGB_CURRENT_ESIRKEPOV ? "Esirkepov" : (sp.current == PICGB_CURRENT_EMZ ? "EmZ" : "none"),
+                 "STRING");
             attr(ps, "particlePush", pusherName(sp.pusher), "STRING");
             attr(ps, "particleInterpolation", "uniform", "STRING");
             attr(ps, "particleSmoothing", "none", "STRING");

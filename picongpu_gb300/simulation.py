@@ -22,7 +22,7 @@ from . import _lib as L
 PUSHERS = {"Boris": L.PUSHER_BORIS, "Free": L.PUSHER_FREE, "HigueraCary": L.PUSHER_HIGUERA_CARY,
            "Vay": L.PUSHER_VAY, None: L.PUSHER_NONE}
 SHAPES = {"CIC": L.SHAPE_CIC, "TSC": L.SHAPE_TSC, "PQS": L.SHAPE_PQS}
-CURRENTS = {"Esirkepov": L.CURRENT_ESIRKEPOV, None: L.CURRENT_NONE}
+CURRENTS = {"Esirkepov": L.CURRENT_ESIRKEPOV, "EmZ": L.CURRENT_EMZ, None: L.CURRENT_NONE}
 SOLVERS = {"Yee": L.SOLVER_YEE}
 SUPERCELLS = {(8, 8, 4): L.SUPERCELL_8x8x4, (4, 4, 4): L.SUPERCELL_4x4x4, (8, 8, 8): L.SUPERCELL_8x8x8}
 

@@ -94,14 +94,21 @@ def test_higuera_cary_and_vay_one_step(orc, pusher, shape):
     _push_and_deposit(orc, shape, (8, 8, 4), pusher, amp=0.3)
 
 
-def _push_and_deposit(orc, shape, sc, pusher, amp=0.05):
+@pytest.mark.parametrize("pusher", ["Boris", "HigueraCary"])
+@pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS"])
+def test_emz_one_step(orc, pusher, shape):
+    """The EmZ deposit (fields/currentDeposition/EmZ/EmZ.hpp) fused into the push, within 1e-6."""
+    _push_and_deposit(orc, shape, (8, 8, 4), pusher, current="EmZ")
+
+
+def _push_and_deposit(orc, shape, sc, pusher, amp=0.05, current="Esirkepov"):
     g = make_grid((32, 32, 32) if sc != (8, 8, 8) else (32, 32, 16), sc=sc)
     gd = g.as_dict()
     rng = np.random.default_rng(100 + len(shape) + sc[2] + len(pusher))
     p = random_particles(gd, 4, rng, u_th=0.2, weight=0.01)  # hot: many cell and supercell crossings
     E = random_field(gd, rng, amp=amp)
     B = random_field(gd, rng, amp=amp)
-    sp = pg.Species("e", charge=-1.0, mass=1.0, pusher=pusher, shape=shape, with_ids=True)
+    sp = pg.Species("e", charge=-1.0, mass=1.0, pusher=pusher, shape=shape, current=current, with_ids=True)
     with pg.Simulation(g) as sim:
         sim.add_species(sp)
         sim.set_particles("e", p)
@@ -122,8 +129,9 @@ def _push_and_deposit(orc, shape, sc, pusher, amp=0.05):
     assert max_rel(Jg, Jo) <= REL
 
 
+@pytest.mark.parametrize("current", ["Esirkepov", "EmZ"])
 @pytest.mark.parametrize("fuse", [True, False])
-def test_full_step_two_species(orc, fuse):
+def test_full_step_two_species(orc, fuse, current):
     """One Simulation::runOneStep of an electron-proton plasma (CIC), both deposit orders."""
     g = make_grid((32, 32, 32), fuse=fuse)
     gd = g.as_dict()
@@ -132,8 +140,8 @@ def test_full_step_two_species(orc, fuse):
     pi = random_particles(gd, 4, rng, u_th=0.05 / np.sqrt(1836.0), mass=1836.0, weight=0.01)
     pi["pos"] = pe["pos"].copy()  # protons start on the electrons: quasi-neutral
     E, B = random_field(gd, rng, 0.02), random_field(gd, rng, 0.02)
-    se = pg.Species("e", -1.0, 1.0, shape="CIC", with_ids=True)
-    si = pg.Species("i", 1.0, 1836.0, shape="CIC", with_ids=True)
+    se = pg.Species("e", -1.0, 1.0, shape="CIC", current=current, with_ids=True)
+    si = pg.Species("i", 1.0, 1836.0, shape="CIC", current=current, with_ids=True)
     with pg.Simulation(g) as sim:
         sim.add_species(se)
         sim.add_species(si)

@@ -115,13 +115,14 @@ def test_exb_drift_kept_by_higuera_cary_and_vay(orc):
     assert dev["Boris"] > 1e-2, dev
 
 
+@pytest.mark.parametrize("current", [1, 2], ids=["Esirkepov", "EmZ"])
 @pytest.mark.parametrize("shape", [1, 2, 3])
-def test_esirkepov_charge_continuity(orc, shape):
-    """(rho1 - rho0)/dt + div J = 0 on every node (Esirkepov's defining property)."""
+def test_charge_continuity(orc, shape, current):
+    """(rho1 - rho0)/dt + div J = 0 on every node, the defining property of Esirkepov and EmZ."""
     g = grid(n=(16, 16, 8))
     rng = np.random.default_rng(7 + shape)
     p = random_particles(g, 3, rng, u_th=0.3)
-    sp = dict(charge=-1.0, mass=1.0, shape=shape, pusher=1, current=1)
+    sp = dict(charge=-1.0, mass=1.0, shape=shape, pusher=1, current=current)
     shp = (g["nz"], g["ny"], g["nx"])
     rho0 = np.zeros(shp, np.float32)
     orc.charge_density(g, sp, p, rho0)
