@@ -462,6 +462,37 @@ def run_pushers(args, local_rank):
     return out
 
 
+def run_thermal(args, local_rank):
+    """The reference's Thermal benchmark (share/picongpu/benchmarks/Thermal: 192^3 cells, 25
+    electrons per cell at kT = 17.5 mc^2, HigueraCary pusher, PQS shape) with its EmZ and
+    Esirkepov variants (cmakeFlags flags[2], flags[5]).  Synthetic seeded start: the
+    Temperature manipulator's normal momenta with u_th = sqrt(kT / mc^2).  Host clock around
+    the timed steps, stream synchronised on both sides."""
+    import picongpu_gb300 as pg
+
+    out = {"workload": "Thermal: 192^3 cells, e 25 ppc, kT = 17.5 mc^2, HigueraCary, PQS, Yee, fp32",
+           "steps": args.thermal_steps, "unit": "particle-steps/s"}
+    for current in ("EmZ", "Esirkepov"):
+        g = pg.Grid(192, 192, 192, dt=DT, supercell=(8, 8, 4), device=local_rank)
+        with pg.Simulation(g) as sim:
+            sim.add_species(pg.Species("e", -1.0, 1.0, pusher="HigueraCary", shape="PQS", current=current))
+            sim.init_plasma("e", 25, density(), float(np.sqrt(17.5)), seed=31, position_seed=32)
+            npart = sim.particle_count("e")
+            for _ in range(args.warmup):
+                sim.step()
+            sim.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.thermal_steps):
+                sim.step()
+            sim.synchronize()
+            dt_wall = time.perf_counter() - t0
+            ok = sim.device_status() == 0
+        out[current] = npart * args.thermal_steps / dt_wall
+        out[current + "_status_ok"] = bool(ok)
+    out["particles"] = npart
+    return out
+
+
 def run_checkpoint(args, local_rank):
     """openPMD checkpoint write and restart read of the two-stream workload on 64^3 cells
     (E, B and 2 x 4.2e6 particles) to a temporary directory, timed with the host clock
@@ -606,6 +637,8 @@ def main():
     ap.add_argument("--laser-steps", type=int, default=40)
     ap.add_argument("--no-pushers", action="store_true")
     ap.add_argument("--no-checkpoint", action="store_true")
+    ap.add_argument("--no-thermal", action="store_true")
+    ap.add_argument("--thermal-steps", type=int, default=20)
     ap.add_argument("--pusher-steps", type=int, default=20)
     ap.add_argument("--adjoint-steps", type=int, default=300)
     ap.add_argument("--adjoint-fd-steps", type=int, default=20)
@@ -663,6 +696,9 @@ def main():
     checkpoint = None
     if not args.no_checkpoint:
         checkpoint = run_checkpoint(args, local_rank)
+    thermal = None
+    if not args.no_thermal:
+        thermal = run_thermal(args, local_rank)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         val, cores, sample = cpu_sample_rate(wl, 10, 1, budget_s=20.0)
@@ -672,7 +708,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded device init)", "config": config,
             "particles": r["npart"], "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"],
             "clocks": r["clocks"], "gpu_launches": r["launches"], "batched": batched, "adjoint": adjoint,
-            "laser_wake": laser, "pushers": pushers, "checkpoint": checkpoint}
+            "laser_wake": laser, "pushers": pushers, "checkpoint": checkpoint, "thermal": thermal}
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch
