@@ -494,15 +494,6 @@ namespace picgb
         }
     }
 
-#ifndef PICGB_J_FIXED
-    // 1: the shared-memory J tile holds 32-bit fixed-point high and low parts
-    // added with native fire-and-forget integer atomics; 0: floats added with
-    // atomicAdd, which for shared memory is a load/compare-and-swap loop on this
-    // target that retries whenever another warp updated the node in between
-    // (measured on the 256^3 two-stream workload: 30.9 vs 39.7 ms per launch)
-#    define PICGB_J_FIXED 1
-#endif
-
     // Shared-memory J tile of one supercell: [3][TT] floats, or [2][3][TT] ints in fixed point.
     template<int TX, int TY, int TT>
     struct TileJ
@@ -534,12 +525,12 @@ namespace picgb
 #if PICGB_J_FIXED
             constexpr float kMagic = 12582912.0f; // 1.5 * 2^23
             constexpr int kMagicBits = 0x4B400000;
-            int* hi = reinterpret_cast<int*>(J);
+            int* w = reinterpret_cast<int*>(J);
             float const t = __fmaf_rn(v, f.hiStep, kMagic); // kMagic + rint(v / 2^k)
             float const a = __fsub_rn(t, kMagic);
             float const r = __fmaf_rn(-a, f.hiUnit, v); // exact (Sterbenz)
-            atomicAdd(hi + idx, __float_as_int(t) - kMagicBits);
-            atomicAdd(hi + 3 * TT + idx, __float_as_int(__fadd_rn(r, kMagic)) - kMagicBits);
+            atomicAdd(w + idx, __float_as_int(t) - kMagicBits);
+            atomicAdd(w + 3 * TT + idx, __float_as_int(__fadd_rn(r, kMagic)) - kMagicBits);
 #else
             atomicAdd(J + idx, v);
 #endif
