@@ -10,11 +10,16 @@
 
 namespace picgb
 {
+#ifndef PICGB_BATCH_MIN_BLOCKS
+    // resident 256-thread blocks per SM the batched kernel's register budget is sized for
+#    define PICGB_BATCH_MIN_BLOCKS 3
+#endif
+
     // Resident blocks the batched kernel's register budget is sized for.
     template<int THREADS>
     constexpr int batchMinBlocks()
     {
-        return THREADS >= 256 ? PICGB_PUSH_MIN_BLOCKS : 2 * PICGB_PUSH_MIN_BLOCKS;
+        return THREADS >= 256 ? PICGB_BATCH_MIN_BLOCKS : 2 * PICGB_BATCH_MIN_BLOCKS;
     }
 
     template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT>

@@ -14,15 +14,26 @@
 
 namespace picgb
 {
-    constexpr int kPushThreads = 256;
+#ifndef PICGB_PUSH_THREADS
+    // threads per supercell block of the single-box push kernel: 16 warps, two blocks
+    // per SM (two-stream 256^3, TSC, ms per launch: 256 threads 30.7, 448 28.5, 512 27.1)
+#    define PICGB_PUSH_THREADS 512
+#endif
+    constexpr int kPushThreads = PICGB_PUSH_THREADS;
 #ifndef PICGB_PUSH_MIN_BLOCKS
-    // resident blocks per SM the push kernel's register budget is sized for
-#    define PICGB_PUSH_MIN_BLOCKS 3
+    // resident blocks per SM the push kernel's register budget is sized for (64
+    // registers at 512 threads, no spills)
+#    define PICGB_PUSH_MIN_BLOCKS 2
 #endif
 
     // Per-warp queue of deposit jobs of particles that cross a cell boundary
-    // (see kPush): kQueueCap jobs of kJobWords words for every warp.
-    constexpr int kQueueCap = 64;
+    // (see kPush): kQueueCap jobs (32 or more) of kJobWords words for every warp.
+#ifndef PICGB_QUEUE_CAP
+    // 32 keeps the 16 queues of a 512-thread block at 18 KB, so two blocks fit an SM
+#    define PICGB_QUEUE_CAP 32
+#endif
+    constexpr int kQueueCap = PICGB_QUEUE_CAP;
+    static_assert(kQueueCap >= 32, "a warp drains 32 jobs at a time");
     constexpr int kJobWords = 9;
 
     template<typename SH, typename SC, int THREADS = kPushThreads>
@@ -379,14 +390,21 @@ namespace picgb
                     atomicAdd(pp.kindCount + 1, (unsigned long long) __popc(crossing));
                 }
             }
-            if(kind == 1)
+            // the lanes that fit go in now; a queue that reaches 32 jobs is drained; the
+            // lanes that did not fit go in after the drain (only with kQueueCap < 63)
+            int const nc = __popc(crossing);
+            int const room = kQueueCap - queued;
+            int const rank = __popc(crossing & laneMaskLt());
+            auto enqueue = [&](int at)
             {
                 if constexpr(EMZ)
-                    queue.put(queued + __popc(crossing & laneMaskLt()), b0, b1, charge, orgB, stat);
+                    queue.put(at, b0, b1, charge, orgB, stat);
                 else
-                    queue.put(queued + __popc(crossing & laneMaskLt()), p0, p1, charge, org, stat);
-            }
-            queued += __popc(crossing);
+                    queue.put(at, p0, p1, charge, org, stat);
+            };
+            if(kind == 1 && rank < room)
+                enqueue(queued + rank);
+            queued += nc < room ? nc : room;
             __syncwarp();
             if(queued >= 32)
             {
@@ -401,6 +419,13 @@ namespace picgb
                 if(lane < queued - 32)
                     queue.move(32 + lane, lane);
                 queued -= 32;
+                __syncwarp();
+            }
+            if(nc > room)
+            {
+                if(kind == 1 && rank >= room)
+                    enqueue(queued + rank - room);
+                queued += nc - room;
                 __syncwarp();
             }
         }
