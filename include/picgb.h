@@ -336,7 +336,7 @@ extern "C"
         picgb_grid_config grid; /* settings shared by all boxes; grid.nx, ny, nz are ignored */
         int32_t nbox;
         const int32_t* dims; /* nbox * 3 cell counts (x, y, z), each a multiple of the supercell */
-        int32_t threads; /* threads per supercell of the batched push: 128 or 256 (0 = 256) */
+        int32_t threads; /* threads per supercell of the batched push: 128, 256 or 512 (0 = 256) */
     } picgb_ensemble_config;
     int picgb_ensemble_create(const picgb_ensemble_config* cfg, picgb_ensemble** out);
     int picgb_ensemble_destroy(picgb_ensemble* ens);
@@ -355,11 +355,13 @@ extern "C"
     /* Kernels launched by batched steps so far (nodes of the step graph times replays). */
     int picgb_ensemble_launch_count(picgb_ensemble* ens, uint64_t* n);
     /* Autotuner: builds the ensemble `cfg` once for each candidate supercell (8x8x4, 4x4x4,
-     * 8x8x8) and threads per supercell (128, 256), initialises the species (nspecies configs,
-     * inits[s * nbox + box]), runs `warmup` + `steps` batched steps and measures
-     * particle-steps/s with CUDA events.  rates[6] (may be NULL) receives the rate of each
-     * candidate in the order (8x8x4,128), (8x8x4,256), (4x4x4,128), ... and 0 for candidates
-     * that do not divide every box; *supercell and *threads receive the fastest. */
+     * 8x8x8) and threads per supercell (128, 256, 512), initialises the species (nspecies
+     * configs, inits[s * nbox + box]), runs `warmup` + `steps` batched steps and measures
+     * particle-steps/s with CUDA events.  rates[PICGB_AUTOTUNE_CANDIDATES] (may be NULL)
+     * receives the rate of each candidate in the order (8x8x4,128), (8x8x4,256), (8x8x4,512),
+     * (4x4x4,128), ... and 0 for candidates that do not divide every box; *supercell and
+     * *threads receive the fastest. */
+#define PICGB_AUTOTUNE_CANDIDATES 9
     int picgb_ensemble_autotune(
         const picgb_ensemble_config* cfg,
         int32_t nspecies,

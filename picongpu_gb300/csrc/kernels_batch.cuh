@@ -15,11 +15,12 @@ namespace picgb
 #    define PICGB_BATCH_MIN_BLOCKS 3
 #endif
 
-    // Resident blocks the batched kernel's register budget is sized for.
+    // Resident blocks the batched kernel's register budget is sized for (512 threads:
+    // two blocks at 64 registers, as the single-box kernel).
     template<int THREADS>
     constexpr int batchMinBlocks()
     {
-        return THREADS >= 256 ? PICGB_BATCH_MIN_BLOCKS : 2 * PICGB_BATCH_MIN_BLOCKS;
+        return THREADS >= 512 ? 2 : (THREADS >= 256 ? PICGB_BATCH_MIN_BLOCKS : 2 * PICGB_BATCH_MIN_BLOCKS);
     }
 
     template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT>
@@ -96,24 +97,30 @@ namespace picgb
     }
 
 // Instantiates the batched launcher of one shape and pusher variant (ALT: HigueraCary
-// and Vay) for the supercell sizes 8x8x4, 4x4x4, 8x8x8 and 128 or 256 threads per
+// and Vay) for the supercell sizes 8x8x4, 4x4x4, 8x8x8 and 128, 256 or 512 threads per
 // supercell.  Each (shape, variant) pair has its own translation unit, so the
 // heaviest instantiations compile in parallel.
 #define PICGB_BATCH_CASES(F, SHAPE, ALT, ...)                                                                         \
-    switch(scId * 2 + (threads == 128 ? 0 : 1))                                                                       \
+    switch(scId * 3 + (threads == 128 ? 0 : (threads == 256 ? 1 : 2)))                                               \
     {                                                                                                                 \
     case 0:                                                                                                           \
         return F<SHAPE, 8, 8, 4, 128, ALT>(__VA_ARGS__);                                                              \
     case 1:                                                                                                           \
         return F<SHAPE, 8, 8, 4, 256, ALT>(__VA_ARGS__);                                                              \
     case 2:                                                                                                           \
-        return F<SHAPE, 4, 4, 4, 128, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 8, 8, 4, 512, ALT>(__VA_ARGS__);                                                              \
     case 3:                                                                                                           \
-        return F<SHAPE, 4, 4, 4, 256, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 4, 4, 4, 128, ALT>(__VA_ARGS__);                                                              \
     case 4:                                                                                                           \
-        return F<SHAPE, 8, 8, 8, 128, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 4, 4, 4, 256, ALT>(__VA_ARGS__);                                                              \
     case 5:                                                                                                           \
+        return F<SHAPE, 4, 4, 4, 512, ALT>(__VA_ARGS__);                                                              \
+    case 6:                                                                                                           \
+        return F<SHAPE, 8, 8, 8, 128, ALT>(__VA_ARGS__);                                                              \
+    case 7:                                                                                                           \
         return F<SHAPE, 8, 8, 8, 256, ALT>(__VA_ARGS__);                                                              \
+    case 8:                                                                                                           \
+        return F<SHAPE, 8, 8, 8, 512, ALT>(__VA_ARGS__);                                                              \
     }
 
 #define PICGB_BATCH_LAUNCHERS(SHAPE, NAME, ALT)                                                                       \
@@ -127,7 +134,7 @@ namespace picgb
         unsigned* status,                                                                                             \
         cudaStream_t stream)                                                                                          \
     {                                                                                                                 \
-        if(threads != 128 && threads != 256)                                                                          \
+        if(threads != 128 && threads != 256 && threads != 512)                                                        \
             return cudaErrorInvalidValue;                                                                             \
         PICGB_BATCH_CASES(launchPushBatchT, SHAPE, ALT, table, items, nitems, counter, status, stream)                \
         return cudaErrorInvalidValue;                                                                                 \

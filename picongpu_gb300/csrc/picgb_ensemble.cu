@@ -332,8 +332,8 @@ extern "C"
         if(cfg->nbox <= 0 || uint32_t(cfg->nbox) > kBatchMaxBoxes || !cfg->dims)
             return fail(PICGB_ERR_INVALID, "an ensemble needs 1 to %u boxes", kBatchMaxBoxes);
         int const threads = cfg->threads ? cfg->threads : 256;
-        if(threads != 128 && threads != 256)
-            return fail(PICGB_ERR_INVALID, "threads per supercell must be 128 or 256, not %d", threads);
+        if(threads != 128 && threads != 256 && threads != 512)
+            return fail(PICGB_ERR_INVALID, "threads per supercell must be 128, 256 or 512, not %d", threads);
         auto e = new picgb_ensemble();
         e->cfg = *cfg;
         e->cfg.dims = nullptr;
@@ -482,9 +482,10 @@ extern "C"
         if(!cfg || !cfg->dims || cfg->nbox <= 0 || nspecies <= 0 || !species || !inits || !bestSupercell || !bestThreads
            || steps == 0)
             return fail(PICGB_ERR_INVALID, "autotune needs a config, species, their inits and steps > 0");
-        static int const cand[6][2] = {{0, 128}, {0, 256}, {1, 128}, {1, 256}, {2, 128}, {2, 256}};
+        static int const cand[PICGB_AUTOTUNE_CANDIDATES][2]
+            = {{0, 128}, {0, 256}, {0, 512}, {1, 128}, {1, 256}, {1, 512}, {2, 128}, {2, 256}, {2, 512}};
         double best = -1.0;
-        for(int c = 0; c < 6; ++c)
+        for(int c = 0; c < PICGB_AUTOTUNE_CANDIDATES; ++c)
         {
             if(rates)
                 rates[c] = 0.0;

@@ -19,8 +19,7 @@ import numpy as np
 from . import _lib as L
 from .simulation import CURRENTS, PUSHERS, SHAPES, SOLVERS, SUPERCELLS, Grid, Simulation, Species
 
-CANDIDATES = [((8, 8, 4), 128), ((8, 8, 4), 256), ((4, 4, 4), 128), ((4, 4, 4), 256), ((8, 8, 8), 128),
-              ((8, 8, 8), 256)]
+CANDIDATES = [(sc, t) for sc in ((8, 8, 4), (4, 4, 4), (8, 8, 8)) for t in (128, 256, 512)]
 
 
 def _config(dims, grid: Grid, threads: int):
@@ -131,8 +130,8 @@ def autotune(dims, species: list[Species], inits: list[list[L.PlasmaInit]], grid
         raise ValueError("inits needs one list of per-box inits per species")
     ini = (L.PlasmaInit * len(flat))(*flat)
     sc, th = ctypes.c_int32(), ctypes.c_int32()
-    rates = (ctypes.c_double * 6)()
+    rates = (ctypes.c_double * len(CANDIDATES))()
     L.call("picgb_ensemble_autotune", ctypes.byref(cfg), len(species), scfg, ini, warmup, steps, ctypes.byref(sc),
            ctypes.byref(th), rates)
     inv = {v: k for k, v in SUPERCELLS.items()}
-    return inv[sc.value], th.value, {CANDIDATES[i]: rates[i] for i in range(6)}
+    return inv[sc.value], th.value, {CANDIDATES[i]: rates[i] for i in range(len(CANDIDATES))}
