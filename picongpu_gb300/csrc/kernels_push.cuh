@@ -165,6 +165,44 @@ namespace picgb
         }
     };
 
+#ifndef PICGB_DRAIN_OUT_OF_LINE
+#    define PICGB_DRAIN_OUT_OF_LINE 1
+#endif
+
+    // Deposit of the queued jobs of lanes [0, njobs) of a warp with the general footprint
+    // (EmZ: the second virtual particles).  The tile and the queue are addressed as word
+    // offsets into the block's dynamic shared memory, so the accesses stay shared-memory
+    // atomics and loads.  Out of line when PICGB_DRAIN_OUT_OF_LINE: the path runs once per
+    // 32 queued jobs, and keeping its code out of the particle loop keeps the loop small
+    // for the instruction cache.
+    template<typename SH, int TX, int TY, int TT, bool EMZ>
+#if PICGB_DRAIN_OUT_OF_LINE
+    __device__ __noinline__
+#else
+    __device__ __forceinline__
+#endif
+        void drainQueue(int jOff, int qOff, int njobs, JFixed jf, float dx, float dy, float dz, float dt, float invVdt)
+    {
+        extern __shared__ __align__(16) float smem[];
+        int const lane = threadIdx.x & 31;
+        if(lane >= njobs)
+            return;
+        WarpQueue const queue{smem + qOff};
+        float q0[3], q1[3], qc;
+        int qo, qs[3];
+        queue.get(lane, q0, q1, qc, qo, qs);
+        GridParams g{};
+        g.dx = dx;
+        g.dy = dy;
+        g.dz = dz;
+        g.dt = dt;
+        using Tile = TileJ<TX, TY, TT>;
+        if constexpr(EMZ)
+            Esirkepov<SH>::runEmZ(Tile{smem + jOff, qo, jf}, q0, q1, qc, g);
+        else
+            Esirkepov<SH>::template run<true>(Tile{smem + jOff, qo, jf}, q0, q1, qs, qc, g, invVdt);
+    }
+
     // Push of the particles of supercell `sc` by one block of THREADS threads.
     // Each thread pushes one particle per round; then the warp deposits at once
     // the lanes whose particle stays in its assignment cell along every axis
@@ -199,7 +237,8 @@ namespace picgb
         float* const Bs = smem + 3 * TG::GT;
         float* const Js = smem + 6 * TG::GT;
         int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        WarpQueue const queue{smem + 6 * TG::GT + TG::JWords + warp * kQueueCap * kJobWords};
+        int const qOff = 6 * TG::GT + TG::JWords + warp * kQueueCap * kJobWords; // word offset of this warp's queue
+        WarpQueue const queue{smem + qOff};
 
         uint32_t const n = sp.count[sc];
         if(threadIdx.x == 0)
@@ -408,13 +447,8 @@ namespace picgb
             __syncwarp();
             if(queued >= 32)
             {
-                float q0[3], q1[3], qc;
-                int qo, qs[3];
-                queue.get(lane, q0, q1, qc, qo, qs);
-                if constexpr(EMZ)
-                    ES::runEmZ(Tile{Js, qo, pp.jf}, q0, q1, qc, g);
-                else
-                    ES::template run<true>(Tile{Js, qo, pp.jf}, q0, q1, qs, qc, g, pp.invVdt);
+                drainQueue<SH, TG::JX, TG::JY, TG::JT, EMZ>(
+                    int(Js - smem), qOff, 32, pp.jf, g.dx, g.dy, g.dz, g.dt, pp.invVdt);
                 __syncwarp();
                 if(lane < queued - 32)
                     queue.move(32 + lane, lane);
@@ -430,16 +464,9 @@ namespace picgb
             }
         }
         // the jobs still queued
-        if(pp.deposit && lane < queued)
-        {
-            float q0[3], q1[3], qc;
-            int qo, qs[3];
-            queue.get(lane, q0, q1, qc, qo, qs);
-            if constexpr(EMZ)
-                ES::runEmZ(Tile{Js, qo, pp.jf}, q0, q1, qc, g);
-            else
-                ES::template run<true>(Tile{Js, qo, pp.jf}, q0, q1, qs, qc, g, pp.invVdt);
-        }
+        if(pp.deposit && queued > 0)
+            drainQueue<SH, TG::JX, TG::JY, TG::JT, EMZ>(
+                int(Js - smem), qOff, queued, pp.jf, g.dx, g.dy, g.dz, g.dt, pp.invVdt);
         __syncthreads(); // every hole is recorded and every deposit done
         if(threadIdx.x == 0)
             sp.nhole[sc] = s_nhole;

@@ -495,9 +495,15 @@ namespace picgb
     }
 
     // Shared-memory J tile of one supercell: [3][TT] floats, or [2][3][TT] ints in fixed point.
+#ifndef PICGB_SHORT_LOOP
+    // 1: the short-footprint deposit runs its three components in a runtime loop
+#    define PICGB_SHORT_LOOP 1
+#endif
+
     template<int TX, int TY, int TT>
     struct TileJ
     {
+        static constexpr int kTT = TT;
         float* J;
         int base; // tile index of the particle's Esirkepov origin (cell + gridShift)
         JFixed f;
@@ -521,7 +527,15 @@ namespace picgb
         {
             int x, y, z;
             rotToReal<C>(ri, rj, rk, x, y, z);
-            int const idx = C * TT + base + x + TX * (y + TY * z);
+            addAt(C * TT + base + x + TX * (y + TY * z), v);
+        }
+
+        // word stride of real axis a (0 x, 1 y, 2 z)
+        __device__ __forceinline__ static int stride(int a) { return a == 0 ? 1 : (a == 1 ? TX : TX * TY); }
+
+        // v at tile word idx of the first plane (component offset included by the caller)
+        __device__ __forceinline__ void addAt(int idx, float v) const
+        {
 #if PICGB_J_FIXED
             constexpr float kMagic = 12582912.0f; // 1.5 * 2^23
             constexpr int kMagicBits = 0x4B400000;
@@ -664,6 +678,65 @@ namespace picgb
                 }
         }
 
+        // The short footprint (the particle stays in its assignment cell along every axis) of
+        // the three rotated components in one runtime loop, so the particle loop holds one
+        // copy of the unrolled (i, j, k) body instead of three.  Same arithmetic as
+        // cpt1D<C, false>; the rotation maps rotated axes i, j, k to real axes C+1, C+2, C.
+        template<typename Acc>
+        __device__ __forceinline__ static void runShort(
+            Acc const& acc,
+            float const p0[3],
+            float const p1[3],
+            float const csd[3],
+            int tileTT)
+        {
+            auto sel = [](float const* p, int a) { return a == 0 ? p[0] : (a == 1 ? p[1] : p[2]); };
+#pragma unroll 1
+            for(int C = 0; C < 3; ++C)
+            {
+                int const ai = C == 2 ? 0 : C + 1;
+                int const aj = C == 0 ? 2 : C - 1;
+                float const q0[3] = {sel(p0, ai), sel(p0, aj), sel(p0, C)};
+                float const q1[3] = {sel(p1, ai), sel(p1, aj), sel(p1, C)};
+                if(q0[2] == q1[2])
+                    continue;
+                int const si = Acc::stride(ai), sj = Acc::stride(aj), sk = Acc::stride(C);
+                int const base = acc.base + C * tileTT;
+                float sj0[S + 1], sj1[S + 1], sk0[S + 1], sk1[S + 1];
+                SH::caArray(q0[1], false, sj0);
+                SH::caArray(q1[1], false, sj1);
+                SH::caArray(q0[2], false, sk0);
+                SH::caArray(q1[2], false, sk1);
+                float dsk[S];
+#pragma unroll
+                for(int k = 0; k < S; ++k)
+                    dsk[k] = fs(sk1[k], sk0[k]);
+                float const ncsd = -sel(csd, C);
+#pragma unroll
+                for(int i = begin; i < end; ++i)
+                {
+                    float const s0i = SH::ca(fs(float(i), q0[0]));
+                    float const dsi = fs(SH::ca(fs(float(i), q1[0])), s0i);
+#pragma unroll
+                    for(int j = begin; j < end; ++j)
+                    {
+                        float const s0j = sj0[j - begin];
+                        float const dsj = fs(sj1[j - begin], s0j);
+                        float const half = fm(0.5f, __fmaf_rn(dsi, s0j, fm(s0i, dsj)));
+                        float const tmp = fm(ncsd, __fmaf_rn(fm(1.0f / 3.0f, dsj), dsi, __fmaf_rn(s0i, s0j, half)));
+                        float run = 0.0f;
+                        int const row = base + i * si + j * sj;
+#pragma unroll
+                        for(int k = begin; k < end - 1; ++k)
+                        {
+                            run = __fmaf_rn(dsk[k - begin], tmp, run);
+                            acc.addAt(row + k * sk, run);
+                        }
+                    }
+                }
+            }
+        }
+
         // the three rotated calls; csd = charge * (1/(V*dt)) * cellEdgeLength (Esirkepov.hpp:188-190)
         template<bool kGeneral, typename Acc>
         __device__ __forceinline__ static void run(
@@ -679,6 +752,14 @@ namespace picgb
             // the accumulator's unit (a power of two) is applied to csd: exact, and the
             // deposited values arrive already scaled
             float const u = acc.unit();
+#if PICGB_SHORT_LOOP
+            if constexpr(!kGeneral)
+            {
+                float const csd[3] = {fm(fm(qv, g.dx), u), fm(fm(qv, g.dy), u), fm(fm(qv, g.dz), u)};
+                runShort(acc, p0, p1, csd, Acc::kTT);
+                return;
+            }
+#endif
             {
                 int const st[3] = {stat[1], stat[2], stat[0]};
                 float const a0[3] = {p0[1], p0[2], p0[0]}, a1[3] = {p1[1], p1[2], p1[0]};
@@ -756,6 +837,14 @@ namespace picgb
             int const st[3] = {kInCell, kInCell, kInCell};
             float const rho = fdv(charge, fm(fm(g.dx, g.dy), g.dz));
             float const u = acc.unit();
+#if PICGB_SHORT_LOOP
+            {
+                float const csd[3] = {fm(fdv(fm(g.dx, rho), g.dt), u), fm(fdv(fm(g.dy, rho), g.dt), u),
+                                      fm(fdv(fm(g.dz, rho), g.dt), u)};
+                runShort(acc, p0, p1, csd, Acc::kTT);
+                return;
+            }
+#endif
             {
                 float const a0[3] = {p0[1], p0[2], p0[0]}, a1[3] = {p1[1], p1[2], p1[0]};
                 cpt1D<0, false>(acc, st, a0, a1, fm(fdv(fm(g.dx, rho), g.dt), u));
