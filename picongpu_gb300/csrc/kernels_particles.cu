@@ -402,6 +402,35 @@ namespace picgb
         }
     }
 
+    // Largest |w| of n values as the bits of a non-negative float (ordered like the values; a
+    // NaN reads above the bits of infinity).  *bits must be zero on entry.
+    __global__ void kMaxAbsBits(uint64_t n, float const* __restrict__ w, unsigned* bits)
+    {
+        unsigned m = 0u;
+        for(uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+        {
+            unsigned const b = __float_as_uint(w[i]) & 0x7FFFFFFFu;
+            m = b > m ? b : m;
+        }
+#pragma unroll
+        for(int o = 16; o > 0; o >>= 1)
+        {
+            unsigned const v = __shfl_xor_sync(0xffffffffu, m, o);
+            m = v > m ? v : m;
+        }
+        if((threadIdx.x & 31) == 0 && m)
+            atomicMax(bits, m);
+    }
+
+    cudaError_t launchMaxAbsBits(float const* w, uint64_t n, unsigned* bits, cudaStream_t stream)
+    {
+        if(n == 0)
+            return cudaSuccess;
+        int const blocks = int(std::min<uint64_t>((n + 255) / 256, 152 * 16));
+        kMaxAbsBits<<<blocks, 256, 0, stream>>>(n, w, bits);
+        return cudaGetLastError();
+    }
+
     cudaError_t launchHistogram(
         int scId,
         uint64_t n,

@@ -555,15 +555,17 @@ extern "C"
         CUDA_TRY(cudaMemcpyAsync(st.lcell, h->lcell, sizeof(uint16_t) * n, cudaMemcpyHostToDevice, s->stream));
         if(st.id)
             CUDA_TRY(cudaMemcpyAsync(st.id, h->id, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s->stream));
+        // per-supercell counts, and in the last word the bits of the largest |w|
         uint32_t* hcount = nullptr;
-        CUDA_TRY(dalloc(hcount, size_t(s->nsc)));
-        CUDA_TRY(cudaMemsetAsync(hcount, 0, sizeof(uint32_t) * s->nsc, s->stream));
+        CUDA_TRY(dalloc(hcount, size_t(s->nsc) + 1));
+        CUDA_TRY(cudaMemsetAsync(hcount, 0, sizeof(uint32_t) * (s->nsc + 1), s->stream));
         CUDA_TRY(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->stream));
         float const* pos3[3] = {st.a[0], st.a[1], st.a[2]};
         CUDA_TRY(launchHistogram(s->cfg.supercell, n, st.sc, st.lcell, pos3, hcount, s->nsc, s->status, s->stream));
-        ++s->launches;
-        std::vector<uint32_t> cnt(s->nsc);
-        CUDA_TRY(cudaMemcpyAsync(cnt.data(), hcount, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(launchMaxAbsBits(st.a[6], n, hcount + s->nsc, s->stream));
+        s->launches += 2;
+        std::vector<uint32_t> cnt(s->nsc + 1);
+        CUDA_TRY(cudaMemcpyAsync(cnt.data(), hcount, sizeof(uint32_t) * (s->nsc + 1), cudaMemcpyDeviceToHost, s->stream));
         unsigned bits = 0;
         if(int r = readStatus(s, &bits, true))
         {
@@ -574,12 +576,13 @@ extern "C"
         if(bits & ST_BAD_CELL)
             return fail(PICGB_ERR_INVALID, "species '%s': a particle has an out-of-range supercell, cell index or in-cell position",
                         sp.name.c_str());
+        unsigned const wbits = cnt[s->nsc];
+        cnt.pop_back();
         uint32_t const mx = cnt.empty() ? 0u : *std::max_element(cnt.begin(), cnt.end());
-        float wmax = 0.0f;
-        for(uint64_t i = 0; i < n; ++i)
-            wmax = std::max(wmax, std::fabs(h->w[i]));
-        if(!std::isfinite(wmax))
+        if(wbits >= 0x7F800000u) // infinity or NaN
             return fail(PICGB_ERR_INVALID, "species '%s': a weighting is not finite", sp.name.c_str());
+        float wmax;
+        std::memcpy(&wmax, &wbits, sizeof(wmax));
         sp.wmax = wmax;
         uint32_t cap = sp.cfg.capacity;
         if(cap == 0)

@@ -132,6 +132,7 @@ namespace picgb
         unsigned* status,
         cudaStream_t stream);
     cudaError_t launchCompact(SpeciesDev const& sp, int nsc, cudaStream_t stream);
+    cudaError_t launchMaxAbsBits(float const* w, uint64_t n, unsigned* bits, cudaStream_t stream);
     cudaError_t launchHistogram(
         int scId,
         uint64_t n,
