@@ -424,6 +424,28 @@ extern "C"
      * without the low-energy branch); synchronises the stream. */
     int picgb_diff_kinetic_energy(picgb_diff* d, const picgb_diff_state* state, int32_t species, double* out, void* stream);
 
+    /* ------------------------------------------------------------ open boundaries and PML
+     * The reference's non-periodic boundaries (`--periodic 0` on an axis): fields absorbed by
+     * the convolutional PML of fields/absorber/pml/Pml.kernel (Yee updates of
+     * fields/absorber/pml/Pml.kernel:400-590, coefficients :130-267, parameters of
+     * param/fieldAbsorber.param), particles absorbed (deleted) when they leave the box.  Beyond
+     * the box the fields are zero.  Values are in the simulation's units: sigma and alpha are
+     * the reference's "normalized" values (divided by eps0), in 1/time. */
+    typedef struct picgb_boundary_config
+    {
+        int32_t open[3]; /* per axis: 0 periodic, 1 open (PML fields, absorbing particles) */
+        int32_t pml_cells[3][2]; /* PML thickness per face (negative, positive) of an open axis */
+        float sigma_max[3]; /* normalized sigma max; < 0: 0.8 (m + 1) c / cell edge (fieldAbsorber.param) */
+        float kappa_max[3]; /* >= 1 */
+        float alpha_max[3]; /* normalized alpha max, >= 0 */
+        float grading_order; /* sigma and kappa grading order m (fieldAbsorber.param: 4) */
+        float alpha_grading_order; /* alpha grading order (fieldAbsorber.param: 1) */
+    } picgb_boundary_config;
+    /* Sets the boundaries (all periodic at creation); resets the PML's convolution fields. Not
+     * for ensemble boxes.  The charge-residual diagnostic stays periodic, so with an open axis
+     * it is meaningful away from the box faces only. */
+    int picgb_set_boundaries(picgb_sim* sim, const picgb_boundary_config* cfg);
+
     /* ------------------------------------------------------------ openPMD checkpoints
      * The reference's Checkpoint and openPMD plugins (plugins/Checkpoint.x.cpp,
      * plugins/openPMD/openPMDWriter.hpp) write E, B and every species in the openPMD 1.1.0

@@ -35,7 +35,13 @@ _lib = None
 class OrcGrid(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("nx", "ny", "nz", "sx", "sy", "sz")] + [
         (n, ctypes.c_float) for n in ("dx", "dy", "dz", "dt", "c", "eps0")
-    ]
+    ] + [("open", ctypes.c_int)]
+
+
+class OrcPml(ctypes.Structure):
+    _fields_ = [("cells", (ctypes.c_int * 2) * 3), ("sigma_max", ctypes.c_double * 3),
+                ("kappa_max", ctypes.c_double * 3), ("alpha_max", ctypes.c_double * 3),
+                ("order", ctypes.c_double), ("alpha_order", ctypes.c_double)]
 
 
 class OrcSpecies(ctypes.Structure):
@@ -96,6 +102,8 @@ def lib() -> ctypes.CDLL:
         L.orc_push.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), P(OrcField), P(OrcField)]
         L.orc_deposit.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), P(OrcField), ctypes.c_int]
         L.orc_esirkepov_one.argtypes = [P(OrcGrid), ctypes.c_int, vp, vp, vp, ctypes.c_float, P(OrcField)]
+        L.orc_yee_b_half_open.argtypes = [P(OrcGrid), vp, P(OrcField), P(OrcField), vp, ctypes.c_int]
+        L.orc_yee_e_open.argtypes = [P(OrcGrid), vp, P(OrcField), P(OrcField), vp]
         L.orc_emz_one.argtypes = [P(OrcGrid), ctypes.c_int, vp, vp, vp, ctypes.c_float, P(OrcField)]
         L.orc_step.argtypes = [
             P(OrcGrid),
@@ -128,8 +136,32 @@ def _ptr(a: np.ndarray) -> int:
 def grid(g) -> OrcGrid:
     """Build the ctypes grid from any object/dict with nx..eps0 attributes."""
     get = (lambda k: g[k]) if isinstance(g, dict) else (lambda k: getattr(g, k))
+    opn = g.get("open", 0) if isinstance(g, dict) else getattr(g, "open", 0)
     return OrcGrid(*[int(get(k)) for k in ("nx", "ny", "nz", "sx", "sy", "sz")],
-                   *[float(get(k)) for k in ("dx", "dy", "dz", "dt", "c", "eps0")])
+                   *[float(get(k)) for k in ("dx", "dy", "dz", "dt", "c", "eps0")], int(opn))
+
+
+def pml(cells, sigma_max, kappa_max, alpha_max, order=4.0, alpha_order=1.0) -> OrcPml:
+    """PML parameters: cells[a] = (negative, positive) thickness, per-axis sigma/kappa/alpha maxima."""
+    p = OrcPml()
+    for a in range(3):
+        p.cells[a][0], p.cells[a][1] = int(cells[a][0]), int(cells[a][1])
+        p.sigma_max[a], p.kappa_max[a], p.alpha_max[a] = float(sigma_max[a]), float(kappa_max[a]), float(alpha_max[a])
+    p.order, p.alpha_order = float(order), float(alpha_order)
+    return p
+
+
+def _psi(psi: np.ndarray):
+    assert psi.dtype == np.float32 and psi.shape[0] == 6 and psi.flags["C_CONTIGUOUS"]
+    return (ctypes.c_void_p * 6)(*[psi[k].ctypes.data for k in range(6)])
+
+
+def yee_b_half_open(g, p: OrcPml, E, B, psiB, update: bool):
+    lib().orc_yee_b_half_open(grid(g), ctypes.byref(p), field(E), field(B), _psi(psiB), int(bool(update)))
+
+
+def yee_e_open(g, p: OrcPml, B, E, psiE):
+    lib().orc_yee_e_open(grid(g), ctypes.byref(p), field(B), field(E), _psi(psiE))
 
 
 def species(s) -> OrcSpecies:

@@ -13,6 +13,13 @@ extern "C"
     {
         int nx, ny, nz, sx, sy, sz;
         float dx, dy, dz, dt, c, eps0;
+        int open; // bit a: axis a open
+    };
+    struct orc_pml
+    {
+        int cells[3][2];
+        double sigma_max[3], kappa_max[3], alpha_max[3];
+        double order, alpha_order;
     };
     struct orc_species
     {
@@ -38,7 +45,7 @@ namespace
 {
     orc::Grid toGrid(orc_grid const* g)
     {
-        return orc::Grid{g->nx, g->ny, g->nz, g->sx, g->sy, g->sz, g->dx, g->dy, g->dz, g->dt, g->c, g->eps0};
+        return orc::Grid{g->nx, g->ny, g->nz, g->sx, g->sy, g->sz, g->dx, g->dy, g->dz, g->dt, g->c, g->eps0, g->open};
     }
     orc::SpeciesParam toSp(orc_species const* s)
     {
@@ -170,6 +177,34 @@ extern "C"
         auto Jf = toF(J);
         orc::JAccess<float> acc{&G, &Jf};
         orc::esirkepov(G, shape, cell, pos, vel, charge, acc);
+    }
+
+    static orc::PmlConfig toPml(orc_pml const* p)
+    {
+        orc::PmlConfig c{};
+        for(int a = 0; a < 3; ++a)
+        {
+            c.cells[a][0] = p->cells[a][0];
+            c.cells[a][1] = p->cells[a][1];
+            c.sigmaMax[a] = p->sigma_max[a];
+            c.kappaMax[a] = p->kappa_max[a];
+            c.alphaMax[a] = p->alpha_max[a];
+        }
+        c.order = p->order;
+        c.alphaOrder = p->alpha_order;
+        return c;
+    }
+
+    void orc_yee_b_half_open(orc_grid const* g, orc_pml const* p, orc_field const* E, orc_field* B, float* const* psi, int update)
+    {
+        auto Bf = toF(B);
+        orc::yeeBHalfOpen(toGrid(g), toPml(p), toF(E), Bf, psi, update != 0);
+    }
+
+    void orc_yee_e_open(orc_grid const* g, orc_pml const* p, orc_field const* B, orc_field* E, float* const* psi)
+    {
+        auto Ef = toF(E);
+        orc::yeeEOpen(toGrid(g), toPml(p), toF(B), Ef, psi);
     }
 
     void orc_emz_one(

@@ -40,6 +40,9 @@ namespace orc
         float dt; // time step
         float c; // speed of light
         float eps0; // vacuum permittivity
+        int open = 0; // bit a: axis a is open (no wrap; fields zero beyond the box, particles absorbed)
+
+        static constexpr size_t kOutside = ~size_t(0); // idx() of a point beyond an open face
 
         int nscx() const { return nx / sx; }
         int nscy() const { return ny / sy; }
@@ -55,7 +58,16 @@ namespace orc
         }
         size_t idx(int x, int y, int z) const
         {
+            if(((open & 1) && (x < 0 || x >= nx)) || ((open & 2) && (y < 0 || y >= ny))
+               || ((open & 4) && (z < 0 || z >= nz)))
+                return kOutside;
             return size_t(wrap(x, nx)) + size_t(nx) * (size_t(wrap(y, ny)) + size_t(ny) * size_t(wrap(z, nz)));
+        }
+        // component value at a flat index, zero beyond an open face
+        template<typename T>
+        static T at(T const* f, size_t i)
+        {
+            return i == kOutside ? T(0) : f[i];
         }
     };
 
@@ -298,12 +310,12 @@ namespace orc
     {
         size_t i0 = g.idx(x, y, z), ix = g.idx(x + 1, y, z), iy = g.idx(x, y + 1, z), iz = g.idx(x, y, z + 1);
         // dF/dx, dF/dy, dF/dz as full vectors (only the needed components are used)
-        T dFdx_y = (F.c[1][ix] - F.c[1][i0]) / T(g.dx);
-        T dFdx_z = (F.c[2][ix] - F.c[2][i0]) / T(g.dx);
-        T dFdy_x = (F.c[0][iy] - F.c[0][i0]) / T(g.dy);
-        T dFdy_z = (F.c[2][iy] - F.c[2][i0]) / T(g.dy);
-        T dFdz_x = (F.c[0][iz] - F.c[0][i0]) / T(g.dz);
-        T dFdz_y = (F.c[1][iz] - F.c[1][i0]) / T(g.dz);
+        T dFdx_y = (Grid::at(F.c[1], ix) - F.c[1][i0]) / T(g.dx);
+        T dFdx_z = (Grid::at(F.c[2], ix) - F.c[2][i0]) / T(g.dx);
+        T dFdy_x = (Grid::at(F.c[0], iy) - F.c[0][i0]) / T(g.dy);
+        T dFdy_z = (Grid::at(F.c[2], iy) - F.c[2][i0]) / T(g.dy);
+        T dFdz_x = (Grid::at(F.c[0], iz) - F.c[0][i0]) / T(g.dz);
+        T dFdz_y = (Grid::at(F.c[1], iz) - F.c[1][i0]) / T(g.dz);
         out[0] = dFdy_z - dFdz_y;
         out[1] = dFdz_x - dFdx_z;
         out[2] = dFdx_y - dFdy_x;
@@ -313,12 +325,12 @@ namespace orc
     inline void curlBackward(Grid const& g, Field3<T> const& F, int x, int y, int z, T out[3])
     {
         size_t i0 = g.idx(x, y, z), ix = g.idx(x - 1, y, z), iy = g.idx(x, y - 1, z), iz = g.idx(x, y, z - 1);
-        T dFdx_y = (F.c[1][i0] - F.c[1][ix]) / T(g.dx);
-        T dFdx_z = (F.c[2][i0] - F.c[2][ix]) / T(g.dx);
-        T dFdy_x = (F.c[0][i0] - F.c[0][iy]) / T(g.dy);
-        T dFdy_z = (F.c[2][i0] - F.c[2][iy]) / T(g.dy);
-        T dFdz_x = (F.c[0][i0] - F.c[0][iz]) / T(g.dz);
-        T dFdz_y = (F.c[1][i0] - F.c[1][iz]) / T(g.dz);
+        T dFdx_y = (F.c[1][i0] - Grid::at(F.c[1], ix)) / T(g.dx);
+        T dFdx_z = (F.c[2][i0] - Grid::at(F.c[2], ix)) / T(g.dx);
+        T dFdy_x = (F.c[0][i0] - Grid::at(F.c[0], iy)) / T(g.dy);
+        T dFdy_z = (F.c[2][i0] - Grid::at(F.c[2], iy)) / T(g.dy);
+        T dFdz_x = (F.c[0][i0] - Grid::at(F.c[0], iz)) / T(g.dz);
+        T dFdz_y = (F.c[1][i0] - Grid::at(F.c[1], iz)) / T(g.dz);
         out[0] = dFdy_z - dFdz_y;
         out[1] = dFdz_x - dFdx_z;
         out[2] = dFdx_y - dFdy_x;
@@ -426,7 +438,7 @@ namespace orc
                     for(int x = begin; x <= end; ++x)
                     {
                         size_t i = g.idx(cell[0] + shift[0] + x, cell[1] + shift[1] + y, cell[2] + shift[2] + z);
-                        result_x = std::fma(F.c[comp][i], sx[x - begin], result_x);
+                        result_x = std::fma(Grid::at(F.c[comp], i), sx[x - begin], result_x);
                     }
                     result_y = std::fma(result_x, sy[y - begin], result_y);
                 }
@@ -674,6 +686,11 @@ namespace orc
     {
         int const ncx = g.nscx(), ncy = g.nscy(), ncz = g.nscz();
         int scx = sc % ncx, scy = (sc / ncx) % ncy, scz = sc / (ncx * ncy);
+        // leaving through an open face: absorbed (-1)
+        if(((g.open & 1) && (scx + dir[0] < 0 || scx + dir[0] >= ncx))
+           || ((g.open & 2) && (scy + dir[1] < 0 || scy + dir[1] >= ncy))
+           || ((g.open & 4) && (scz + dir[2] < 0 || scz + dir[2] >= ncz)))
+            return -1;
         scx = Grid::wrap(scx + dir[0], ncx);
         scy = Grid::wrap(scy + dir[1], ncy);
         scz = Grid::wrap(scz + dir[2], ncz);
@@ -688,6 +705,8 @@ namespace orc
 #pragma omp parallel for schedule(static)
         for(long long k = 0; k < (long long) P.n; ++k)
         {
+            if(P.sc[k] < 0) // absorbed at an open face in an earlier step
+                continue;
             int cell[3];
             cellOf(g, P.sc[k], P.lcell[k], cell);
             T pos[3] = {P.pos[0][k], P.pos[1][k], P.pos[2][k]};
@@ -751,7 +770,12 @@ namespace orc
     {
         Grid const* g;
         Field3<T>* J;
-        void add(int comp, int x, int y, int z, T v) { J->c[comp][g->idx(x, y, z)] += v; }
+        void add(int comp, int x, int y, int z, T v)
+        {
+            size_t const i = g->idx(x, y, z);
+            if(i != Grid::kOutside) // current beyond an open face is dropped
+                J->c[comp][i] += v;
+        }
     };
 
     // cptCurrent1D (fields/currentDeposition/Esirkepov/Esirkepov.hpp:147-242) in the rotated frame:
@@ -1004,6 +1028,8 @@ namespace orc
         JAccess<T> acc{&g, &J};
         for(size_t k = 0; k < P.n; ++k)
         {
+            if(P.sc[k] < 0)
+                continue;
             int cell[3];
             cellOf(g, P.sc[k], P.lcell[k], cell);
             T const pos[3] = {P.pos[0][k], P.pos[1][k], P.pos[2][k]};
@@ -1042,6 +1068,8 @@ namespace orc
             size_t const k0 = std::min(P.n, chunk * t), k1 = std::min(P.n, k0 + chunk);
             for(size_t k = k0; k < k1; ++k)
             {
+                if(P.sc[k] < 0)
+                    continue;
                 int cell[3];
                 cellOf(g, P.sc[k], P.lcell[k], cell);
                 T const pos[3] = {P.pos[0][k], P.pos[1][k], P.pos[2][k]};
@@ -1072,6 +1100,8 @@ namespace orc
         T const V = T(g.dx) * T(g.dy) * T(g.dz);
         for(size_t k = 0; k < P.n; ++k)
         {
+            if(P.sc[k] < 0)
+                continue;
             int cell[3];
             cellOf(g, P.sc[k], P.lcell[k], cell);
             T const attr = (T(sp.charge) * P.w[k]) / V;
@@ -1081,7 +1111,9 @@ namespace orc
                 T assign = T(1.0);
                 for(int d = 0; d < 3; ++d)
                     assign *= ShapeFn<T>::ca(sp.shape, T(off[d]) - P.pos[d][k]);
-                rho[g.idx(cell[0] + off[0], cell[1] + off[1], cell[2] + off[2])] += assign * attr;
+                size_t const ri = g.idx(cell[0] + off[0], cell[1] + off[1], cell[2] + off[2]);
+                if(ri != Grid::kOutside)
+                    rho[ri] += assign * attr;
             }
         }
     }
@@ -1097,9 +1129,9 @@ namespace orc
                 for(int x = 0; x < g.nx; ++x)
                 {
                     size_t i = g.idx(x, y, z);
-                    T div = (E.c[0][i] - E.c[0][g.idx(x - 1, y, z)]) * rw
-                        + (E.c[1][i] - E.c[1][g.idx(x, y - 1, z)]) * rh
-                        + (E.c[2][i] - E.c[2][g.idx(x, y, z - 1)]) * rd;
+                    T div = (E.c[0][i] - Grid::at(E.c[0], g.idx(x - 1, y, z))) * rw
+                        + (E.c[1][i] - Grid::at(E.c[1], g.idx(x, y - 1, z))) * rh
+                        + (E.c[2][i] - Grid::at(E.c[2], g.idx(x, y, z - 1))) * rd;
                     T r = std::abs(div * T(g.eps0) - rho[i]);
                     if(out)
                         out[i] = r;
@@ -1128,6 +1160,8 @@ namespace orc
         double sum = 0.0;
         for(size_t k = 0; k < P.n; ++k)
         {
+            if(P.sc[k] < 0)
+                continue;
             T const mom[3] = {P.mom[0][k], P.mom[1][k], P.mom[2][k]};
             sum += double(kinEnergy(mom, T(sp.mass) * P.w[k], T(g.c)));
         }
@@ -1185,5 +1219,139 @@ namespace orc
                 depositThreaded(g, sp[s], P[s], J, depositThreads);
         addCurrent(g, J, E);
         yeeBHalf(g, E, B);
+    }
+    // ---------------------------------------------------------------- open boundaries, PML
+    // Convolutional PML of fields/absorber/pml/Pml.kernel for the open axes of g.open.
+    struct PmlConfig
+    {
+        int cells[3][2]; // thickness at the negative and positive face of each open axis
+        double sigmaMax[3], kappaMax[3], alphaMax[3]; // normalized (divided by eps0), 1/time
+        double order, alphaOrder; // grading orders
+    };
+
+    // b, c, kappa at position x (cells) along axis a (Pml.kernel:130-267): relative depth d,
+    // sigma = sigmaMax d^m, kappa = 1 + (kappaMax - 1) d^m, alpha = alphaMax (1 - d)^ma,
+    // b = exp(-(sigma / kappa + alpha) dt), c = sigma (b - 1) / (kappa (sigma + alpha kappa)).
+    inline void pmlCoef(Grid const& g, PmlConfig const& p, int a, double x, float out[3])
+    {
+        int const n = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+        double depth = 0.0;
+        if(g.open & (1 << a))
+        {
+            double const neg = p.cells[a][0], pos = p.cells[a][1];
+            double const rightStart = double(n) - pos;
+            if(x < neg)
+                depth = (neg - x) / neg;
+            else if(x > rightStart && pos > 0)
+                depth = (x - rightStart) / pos;
+        }
+        double sigma = 0.0, alpha = 0.0, kappa = 1.0;
+        if(depth != 0.0)
+        {
+            double const grade = std::pow(depth, p.order);
+            sigma = p.sigmaMax[a] * grade;
+            kappa = 1.0 + (p.kappaMax[a] - 1.0) * grade;
+            alpha = p.alphaMax[a] * std::pow(1.0 - depth, p.alphaOrder);
+        }
+        double const b = std::exp(-(sigma / kappa + alpha) * double(g.dt));
+        double const den = kappa * (sigma + alpha * kappa);
+        out[0] = float(b);
+        out[1] = float(den != 0.0 ? sigma * (b - 1.0) / den : 0.0);
+        out[2] = float(kappa);
+    }
+
+    // psi component order: xy, xz, yx, yz, zx, zy (psi.ab: field component a, derivative along b)
+    enum
+    {
+        PSI_XY,
+        PSI_XZ,
+        PSI_YX,
+        PSI_YZ,
+        PSI_ZX,
+        PSI_ZY
+    };
+
+    // B half step with the PML (Pml.kernel:522-581); the convolution fields advance when updatePsi.
+    inline void yeeBHalfOpen(Grid const& g, PmlConfig const& p, Field3<float> const& E, Field3<float>& B, float* const psi[6], bool updatePsi)
+    {
+#pragma omp parallel for schedule(static)
+        for(int z = 0; z < g.nz; ++z)
+            for(int y = 0; y < g.ny; ++y)
+                for(int x = 0; x < g.nx; ++x)
+                {
+                    size_t const i = g.idx(x, y, z), ix = g.idx(x + 1, y, z), iy = g.idx(x, y + 1, z),
+                                 iz = g.idx(x, y, z + 1);
+                    float const dFdx_y = (Grid::at(E.c[1], ix) - E.c[1][i]) / g.dx;
+                    float const dFdx_z = (Grid::at(E.c[2], ix) - E.c[2][i]) / g.dx;
+                    float const dFdy_x = (Grid::at(E.c[0], iy) - E.c[0][i]) / g.dy;
+                    float const dFdy_z = (Grid::at(E.c[2], iy) - E.c[2][i]) / g.dy;
+                    float const dFdz_x = (Grid::at(E.c[0], iz) - E.c[0][i]) / g.dz;
+                    float const dFdz_y = (Grid::at(E.c[1], iz) - E.c[1][i]) / g.dz;
+                    float cx[3], cy[3], cz[3];
+                    pmlCoef(g, p, 0, x + 0.5, cx);
+                    pmlCoef(g, p, 1, y + 0.5, cy);
+                    pmlCoef(g, p, 2, z + 0.5, cz);
+                    if(cx[0] * cy[0] * cz[0] == 1.0f)
+                    {
+                        B.c[0][i] = B.c[0][i] - (dFdy_z - dFdz_y) * 0.5f * g.dt;
+                        B.c[1][i] = B.c[1][i] - (dFdz_x - dFdx_z) * 0.5f * g.dt;
+                        B.c[2][i] = B.c[2][i] - (dFdx_y - dFdy_x) * 0.5f * g.dt;
+                        continue;
+                    }
+                    if(updatePsi)
+                    {
+                        psi[PSI_YX][i] = cx[0] * psi[PSI_YX][i] + cx[1] * dFdx_z;
+                        psi[PSI_ZX][i] = cx[0] * psi[PSI_ZX][i] + cx[1] * dFdx_y;
+                        psi[PSI_XY][i] = cy[0] * psi[PSI_XY][i] + cy[1] * dFdy_z;
+                        psi[PSI_ZY][i] = cy[0] * psi[PSI_ZY][i] + cy[1] * dFdy_x;
+                        psi[PSI_XZ][i] = cz[0] * psi[PSI_XZ][i] + cz[1] * dFdz_y;
+                        psi[PSI_YZ][i] = cz[0] * psi[PSI_YZ][i] + cz[1] * dFdz_x;
+                    }
+                    float const h = 0.5f * g.dt;
+                    B.c[0][i] += h * (dFdz_y / cz[2] - dFdy_z / cy[2] + psi[PSI_XZ][i] - psi[PSI_XY][i]);
+                    B.c[1][i] += h * (dFdx_z / cx[2] - dFdz_x / cz[2] + psi[PSI_YX][i] - psi[PSI_YZ][i]);
+                    B.c[2][i] += h * (dFdy_x / cy[2] - dFdx_y / cx[2] + psi[PSI_ZY][i] - psi[PSI_ZX][i]);
+                }
+    }
+
+    // E step with the PML (Pml.kernel:424-475); the convolution fields advance every call.
+    inline void yeeEOpen(Grid const& g, PmlConfig const& p, Field3<float> const& B, Field3<float>& E, float* const psi[6])
+    {
+        float const c2 = g.c * g.c;
+#pragma omp parallel for schedule(static)
+        for(int z = 0; z < g.nz; ++z)
+            for(int y = 0; y < g.ny; ++y)
+                for(int x = 0; x < g.nx; ++x)
+                {
+                    size_t const i = g.idx(x, y, z), ix = g.idx(x - 1, y, z), iy = g.idx(x, y - 1, z),
+                                 iz = g.idx(x, y, z - 1);
+                    float const dFdx_y = (B.c[1][i] - Grid::at(B.c[1], ix)) / g.dx;
+                    float const dFdx_z = (B.c[2][i] - Grid::at(B.c[2], ix)) / g.dx;
+                    float const dFdy_x = (B.c[0][i] - Grid::at(B.c[0], iy)) / g.dy;
+                    float const dFdy_z = (B.c[2][i] - Grid::at(B.c[2], iy)) / g.dy;
+                    float const dFdz_x = (B.c[0][i] - Grid::at(B.c[0], iz)) / g.dz;
+                    float const dFdz_y = (B.c[1][i] - Grid::at(B.c[1], iz)) / g.dz;
+                    float cx[3], cy[3], cz[3];
+                    pmlCoef(g, p, 0, x, cx);
+                    pmlCoef(g, p, 1, y, cy);
+                    pmlCoef(g, p, 2, z, cz);
+                    if(cx[0] * cy[0] * cz[0] == 1.0f)
+                    {
+                        E.c[0][i] = E.c[0][i] + (dFdy_z - dFdz_y) * c2 * g.dt;
+                        E.c[1][i] = E.c[1][i] + (dFdz_x - dFdx_z) * c2 * g.dt;
+                        E.c[2][i] = E.c[2][i] + (dFdx_y - dFdy_x) * c2 * g.dt;
+                        continue;
+                    }
+                    psi[PSI_YX][i] = cx[0] * psi[PSI_YX][i] + cx[1] * dFdx_z;
+                    psi[PSI_ZX][i] = cx[0] * psi[PSI_ZX][i] + cx[1] * dFdx_y;
+                    psi[PSI_XY][i] = cy[0] * psi[PSI_XY][i] + cy[1] * dFdy_z;
+                    psi[PSI_ZY][i] = cy[0] * psi[PSI_ZY][i] + cy[1] * dFdy_x;
+                    psi[PSI_XZ][i] = cz[0] * psi[PSI_XZ][i] + cz[1] * dFdz_y;
+                    psi[PSI_YZ][i] = cz[0] * psi[PSI_YZ][i] + cz[1] * dFdz_x;
+                    float const c2dt = c2 * g.dt;
+                    E.c[0][i] += c2dt * (dFdy_z / cy[2] - dFdz_y / cz[2] + psi[PSI_XY][i] - psi[PSI_XZ][i]);
+                    E.c[1][i] += c2dt * (dFdz_x / cz[2] - dFdx_z / cx[2] + psi[PSI_YZ][i] - psi[PSI_YX][i]);
+                    E.c[2][i] += c2dt * (dFdx_y / cx[2] - dFdy_x / cy[2] + psi[PSI_ZX][i] - psi[PSI_ZY][i]);
+                }
     }
 } // namespace orc

@@ -50,6 +50,12 @@ class OpenPMDSpecies(ctypes.Structure):
                 ("current", c_int), ("particles", Particles)]
 
 
+class BoundaryConfig(ctypes.Structure):
+    _fields_ = [("open", c_int * 3), ("pml_cells", (c_int * 2) * 3), ("sigma_max", c_float * 3),
+                ("kappa_max", c_float * 3), ("alpha_max", c_float * 3), ("grading_order", c_float),
+                ("alpha_grading_order", c_float)]
+
+
 class BufferDesc(ctypes.Structure):
     _fields_ = [("kind", c_int), ("ncomp", c_int), ("ptr", c_void_p * 10), ("dims", ctypes.c_int64 * 3),
                 ("stride", ctypes.c_int64 * 3), ("guard", c_int * 3), ("elem_bytes", c_int), ("capacity", c_uint32),
@@ -149,6 +155,7 @@ SIGNATURES = [
     ("picgb_openpmd_read_species", c_int, [c_char_p, c_uint32, c_char_p, P(GridConfig), P(Particles)]),
     ("picgb_openpmd_read_mesh", c_int, [c_char_p, c_uint32, c_char_p, P(GridConfig), P(c_void_p)]),
     ("picgb_checkpoint_write", c_int, [c_void_p, c_char_p, c_uint32]),
+    ("picgb_set_boundaries", c_int, [c_void_p, P(BoundaryConfig)]),
     ("picgb_checkpoint_read", c_int, [c_void_p, c_char_p, c_uint32]),
     ("picgb_diff_create", c_int, [P(DiffConfig), c_int, P(DiffSpecies), P(c_void_p)]),
     ("picgb_diff_destroy", c_int, [c_void_p]),

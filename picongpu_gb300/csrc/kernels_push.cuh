@@ -75,7 +75,13 @@ namespace picgb
         for(int t = threadIdx.x; t < TT; t += blockDim.x)
         {
             int const tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
-            int const gx = wrapi(ox + tx, g.nx), gy = wrapi(oy + ty, g.ny), gz = wrapi(oz + tz, g.nz);
+            int const gx = wrapOrOutside(ox + tx, g.nx, g.open & 1), gy = wrapOrOutside(oy + ty, g.ny, g.open & 2),
+                      gz = wrapOrOutside(oz + tz, g.nz, g.open & 4);
+            if((gx | gy | gz) < 0) // beyond an open face the fields are zero
+            {
+                dst[t] = dst[TT + t] = dst[2 * TT + t] = 0.0f;
+                continue;
+            }
             size_t const gi = size_t(gx) + size_t(g.nx) * (size_t(gy) + size_t(g.ny) * size_t(gz));
             dst[t] = __ldg(src + gi);
             dst[TT + t] = __ldg(src + ncell + gi);
@@ -84,7 +90,9 @@ namespace picgb
     }
 
     // Add a shared-memory J tile into the global J with periodic wrap (the
-    // reference's guard add of FieldJ, FieldJ.x.cpp:156-169, folded in).
+    // reference's guard add of FieldJ, FieldJ.x.cpp:156-169, folded in).  Beyond an
+    // open face the current is dropped, as the reference's guard current at a
+    // non-periodic boundary is.
     template<int TX, int TY, int TT>
     __device__ __forceinline__ void flushTile(
         float const* __restrict__ Js,
@@ -103,7 +111,10 @@ namespace picgb
             if(vx == 0.0f && vy == 0.0f && vz == 0.0f)
                 continue;
             int const tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
-            int const gx = wrapi(ox + tx, g.nx), gy = wrapi(oy + ty, g.ny), gz = wrapi(oz + tz, g.nz);
+            int const gx = wrapOrOutside(ox + tx, g.nx, g.open & 1), gy = wrapOrOutside(oy + ty, g.ny, g.open & 2),
+                      gz = wrapOrOutside(oz + tz, g.nz, g.open & 4);
+            if((gx | gy | gz) < 0)
+                continue;
             size_t const gi = size_t(gx) + size_t(g.nx) * (size_t(gy) + size_t(g.ny) * size_t(gz));
             if(vx != 0.0f)
                 atomicAdd(J + gi, vx);
@@ -362,46 +373,52 @@ namespace picgb
                 }
                 else
                 {
-                    int const dx = wrapi(scx + dir[0], g.nscx), dy = wrapi(scy + dir[1], g.nscy),
-                              dz = wrapi(scz + dir[2], g.nscz);
+                    int const dx = wrapOrOutside(scx + dir[0], g.nscx, g.open & 1),
+                              dy = wrapOrOutside(scy + dir[1], g.nscy, g.open & 2),
+                              dz = wrapOrOutside(scz + dir[2], g.nscz, g.open & 4);
                     int const dsc = dx + g.nscx * (dy + g.nscy * dz);
                     uint32_t const id = sp.id ? sp.id[slot] : 0u;
-                    uint32_t const s = atomicAdd(sp.tail + dsc, 1u);
-                    if(s < sp.cap)
+                    // a particle that leaves the box through an open face is absorbed: it only
+                    // vacates its slot (the reference's absorbing particle boundary)
+                    if((dx | dy | dz) >= 0)
                     {
-                        size_t const d = size_t(dsc) * sp.cap + s;
-                        sp.px[d] = pos[0];
-                        sp.py[d] = pos[1];
-                        sp.pz[d] = pos[2];
-                        sp.ux[d] = mom[0];
-                        sp.uy[d] = mom[1];
-                        sp.uz[d] = mom[2];
-                        sp.w[d] = w;
-                        sp.lcell[d] = uint16_t(nlc);
-                        if(sp.id)
-                            sp.id[d] = id;
-                    }
-                    else
-                    {
-                        uint32_t const q = atomicAdd(sp.sp_count, 1u);
-                        if(q < sp.spill_cap)
+                        uint32_t const s = atomicAdd(sp.tail + dsc, 1u);
+                        if(s < sp.cap)
                         {
-                            float* a = sp.sp_attr;
-                            size_t const C = sp.spill_cap;
-                            a[q] = pos[0];
-                            a[C + q] = pos[1];
-                            a[2 * C + q] = pos[2];
-                            a[3 * C + q] = mom[0];
-                            a[4 * C + q] = mom[1];
-                            a[5 * C + q] = mom[2];
-                            a[6 * C + q] = w;
-                            sp.sp_sc[q] = dsc;
-                            sp.sp_lcell[q] = uint16_t(nlc);
-                            sp.sp_id[q] = id;
-                            atomicOr(status, ST_OVERFLOW);
+                            size_t const d = size_t(dsc) * sp.cap + s;
+                            sp.px[d] = pos[0];
+                            sp.py[d] = pos[1];
+                            sp.pz[d] = pos[2];
+                            sp.ux[d] = mom[0];
+                            sp.uy[d] = mom[1];
+                            sp.uz[d] = mom[2];
+                            sp.w[d] = w;
+                            sp.lcell[d] = uint16_t(nlc);
+                            if(sp.id)
+                                sp.id[d] = id;
                         }
                         else
-                            atomicOr(status, ST_OVERFLOW | ST_LOST);
+                        {
+                            uint32_t const q = atomicAdd(sp.sp_count, 1u);
+                            if(q < sp.spill_cap)
+                            {
+                                float* a = sp.sp_attr;
+                                size_t const C = sp.spill_cap;
+                                a[q] = pos[0];
+                                a[C + q] = pos[1];
+                                a[2 * C + q] = pos[2];
+                                a[3 * C + q] = mom[0];
+                                a[4 * C + q] = mom[1];
+                                a[5 * C + q] = mom[2];
+                                a[6 * C + q] = w;
+                                sp.sp_sc[q] = dsc;
+                                sp.sp_lcell[q] = uint16_t(nlc);
+                                sp.sp_id[q] = id;
+                                atomicOr(status, ST_OVERFLOW);
+                            }
+                            else
+                                atomicOr(status, ST_OVERFLOW | ST_LOST);
+                        }
                     }
                     uint32_t const h = atomicAdd(&s_nhole, 1u);
                     sp.holes[base + h] = uint16_t(k);

@@ -490,6 +490,9 @@ int picgb::host::destroySim(picgb_sim* s)
     dfree(s->energy);
     dfree(s->maxBits);
     dfree(s->kindCount);
+    dfree(s->pml.psiE);
+    dfree(s->pml.psiB);
+    dfree(s->pmlTab);
     if(s->hostStatus)
         cudaFreeHost(s->hostStatus);
     profFlush(s);
@@ -886,14 +889,18 @@ extern "C"
         if(int r = checkSim(s))
             return r;
         float const t = float(double(step) * s->cfg.dt);
-        CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_B, [&] { return launchYeeBHalf(s->E, s->B, s->g, s->stream); }));
+        // the second half of the B update (FDTDBase.hpp:166-226): PML convolution fields unchanged
+        CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_B, [&] {
+            return s->g.open ? launchYeeBHalfOpen(s->E, s->B, s->g, s->pml, false, s->stream)
+                             : launchYeeBHalf(s->E, s->B, s->g, s->stream);
+        }));
         CUDA_TRY(launchIncidentB(s->B, s->g, s->inc, t, s->stream)); // incident E at t (Solver.hpp:500-533)
         // with the fused deposit J is complete here: E += curl B c^2 dt and E += coeff J in one pass
         float const* J = s->cfg.fuse_deposit ? s->J : nullptr;
-        CUDA_TRY(timedLaunch(
-            s,
-            PICGB_KERNEL_YEE_E,
-            [&] { return launchYeeE(s->B, s->E, J, s->coeffJ(), s->g, s->stream); }));
+        CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_E, [&] {
+            return s->g.open ? launchYeeEOpen(s->B, s->E, J, s->coeffJ(), s->g, s->pml, s->stream)
+                             : launchYeeE(s->B, s->E, J, s->coeffJ(), s->g, s->stream);
+        }));
         CUDA_TRY(launchIncidentE(s->E, s->g, s->inc, t + 0.5f * s->cfg.dt, s->stream)); // incident B at t + dt/2
         return PICGB_OK;
     }
@@ -934,8 +941,74 @@ extern "C"
     {
         if(int r = checkSim(s))
             return r;
-        CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_B, [&] { return launchYeeBHalf(s->E, s->B, s->g, s->stream); }));
+        // the first half of the B update: the PML convolution fields advance (FDTDBase.hpp:199-208)
+        CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_B, [&] {
+            return s->g.open ? launchYeeBHalfOpen(s->E, s->B, s->g, s->pml, true, s->stream)
+                             : launchYeeBHalf(s->E, s->B, s->g, s->stream);
+        }));
         CUDA_TRY(launchIncidentB(s->B, s->g, s->inc, float(double(step + 1) * s->cfg.dt), s->stream)); // E at t + dt
+        return PICGB_OK;
+    }
+
+    int picgb_set_boundaries(picgb_sim* s, const picgb_boundary_config* b)
+    {
+        if(int r = checkSim(s))
+            return r;
+        if(!b)
+            return fail(PICGB_ERR_INVALID, "null boundary config");
+        if(s->inEnsemble)
+            return fail(PICGB_ERR_UNSUPPORTED, "the boxes of an ensemble are periodic");
+        int const cells[3] = {s->cfg.nx, s->cfg.ny, s->cfg.nz};
+        float const edge[3] = {s->cfg.dx, s->cfg.dy, s->cfg.dz};
+        double const m = b->grading_order, ma = b->alpha_grading_order;
+        PmlAxis ax[3];
+        int open = 0;
+        for(int a = 0; a < 3; ++a)
+        {
+            if(b->open[a] != 0 && b->open[a] != 1)
+                return fail(PICGB_ERR_INVALID, "open[%d] must be 0 or 1", a);
+            if(!b->open[a])
+                continue;
+            int const neg = b->pml_cells[a][0], pos = b->pml_cells[a][1];
+            if(neg < 0 || pos < 0 || neg + pos > cells[a])
+                return fail(PICGB_ERR_INVALID, "PML of %d + %d cells does not fit %d cells on axis %d", neg, pos,
+                            cells[a], a);
+            if(!(m >= 0.0) || !(ma >= 0.0) || !(b->kappa_max[a] >= 1.0f) || !(b->alpha_max[a] >= 0.0f))
+                return fail(PICGB_ERR_INVALID, "PML needs grading orders >= 0, kappa_max >= 1 and alpha_max >= 0");
+            ax[a].open = true;
+            ax[a].cells = cells[a];
+            ax[a].neg = neg;
+            ax[a].pos = pos;
+            // default sigma: SIGMA_OPT = 0.8 (m + 1) / (Z0 d), normalized by eps0: 0.8 (m + 1) c / d
+            ax[a].sigmaMax = b->sigma_max[a] < 0.0f ? 0.8 * (m + 1.0) * double(s->cfg.c) / double(edge[a])
+                                                     : double(b->sigma_max[a]);
+            ax[a].kappaMax = b->kappa_max[a];
+            ax[a].alphaMax = b->alpha_max[a];
+            ax[a].order = m;
+            ax[a].alphaOrder = ma;
+            open |= 1 << a;
+        }
+        CUDA_TRY(cudaSetDevice(s->cfg.device));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        dfree(s->pml.psiE);
+        dfree(s->pml.psiB);
+        dfree(s->pmlTab);
+        s->pml = PmlDev{};
+        s->g.open = 0; // set below once the PML state exists
+        if(!open)
+            return PICGB_OK;
+        int const nmax = std::max(cells[0], std::max(cells[1], cells[2]));
+        std::vector<float> const tab = pmlTables(ax, double(s->cfg.dt), nmax);
+        CUDA_TRY(dalloc(s->pmlTab, tab.size()));
+        CUDA_TRY(cudaMemcpy(s->pmlTab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice));
+        CUDA_TRY(dalloc(s->pml.psiE, 6 * s->ncell));
+        CUDA_TRY(dalloc(s->pml.psiB, 6 * s->ncell));
+        CUDA_TRY(cudaMemsetAsync(s->pml.psiE, 0, sizeof(float) * 6 * s->ncell, s->stream));
+        CUDA_TRY(cudaMemsetAsync(s->pml.psiB, 0, sizeof(float) * 6 * s->ncell, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        s->pml.tab = s->pmlTab;
+        s->pml.nmax = nmax;
+        s->g.open = open;
         return PICGB_OK;
     }
 

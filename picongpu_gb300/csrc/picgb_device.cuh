@@ -172,7 +172,16 @@ namespace picgb
         float dx, dy, dz, dt, c, eps0;
         float rd[3]; // 1/dx, 1/dy, 1/dz
         int recipExact; // all cell sizes are powers of two: x / d == x * (1/d) exactly
+        int open; // bit a set: axis a is open (no wrap; PML fields, absorbing particles)
     };
+
+    // Index along an axis of n cells: periodic wrap, or -1 outside the box on an open axis.
+    __device__ __forceinline__ int wrapOrOutside(int i, int n, bool open)
+    {
+        if(open)
+            return (i < 0 || i >= n) ? -1 : i;
+        return i < 0 ? i + n : (i >= n ? i - n : i);
+    }
 
     // x / cellSize[d]: a multiplication by the exact reciprocal when the cell size is a
     // power of two (bit-identical to the IEEE division), the division otherwise.

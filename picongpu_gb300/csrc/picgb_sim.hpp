@@ -6,6 +6,7 @@
 #include "picgb.h"
 #include "picgb_device.cuh"
 #include "picgb_internal.hpp"
+#include "picgb_pml.hpp"
 
 #include <cuda_runtime.h>
 
@@ -134,6 +135,8 @@ struct picgb_sim
     bool ownStream = false;
     bool inEnsemble = false; // owned by a picgb_ensemble: not destroyed through picgb_destroy
     picgb::IncidentParams inc{}; // incident pulse (TF/SF surface), disabled by default
+    picgb::PmlDev pml{}; // open boundaries: convolution fields and coefficient tables (g.open != 0)
+    float* pmlTab = nullptr;
     uint64_t launches = 0;
     std::vector<std::unique_ptr<picgb::host::Species>> species;
     std::map<std::string, picgb::host::Entry> registry;

@@ -251,6 +251,23 @@ class Simulation:
         L.call("picgb_field_get", self.handle, name.encode(), ptrs)
         return a
 
+    # ------------------------------------------------------------ boundaries
+    def set_boundaries(self, open_axes=(False, False, False), pml_cells=((0, 0), (0, 0), (0, 0)), sigma_max=None,
+                       kappa_max=(1.0, 1.0, 1.0), alpha_max=(0.0, 0.0, 0.0), grading_order: float = 4.0,
+                       alpha_grading_order: float = 1.0) -> None:
+        """Open axes (PML fields, absorbing particles) as the reference's non-periodic boundaries
+        with fields/absorber/pml; sigma_max None: 0.8 (m + 1) c / cell edge per axis."""
+        b = L.BoundaryConfig()
+        for a in range(3):
+            b.open[a] = int(bool(open_axes[a]))
+            b.pml_cells[a][0], b.pml_cells[a][1] = int(pml_cells[a][0]), int(pml_cells[a][1])
+            b.sigma_max[a] = -1.0 if sigma_max is None else float(sigma_max[a])
+            b.kappa_max[a] = float(kappa_max[a])
+            b.alpha_max[a] = float(alpha_max[a])
+        b.grading_order = grading_order
+        b.alpha_grading_order = alpha_grading_order
+        L.call("picgb_set_boundaries", self.handle, ctypes.byref(b))
+
     # ------------------------------------------------------------ checkpoints
     def write_checkpoint(self, directory: str, step: int | None = None) -> str:
         """openPMD checkpoint of E, B and every species as iteration ``step`` (default: the

@@ -56,6 +56,7 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), si
  sizeof(picgb_particles), sizeof(picgb_buffer_desc), sizeof(picgb_plasma_init), sizeof(picgb_ensemble_config));
  printf("%zu %zu %zu %zu\n", sizeof(picgb_diff_config), sizeof(picgb_diff_species), sizeof(picgb_diff_state),
  sizeof(picgb_incident_field));
+ printf("%zu %zu\n", sizeof(picgb_openpmd_species), sizeof(picgb_boundary_config));
  return 0;}
 """
     with tempfile.TemporaryDirectory() as d:
@@ -66,7 +67,7 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(picgb_grid_config), si
         sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     mine = [ctypes.sizeof(t) for t in (_lib.GridConfig, _lib.SpeciesConfig, _lib.Particles, _lib.BufferDesc,
                                        _lib.PlasmaInit, _lib.EnsembleConfig, _lib.DiffConfig, _lib.DiffSpecies,
-                                       _lib.DiffState, _lib.IncidentField)]
+                                       _lib.DiffState, _lib.IncidentField, _lib.OpenPMDSpecies, _lib.BoundaryConfig)]
     assert mine == sizes
 
 

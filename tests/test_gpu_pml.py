@@ -1,0 +1,116 @@
+"""Open boundaries on the GPU (the reference's non-periodic axes with fields/absorber/pml): the
+PML Yee updates are bit-exact with the oracle, a plane pulse is absorbed, and particles that
+leave through an open face are absorbed while the others push and deposit as in the oracle."""
+import numpy as np
+import pytest
+
+import picongpu_gb300 as pg
+from plasma import random_field, random_particles
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def orc():
+    import oracle
+
+    oracle.build()
+    oracle.set_threads(1)
+    return oracle
+
+
+def _by_id(p):
+    o = np.argsort(p["id"], kind="stable")
+    return {k: (v[:, o] if v.ndim == 2 else v[o]) for k, v in p.items()}
+
+
+def test_pml_updates_match_oracle(orc):
+    g = pg.Grid(24, 40, 16)
+    gd = g.as_dict()
+    gd["open"] = 3  # x and y open, z periodic
+    cells = ((4, 0), (6, 6), (0, 0))
+    sigma, kappa, alpha = (3.0, 4.0, 0.0), (1.5, 2.0, 1.0), (0.1, 0.2, 0.0)
+    rng = np.random.default_rng(21)
+    E, B = random_field(gd, rng, 0.1), random_field(gd, rng, 0.1)
+    with pg.Simulation(g) as sim:
+        sim.set_boundaries(open_axes=(True, True, False), pml_cells=cells, sigma_max=sigma, kappa_max=kappa,
+                           alpha_max=alpha, grading_order=3.0, alpha_grading_order=1.0)
+        sim.set_field("E", E)
+        sim.set_field("B", B)
+        for _ in range(5):
+            sim.stage("current_reset")
+            sim.stage("field_before")
+            sim.stage("field_after")
+        Eg, Bg = sim.get_field("E"), sim.get_field("B")
+    p = orc.pml(cells, sigma, kappa, alpha, order=3.0, alpha_order=1.0)
+    psiE = np.zeros((6,) + E.shape[1:], np.float32)
+    psiB = np.zeros_like(psiE)
+    for _ in range(5):
+        orc.yee_b_half_open(gd, p, E, B, psiB, update=False)
+        orc.yee_e_open(gd, p, B, E, psiE)
+        orc.yee_b_half_open(gd, p, E, B, psiB, update=True)
+    assert np.array_equal(Eg, E) and np.array_equal(Bg, B)
+
+
+def test_pml_absorbs_a_plane_pulse():
+    """The pulse of the oracle test, with the default sigma (0.8 (m + 1) c / dy, m = 4)."""
+    import sys, os
+
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_oracle_pml import _energy, _interior, _pulse
+
+    g = pg.Grid(8, 96, 8)
+    E, B = _pulse(g.as_dict())
+    e0 = _energy(E, B)
+    with pg.Simulation(g) as sim:
+        sim.set_boundaries(open_axes=(False, True, False), pml_cells=((0, 0), (12, 12), (0, 0)))
+        sim.set_field("E", E)
+        sim.set_field("B", B)
+        sim.run(200)
+        Eg, Bg = sim.get_field("E"), sim.get_field("B")
+    assert _interior(Eg, Bg, 12, 84) < 1e-7 * e0
+
+
+def test_particles_absorbed_at_open_faces_and_the_rest_match_oracle(orc):
+    """Hot electrons (u_th 0.3) in a box open along x: particles crossing x = 0 or x = nx are
+    removed; positions, momenta and cells of the others match the oracle, and so does J away
+    from the open faces.  (The GPU deposits a leaving particle's current before removing it,
+    the oracle drops that particle; the difference stays within the shape's reach of the face,
+    inside the PML.)"""
+    g = pg.Grid(32, 16, 16)
+    gd = g.as_dict()
+    gd["open"] = 1
+    rng = np.random.default_rng(8)
+    p = random_particles(gd, 4, rng, u_th=0.3, weight=0.01)
+    E, B = random_field(gd, rng, 0.05), random_field(gd, rng, 0.05)
+    sp = pg.Species("e", -1.0, 1.0, shape="TSC", with_ids=True)
+    with pg.Simulation(g) as sim:
+        sim.set_boundaries(open_axes=(True, False, False), pml_cells=((4, 4), (0, 0), (0, 0)))
+        sim.add_species(sp)
+        sim.set_particles("e", p)
+        sim.set_field("E", E)
+        sim.set_field("B", B)
+        sim.stage("current_reset")
+        sim.stage("push")
+        assert sim.device_status() == 0
+        q = _by_id(sim.get_particles("e"))
+        Jg = sim.get_field("J")
+    ref = {k: v.copy() for k, v in p.items()}
+    orc.push(gd, sp.as_dict(), ref, E, B)
+    Jo = np.zeros_like(E)
+    orc.deposit(gd, sp.as_dict(), ref, Jo)
+    kept = ref["sc"] >= 0
+    assert 0 < (~kept).sum() < kept.sum()  # some, not all, left through the open faces
+    r = {k: v[..., kept] for k, v in ref.items()}
+    for k in ("id", "pos", "mom", "sc", "lcell"):
+        assert np.array_equal(q[k], r[k]), k
+    inner = (slice(None), slice(None), slice(None), slice(4, 28))
+    assert np.abs(Jg[inner] - Jo[inner]).max() <= 1e-6 * np.abs(Jo).max()
+
+
+def test_ensemble_boxes_stay_periodic():
+    ens = pg.Ensemble([(16, 16, 16)])
+    with pytest.raises(pg.PicError) as e:
+        ens.box(0).set_boundaries(open_axes=(True, False, False), pml_cells=((4, 4), (0, 0), (0, 0)))
+    assert e.value.code == pg._lib.ERR_UNSUPPORTED
+    ens.close()

@@ -1,0 +1,86 @@
+"""The oracle's open boundaries and PML (fields/absorber/pml/Pml.kernel): a plane pulse that runs
+into the PML of an open axis is absorbed, the same pulse against an open face without PML
+is reflected by the zero exterior field, and particles leaving through an open face are
+absorbed."""
+import numpy as np
+import pytest
+
+from plasma import grid
+
+
+def _pulse(g, y0=24.0, width=4.0, amp=1.0):
+    """E_x and B_z of a pulse travelling along +y (E x B along +y), on the Yee positions."""
+    E = np.zeros((3, g["nz"], g["ny"], g["nx"]), np.float32)
+    B = np.zeros_like(E)
+    y = np.arange(g["ny"], dtype=np.float64)
+    ex = amp * np.exp(-(((y - y0) / width) ** 2))  # E_x at y = j
+    bz = -amp * np.exp(-(((y + 0.5 - y0 - 0.5 * g["dt"]) / width) ** 2))  # B_z at y = j + 1/2, t = -dt/2
+    E[0] = ex[None, :, None]
+    B[2] = bz[None, :, None]
+    return E, B
+
+
+def _energy(E, B):
+    return float((E.astype(np.float64) ** 2).sum() + (B.astype(np.float64) ** 2).sum())
+
+
+def _run(orc, g, p, E, B, steps):
+    psiE = np.zeros((6,) + E.shape[1:], np.float32)
+    psiB = np.zeros_like(psiE)
+    for _ in range(steps):
+        orc.yee_b_half_open(g, p, E, B, psiB, update=False)
+        orc.yee_e_open(g, p, B, E, psiE)
+        orc.yee_b_half_open(g, p, E, B, psiB, update=True)
+    return E, B
+
+
+def _interior(E, B, lo, hi):
+    prof = (E.astype(np.float64) ** 2).sum(axis=(0, 1, 3)) + (B.astype(np.float64) ** 2).sum(axis=(0, 1, 3))
+    return float(prof[lo:hi].sum())
+
+
+@pytest.mark.parametrize("alpha", [0.0, 0.2])
+def test_pml_absorbs_a_plane_pulse(orc, alpha):
+    """12-cell PML, sigma_opt = 0.8 (m + 1) c / dy, m = 4 (param/fieldAbsorber.param): after the pulse
+    has run ~115 cells (into the PML and, if reflected, back) the region between the layers holds
+    less than 1e-7 of its energy.  With alpha > 0 the low frequencies linger inside the layer."""
+    g = grid(n=(8, 96, 8), sc=(8, 8, 4))
+    g["open"] = 2  # y open
+    m = 4.0
+    p = orc.pml(((0, 0), (12, 12), (0, 0)), [0.0, 0.8 * (m + 1) * g["c"] / g["dy"], 0.0], [1.0] * 3, [0.0, alpha, 0.0],
+                order=m)
+    E, B = _pulse(g)
+    e0 = _energy(E, B)
+    E, B = _run(orc, g, p, E, B, 200)
+    assert _interior(E, B, 12, 84) < 1e-7 * e0
+
+
+def test_open_face_without_pml_reflects(orc):
+    """Zero exterior fields act as a conductor: with no PML cells the pulse comes back whole."""
+    g = grid(n=(8, 96, 8), sc=(8, 8, 4))
+    g["open"] = 2
+    p = orc.pml(((0, 0), (0, 0), (0, 0)), [0.0] * 3, [1.0] * 3, [0.0] * 3)
+    E, B = _pulse(g)
+    e0 = _energy(E, B)
+    E, B = _run(orc, g, p, E, B, 200)
+    assert _energy(E, B) > 0.9 * e0
+
+
+def test_particles_leave_through_an_open_face(orc):
+    g = grid(n=(16, 16, 8), sc=(8, 8, 4))
+    g["open"] = 1  # x open
+    n = 64
+    rng = np.random.default_rng(3)
+    cx = np.where(np.arange(n) % 2 == 0, 15, 0)  # edge cells
+    cy, cz = rng.integers(0, 16, n), rng.integers(0, 8, n)
+    sc = (cx // 8) + 2 * ((cy // 8) + 2 * (cz // 4))
+    lc = (cx % 8) + 8 * ((cy % 8) + 8 * (cz % 4))
+    pos = rng.random((3, n), dtype=np.float32)
+    pos[0] = np.where(cx == 15, 0.95, 0.05).astype(np.float32)
+    u = np.where(cx == 15, 0.5, -0.5)  # towards the nearest x face
+    p = dict(pos=pos, mom=np.stack([u, np.zeros(n), np.zeros(n)]).astype(np.float32), w=np.ones(n, np.float32),
+             sc=sc.astype(np.int32), lcell=lc.astype(np.uint16))
+    sp = dict(charge=-1.0, mass=1.0, shape=2, pusher=1, current=1)  # free streaming
+    zero = np.zeros((3, 8, 16, 16), np.float32)
+    orc.push(g, sp, p, zero, zero)
+    assert (p["sc"] < 0).all()  # every particle crossed its open face and was absorbed
