@@ -72,15 +72,27 @@ namespace picgb
         GridParams const& g,
         size_t ncell)
     {
+        bool const anyOpen = g.open != 0; // uniform: the periodic box takes the plain wrap
         for(int t = threadIdx.x; t < TT; t += blockDim.x)
         {
             int const tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
-            int const gx = wrapOrOutside(ox + tx, g.nx, g.open & 1), gy = wrapOrOutside(oy + ty, g.ny, g.open & 2),
-                      gz = wrapOrOutside(oz + tz, g.nz, g.open & 4);
-            if((gx | gy | gz) < 0) // beyond an open face the fields are zero
+            int gx, gy, gz;
+            if(!anyOpen)
             {
-                dst[t] = dst[TT + t] = dst[2 * TT + t] = 0.0f;
-                continue;
+                gx = wrapi(ox + tx, g.nx);
+                gy = wrapi(oy + ty, g.ny);
+                gz = wrapi(oz + tz, g.nz);
+            }
+            else
+            {
+                gx = wrapOrOutside(ox + tx, g.nx, g.open & 1);
+                gy = wrapOrOutside(oy + ty, g.ny, g.open & 2);
+                gz = wrapOrOutside(oz + tz, g.nz, g.open & 4);
+                if((gx | gy | gz) < 0) // beyond an open face the fields are zero
+                {
+                    dst[t] = dst[TT + t] = dst[2 * TT + t] = 0.0f;
+                    continue;
+                }
             }
             size_t const gi = size_t(gx) + size_t(g.nx) * (size_t(gy) + size_t(g.ny) * size_t(gz));
             dst[t] = __ldg(src + gi);
@@ -104,6 +116,7 @@ namespace picgb
         size_t ncell,
         JFixed const& f)
     {
+        bool const anyOpen = g.open != 0;
         for(int t = threadIdx.x; t < TT; t += blockDim.x)
         {
             float const vx = tileValue<TT>(Js, t, f), vy = tileValue<TT>(Js, TT + t, f),
@@ -111,10 +124,21 @@ namespace picgb
             if(vx == 0.0f && vy == 0.0f && vz == 0.0f)
                 continue;
             int const tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
-            int const gx = wrapOrOutside(ox + tx, g.nx, g.open & 1), gy = wrapOrOutside(oy + ty, g.ny, g.open & 2),
-                      gz = wrapOrOutside(oz + tz, g.nz, g.open & 4);
-            if((gx | gy | gz) < 0)
-                continue;
+            int gx, gy, gz;
+            if(!anyOpen)
+            {
+                gx = wrapi(ox + tx, g.nx);
+                gy = wrapi(oy + ty, g.ny);
+                gz = wrapi(oz + tz, g.nz);
+            }
+            else
+            {
+                gx = wrapOrOutside(ox + tx, g.nx, g.open & 1);
+                gy = wrapOrOutside(oy + ty, g.ny, g.open & 2);
+                gz = wrapOrOutside(oz + tz, g.nz, g.open & 4);
+                if((gx | gy | gz) < 0)
+                    continue;
+            }
             size_t const gi = size_t(gx) + size_t(g.nx) * (size_t(gy) + size_t(g.ny) * size_t(gz));
             if(vx != 0.0f)
                 atomicAdd(J + gi, vx);
