@@ -210,6 +210,12 @@ namespace
     }
 
     // ---- the writer
+    // names of the six components of a PML convolution field (psi.ab: field component a,
+    // derivative along b), in the order of the device arrays
+    char const* const kPsiNames[6] = {"xy", "xz", "yx", "yz", "zx", "zy"};
+
+    // psiE, psiB: the PML convolution fields (6 host arrays of nx*ny*nz floats each) written as
+    // the extra meshes "PmlPsiE" and "PmlPsiB", or null
     void writeSeries(
         char const* dir,
         uint32_t step,
@@ -217,7 +223,9 @@ namespace
         float const* const* E,
         float const* const* B,
         int nspecies,
-        picgb_openpmd_species const* species)
+        picgb_openpmd_species const* species,
+        float const* const* psiE = nullptr,
+        float const* const* psiB = nullptr)
     {
         int sc[3];
         checkGrid(&g, sc);
@@ -291,6 +299,32 @@ namespace
                 attr(comp, "position", vec({st[0], st[1], st[2]}), "VEC_FLOAT");
                 attr(comp, "unitSI", 1.0, "DOUBLE");
                 std::string const file = std::string("meshes_") + name + "_" + kComp[c] + ".bin";
+                externalDataset(comp, "FLOAT", meshExtent, 3, file);
+                writeRaw(base + "/" + file, data[c], sizeof(float) * ncell);
+            }
+        }
+
+        for(int f = 0; f < 2 && psiE && psiB; ++f)
+        {
+            // not an openPMD record of the reference: the state of the open boundaries' PML
+            char const* name = f == 0 ? "PmlPsiE" : "PmlPsiB";
+            float const* const* data = f == 0 ? psiE : psiB;
+            Value& m = child(meshes, name);
+            attr(m, "geometry", "cartesian", "STRING");
+            attr(m, "dataOrder", "C", "STRING");
+            attr(m, "axisLabels", strings({"z", "y", "x"}), "VEC_STRING");
+            attr(m, "gridSpacing", vec({g.dz, g.dy, g.dx}), "VEC_DOUBLE");
+            attr(m, "gridGlobalOffset", vec({0.0, 0.0, 0.0}), "VEC_DOUBLE");
+            attr(m, "gridUnitSI", 1.0, "DOUBLE");
+            attr(m, "unitDimension", f == 0 ? dims(1, 1, -3, -1) : dims(0, 1, -2, -1), "ARR_DBL_7");
+            attr(m, "timeOffset", 0.0, "FLOAT");
+            for(int c = 0; c < 6; ++c)
+            {
+                Value& comp = child(m, kPsiNames[c]);
+                float const* st = f == 0 ? kStagE[c / 2] : kStagB[c / 2];
+                attr(comp, "position", vec({st[0], st[1], st[2]}), "VEC_FLOAT");
+                attr(comp, "unitSI", 1.0, "DOUBLE");
+                std::string const file = std::string("meshes_") + name + "_" + kPsiNames[c] + ".bin";
                 externalDataset(comp, "FLOAT", meshExtent, 3, file);
                 writeRaw(base + "/" + file, data[c], sizeof(float) * ncell);
             }
@@ -524,6 +558,42 @@ namespace
         h->n = n;
     }
 
+    // Reads the components `comps` of mesh `name`; returns false when the mesh is absent and
+    // `optional` is set.
+    bool readMeshComponents(
+        char const* dir,
+        uint32_t step,
+        char const* name,
+        picgb_grid_config const* g,
+        float* const* host,
+        char const* const* comps,
+        int ncomp,
+        bool optional)
+    {
+        int sc[3];
+        checkGrid(g, sc);
+        Index const x = openIndex(dir, step);
+        Value const* ms = x.it->find("meshes");
+        Value const* m = ms ? ms->find(name) : nullptr;
+        if(!m)
+        {
+            if(optional)
+                return false;
+            throw std::out_of_range(std::string("mesh '") + name + "' is not in the checkpoint");
+        }
+        uint64_t const ncell = uint64_t(g->nx) * g->ny * g->nz;
+        double const want[3] = {double(g->nz), double(g->ny), double(g->nx)};
+        for(int c = 0; c < ncomp; ++c)
+        {
+            Value const& comp = m->at(comps[c]);
+            auto const& e = comp.at("extent").items();
+            if(e.size() != 3 || e[0].number() != want[0] || e[1].number() != want[1] || e[2].number() != want[2])
+                throw IoError(std::string("mesh ") + name + " has another extent than the grid");
+            readExternal(dir, step, comp, "FLOAT", host[c], sizeof(float), ncell);
+        }
+        return true;
+    }
+
     void readMesh(char const* dir, uint32_t step, char const* name, picgb_grid_config const* g, float* const* host)
     {
         int sc[3];
@@ -706,7 +776,25 @@ extern "C"
                         if(int r = picgb_species_get(s, int32_t(i), &p))
                             return r;
                 }
-                writeSeries(dir, step, s->cfg, pe, pb, int(out.size()), out.data());
+                // the PML convolution fields of open boundaries, so that a restart continues exactly
+                std::vector<float> psi;
+                float* qe[6] = {};
+                float* qb[6] = {};
+                if(s->g.open)
+                {
+                    psi.resize(12 * ncell);
+                    CUDA_TRY(cudaMemcpyAsync(psi.data(), s->pml.psiE, sizeof(float) * 6 * ncell, cudaMemcpyDeviceToHost, s->stream));
+                    CUDA_TRY(cudaMemcpyAsync(psi.data() + 6 * ncell, s->pml.psiB, sizeof(float) * 6 * ncell, cudaMemcpyDeviceToHost,
+                                             s->stream));
+                    CUDA_TRY(cudaStreamSynchronize(s->stream));
+                    for(int c = 0; c < 6; ++c)
+                    {
+                        qe[c] = psi.data() + c * ncell;
+                        qb[c] = psi.data() + (6 + c) * ncell;
+                    }
+                }
+                writeSeries(dir, step, s->cfg, pe, pb, int(out.size()), out.data(), s->g.open ? qe : nullptr,
+                            s->g.open ? qb : nullptr);
                 return int(PICGB_OK);
             });
     }
@@ -731,6 +819,21 @@ extern "C"
                 std::fill(f.begin(), f.end(), 0.0f);
                 if(int r = picgb_field_set(s, "J", p3))
                     return r;
+                if(s->g.open)
+                {
+                    // PML state of the checkpoint if it has one (set_boundaries zeroed it before)
+                    std::vector<float> psi(6 * ncell);
+                    float* q[6];
+                    for(int c = 0; c < 6; ++c)
+                        q[c] = psi.data() + c * ncell;
+                    for(int fld = 0; fld < 2; ++fld)
+                        if(readMeshComponents(dir, step, fld == 0 ? "PmlPsiE" : "PmlPsiB", &s->cfg, q, kPsiNames, 6, true))
+                        {
+                            CUDA_TRY(cudaMemcpyAsync(fld == 0 ? s->pml.psiE : s->pml.psiB, psi.data(), sizeof(float) * 6 * ncell,
+                                                     cudaMemcpyHostToDevice, s->stream));
+                            CUDA_TRY(cudaStreamSynchronize(s->stream));
+                        }
+                }
                 Index const x = openIndex(dir, step);
                 for(size_t i = 0; i < s->species.size(); ++i)
                 {

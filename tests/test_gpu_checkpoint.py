@@ -132,3 +132,33 @@ def test_restart_needs_every_species(tmp_path):
         with pytest.raises(pg.PicError) as e:
             c.read_checkpoint(d, 0)
         assert e.value.code == pg._lib.ERR_IO
+
+
+def test_restart_with_open_boundaries_is_exact(tmp_path):
+    """A pulse in a box open along y with a PML: the checkpoint keeps the PML's convolution
+    fields, so the fields after a restart continue bit for bit (no particles, no atomics)."""
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_oracle_pml import _pulse
+
+    d = str(tmp_path / "ckpt")
+    g = pg.Grid(8, 96, 8)
+    E, B = _pulse(g.as_dict(), y0=70.0)
+    bnd = dict(open_axes=(False, True, False), pml_cells=((0, 0), (12, 12), (0, 0)), alpha_max=(0.0, 0.2, 0.0))
+    with pg.Simulation(g) as a:
+        a.set_boundaries(**bnd)
+        a.set_field("E", E)
+        a.set_field("B", B)
+        a.run(20)  # the pulse is inside the positive PML now
+        a.write_checkpoint(d)
+        a.run(20)
+        Ea, Ba = a.get_field("E"), a.get_field("B")
+    with pg.Simulation(g) as b:
+        b.set_boundaries(**bnd)
+        b.read_checkpoint(d, 20)
+        b.run(20)
+        Eb, Bb = b.get_field("E"), b.get_field("B")
+    assert np.array_equal(Ea, Eb) and np.array_equal(Ba, Bb)
+    assert os.path.exists(os.path.join(d, "simData_20", "meshes_PmlPsiB_zy.bin"))
