@@ -424,22 +424,32 @@ extern "C"
      * without the low-energy branch); synchronises the stream. */
     int picgb_diff_kinetic_energy(picgb_diff* d, const picgb_diff_state* state, int32_t species, double* out, void* stream);
 
-    /* ------------------------------------------------------------ open boundaries and PML
-     * The reference's non-periodic boundaries (`--periodic 0` on an axis): fields absorbed by
-     * the convolutional PML of fields/absorber/pml/Pml.kernel (Yee updates of
-     * fields/absorber/pml/Pml.kernel:400-590, coefficients :130-267, parameters of
-     * param/fieldAbsorber.param), particles absorbed (deleted) when they leave the box.  Beyond
-     * the box the fields are zero.  Values are in the simulation's units: sigma and alpha are
-     * the reference's "normalized" values (divided by eps0), in 1/time. */
+    /* ------------------------------------------------------------ open boundaries and absorbers
+     * The reference's non-periodic boundaries (`--periodic 0` on an axis): fields absorbed in
+     * layers at the open faces, particles absorbed (deleted) when they leave the box.  Beyond
+     * the box the fields are zero.  Absorbers (param/fieldAbsorber.param):
+     *  - PICGB_ABSORBER_PML: the convolutional PML of fields/absorber/pml (Yee updates of
+     *    Pml.kernel:400-590, coefficients :130-267); sigma and alpha are the reference's
+     *    "normalized" values (divided by eps0), in 1/time of the simulation's units;
+     *  - PICGB_ABSORBER_EXPONENTIAL: fields/absorber/exponential/Exponential.kernel, a cell at
+     *    depth f (1 .. thickness - 1 cells from the layer's inner edge) is multiplied by
+     *    exp(-strength f) after each E update and after the B half update that follows it. */
+    enum picgb_absorber
+    {
+        PICGB_ABSORBER_PML = 0,
+        PICGB_ABSORBER_EXPONENTIAL = 1
+    };
     typedef struct picgb_boundary_config
     {
-        int32_t open[3]; /* per axis: 0 periodic, 1 open (PML fields, absorbing particles) */
-        int32_t pml_cells[3][2]; /* PML thickness per face (negative, positive) of an open axis */
-        float sigma_max[3]; /* normalized sigma max; < 0: 0.8 (m + 1) c / cell edge (fieldAbsorber.param) */
-        float kappa_max[3]; /* >= 1 */
-        float alpha_max[3]; /* normalized alpha max, >= 0 */
-        float grading_order; /* sigma and kappa grading order m (fieldAbsorber.param: 4) */
-        float alpha_grading_order; /* alpha grading order (fieldAbsorber.param: 1) */
+        int32_t open[3]; /* per axis: 0 periodic, 1 open (absorbing layers, absorbing particles) */
+        int32_t absorber; /* enum picgb_absorber */
+        int32_t thickness[3][2]; /* absorber thickness per face (negative, positive) of an open axis */
+        float sigma_max[3]; /* PML: normalized sigma max; < 0: 0.8 (m + 1) c / cell edge */
+        float kappa_max[3]; /* PML: >= 1 */
+        float alpha_max[3]; /* PML: normalized alpha max, >= 0 */
+        float grading_order; /* PML: sigma and kappa grading order m (fieldAbsorber.param: 4) */
+        float alpha_grading_order; /* PML: alpha grading order (fieldAbsorber.param: 1) */
+        float strength[3][2]; /* exponential: strength per face (fieldAbsorber.param: 1e-3) */
     } picgb_boundary_config;
     /* Sets the boundaries (all periodic at creation); resets the PML's convolution fields. Not
      * for ensemble boxes.  The charge-residual diagnostic stays periodic, so with an open axis

@@ -51,9 +51,9 @@ class OpenPMDSpecies(ctypes.Structure):
 
 
 class BoundaryConfig(ctypes.Structure):
-    _fields_ = [("open", c_int * 3), ("pml_cells", (c_int * 2) * 3), ("sigma_max", c_float * 3),
+    _fields_ = [("open", c_int * 3), ("absorber", c_int), ("thickness", (c_int * 2) * 3), ("sigma_max", c_float * 3),
                 ("kappa_max", c_float * 3), ("alpha_max", c_float * 3), ("grading_order", c_float),
-                ("alpha_grading_order", c_float)]
+                ("alpha_grading_order", c_float), ("strength", (c_float * 2) * 3)]
 
 
 class BufferDesc(ctypes.Structure):

@@ -152,6 +152,36 @@ namespace picgb
         }
     }
 
+    // The exponential absorber (fields/absorber/exponential/Exponential.kernel:50-90) on one field.
+    __global__ void __launch_bounds__(kPmlBX) kAbsorbExponential(float* __restrict__ F, GridParams g, float const* __restrict__ damp, int nmax)
+    {
+        int const x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+        if(x >= g.nx)
+            return;
+        float const f[3] = {__ldg(damp + x), __ldg(damp + nmax + y), __ldg(damp + 2 * nmax + z)};
+        if(f[0] == 1.0f && f[1] == 1.0f && f[2] == 1.0f)
+            return;
+        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+        size_t const i = cellIndex(g, x, y, z);
+#pragma unroll
+        for(int c = 0; c < 3; ++c)
+        {
+            float v = F[c * nc + i];
+#pragma unroll
+            for(int a = 0; a < 3; ++a)
+                if(f[a] != 1.0f)
+                    v = fm(v, f[a]);
+            F[c * nc + i] = v;
+        }
+    }
+
+    cudaError_t launchAbsorbExponential(float* F, GridParams const& g, float const* damp, int nmax, cudaStream_t stream)
+    {
+        dim3 const grid((g.nx + kPmlBX - 1) / kPmlBX, g.ny, g.nz);
+        kAbsorbExponential<<<grid, kPmlBX, 0, stream>>>(F, g, damp, nmax);
+        return cudaGetLastError();
+    }
+
     cudaError_t launchYeeBHalfOpen(float const* E, float* B, GridParams const& g, PmlDev const& p, bool updatePsi, cudaStream_t stream)
     {
         dim3 const grid((g.nx + kPmlBX - 1) / kPmlBX, g.ny, g.nz);

@@ -493,6 +493,7 @@ int picgb::host::destroySim(picgb_sim* s)
     dfree(s->pml.psiE);
     dfree(s->pml.psiB);
     dfree(s->pmlTab);
+    dfree(s->expDamp);
     if(s->hostStatus)
         cudaFreeHost(s->hostStatus);
     profFlush(s);
@@ -902,6 +903,8 @@ extern "C"
                              : launchYeeE(s->B, s->E, J, s->coeffJ(), s->g, s->stream);
         }));
         CUDA_TRY(launchIncidentE(s->E, s->g, s->inc, t + 0.5f * s->cfg.dt, s->stream)); // incident B at t + dt/2
+        if(s->expDamp) // exponential absorber on E (FDTDBase.hpp:121-124)
+            CUDA_TRY(launchAbsorbExponential(s->E, s->g, s->expDamp, s->pml.nmax, s->stream));
         return PICGB_OK;
     }
 
@@ -947,6 +950,8 @@ extern "C"
                              : launchYeeBHalf(s->E, s->B, s->g, s->stream);
         }));
         CUDA_TRY(launchIncidentB(s->B, s->g, s->inc, float(double(step + 1) * s->cfg.dt), s->stream)); // E at t + dt
+        if(s->expDamp) // exponential absorber on B (FDTDBase.hpp:178-182)
+            CUDA_TRY(launchAbsorbExponential(s->B, s->g, s->expDamp, s->pml.nmax, s->stream));
         return PICGB_OK;
     }
 
@@ -967,18 +972,23 @@ extern "C"
         {
             if(b->open[a] != 0 && b->open[a] != 1)
                 return fail(PICGB_ERR_INVALID, "open[%d] must be 0 or 1", a);
+            if(b->absorber != PICGB_ABSORBER_PML && b->absorber != PICGB_ABSORBER_EXPONENTIAL)
+                return fail(PICGB_ERR_INVALID, "unknown absorber %d", int(b->absorber));
             if(!b->open[a])
                 continue;
-            int const neg = b->pml_cells[a][0], pos = b->pml_cells[a][1];
+            int const neg = b->thickness[a][0], pos = b->thickness[a][1];
             if(neg < 0 || pos < 0 || neg + pos > cells[a])
-                return fail(PICGB_ERR_INVALID, "PML of %d + %d cells does not fit %d cells on axis %d", neg, pos,
+                return fail(PICGB_ERR_INVALID, "absorber of %d + %d cells does not fit %d cells on axis %d", neg, pos,
                             cells[a], a);
+            if(!(b->strength[a][0] >= 0.0f) || !(b->strength[a][1] >= 0.0f))
+                return fail(PICGB_ERR_INVALID, "exponential absorber strengths must be >= 0");
             if(!(m >= 0.0) || !(ma >= 0.0) || !(b->kappa_max[a] >= 1.0f) || !(b->alpha_max[a] >= 0.0f))
                 return fail(PICGB_ERR_INVALID, "PML needs grading orders >= 0, kappa_max >= 1 and alpha_max >= 0");
             ax[a].open = true;
             ax[a].cells = cells[a];
-            ax[a].neg = neg;
-            ax[a].pos = pos;
+            bool const pml = b->absorber == PICGB_ABSORBER_PML;
+            ax[a].neg = pml ? neg : 0; // without PML layers the open Yee update is the plain one
+            ax[a].pos = pml ? pos : 0;
             // default sigma: SIGMA_OPT = 0.8 (m + 1) / (Z0 d), normalized by eps0: 0.8 (m + 1) c / d
             ax[a].sigmaMax = b->sigma_max[a] < 0.0f ? 0.8 * (m + 1.0) * double(s->cfg.c) / double(edge[a])
                                                      : double(b->sigma_max[a]);
@@ -993,6 +1003,7 @@ extern "C"
         dfree(s->pml.psiE);
         dfree(s->pml.psiB);
         dfree(s->pmlTab);
+        dfree(s->expDamp);
         s->pml = PmlDev{};
         s->g.open = 0; // set below once the PML state exists
         if(!open)
@@ -1001,10 +1012,19 @@ extern "C"
         std::vector<float> const tab = pmlTables(ax, double(s->cfg.dt), nmax);
         CUDA_TRY(dalloc(s->pmlTab, tab.size()));
         CUDA_TRY(cudaMemcpy(s->pmlTab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice));
-        CUDA_TRY(dalloc(s->pml.psiE, 6 * s->ncell));
-        CUDA_TRY(dalloc(s->pml.psiB, 6 * s->ncell));
-        CUDA_TRY(cudaMemsetAsync(s->pml.psiE, 0, sizeof(float) * 6 * s->ncell, s->stream));
-        CUDA_TRY(cudaMemsetAsync(s->pml.psiB, 0, sizeof(float) * 6 * s->ncell, s->stream));
+        if(b->absorber == PICGB_ABSORBER_PML)
+        {
+            CUDA_TRY(dalloc(s->pml.psiE, 6 * s->ncell));
+            CUDA_TRY(dalloc(s->pml.psiB, 6 * s->ncell));
+            CUDA_TRY(cudaMemsetAsync(s->pml.psiE, 0, sizeof(float) * 6 * s->ncell, s->stream));
+            CUDA_TRY(cudaMemsetAsync(s->pml.psiB, 0, sizeof(float) * 6 * s->ncell, s->stream));
+        }
+        else
+        {
+            std::vector<float> const damp = expDampTable(cells, b->thickness, b->strength, open, nmax);
+            CUDA_TRY(dalloc(s->expDamp, damp.size()));
+            CUDA_TRY(cudaMemcpy(s->expDamp, damp.data(), sizeof(float) * damp.size(), cudaMemcpyHostToDevice));
+        }
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         s->pml.tab = s->pmlTab;
         s->pml.nmax = nmax;

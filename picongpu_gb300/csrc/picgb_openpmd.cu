@@ -780,7 +780,7 @@ extern "C"
                 std::vector<float> psi;
                 float* qe[6] = {};
                 float* qb[6] = {};
-                if(s->g.open)
+                if(s->g.open && s->pml.psiE)
                 {
                     psi.resize(12 * ncell);
                     CUDA_TRY(cudaMemcpyAsync(psi.data(), s->pml.psiE, sizeof(float) * 6 * ncell, cudaMemcpyDeviceToHost, s->stream));
@@ -793,8 +793,9 @@ extern "C"
                         qb[c] = psi.data() + (6 + c) * ncell;
                     }
                 }
-                writeSeries(dir, step, s->cfg, pe, pb, int(out.size()), out.data(), s->g.open ? qe : nullptr,
-                            s->g.open ? qb : nullptr);
+                bool const withPsi = s->g.open && s->pml.psiE;
+                writeSeries(dir, step, s->cfg, pe, pb, int(out.size()), out.data(), withPsi ? qe : nullptr,
+                            withPsi ? qb : nullptr);
                 return int(PICGB_OK);
             });
     }
@@ -819,7 +820,7 @@ extern "C"
                 std::fill(f.begin(), f.end(), 0.0f);
                 if(int r = picgb_field_set(s, "J", p3))
                     return r;
-                if(s->g.open)
+                if(s->g.open && s->pml.psiE)
                 {
                     // PML state of the checkpoint if it has one (set_boundaries zeroed it before)
                     std::vector<float> psi(6 * ncell);

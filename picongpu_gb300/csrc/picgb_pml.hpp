@@ -86,6 +86,34 @@ namespace picgb
         return t;
     }
 
+    // Damping factor per axis and cell of the exponential absorber (Exponential.kernel:50-90): a
+    // cell f = 1 .. thickness - 1 cells deep into a face's layer (counted from the layer's inner
+    // edge) is multiplied by exp(-strength f); 1 elsewhere.  Rounded to float from double.
+    inline std::vector<float> expDampTable(int const cells[3], int const thick[3][2], float const strength[3][2], int open, int nmax)
+    {
+        std::vector<float> t(size_t(3) * nmax, 1.0f);
+        for(int a = 0; a < 3; ++a)
+        {
+            if(!(open & (1 << a)))
+                continue;
+            for(int i = 0; i < cells[a]; ++i)
+            {
+                double d = 1.0;
+                int const fNeg = thick[a][0] - 1 - i;
+                if(fNeg > 0)
+                    d *= std::exp(-double(strength[a][0]) * double(fNeg));
+                int const fPos = i - cells[a] + thick[a][1];
+                if(fPos > 0)
+                    d *= std::exp(-double(strength[a][1]) * double(fPos));
+                t[size_t(a) * nmax + i] = float(d);
+            }
+        }
+        return t;
+    }
+
+    // F *= damp_x(x), then *= damp_y(y), then *= damp_z(z), each factor != 1 one rounding step
+    cudaError_t launchAbsorbExponential(float* F, GridParams const& g, float const* damp, int nmax, cudaStream_t stream);
+
     cudaError_t launchYeeBHalfOpen(float const* E, float* B, GridParams const& g, PmlDev const& p, bool updatePsi, cudaStream_t stream);
     cudaError_t launchYeeEOpen(
         float const* B,

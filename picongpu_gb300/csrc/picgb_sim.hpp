@@ -137,6 +137,7 @@ struct picgb_sim
     picgb::IncidentParams inc{}; // incident pulse (TF/SF surface), disabled by default
     picgb::PmlDev pml{}; // open boundaries: convolution fields and coefficient tables (g.open != 0)
     float* pmlTab = nullptr;
+    float* expDamp = nullptr; // exponential absorber: damping factors [3][pml.nmax], or null
     uint64_t launches = 0;
     std::vector<std::unique_ptr<picgb::host::Species>> species;
     std::map<std::string, picgb::host::Entry> registry;

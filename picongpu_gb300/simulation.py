@@ -252,18 +252,23 @@ class Simulation:
         return a
 
     # ------------------------------------------------------------ boundaries
-    def set_boundaries(self, open_axes=(False, False, False), pml_cells=((0, 0), (0, 0), (0, 0)), sigma_max=None,
-                       kappa_max=(1.0, 1.0, 1.0), alpha_max=(0.0, 0.0, 0.0), grading_order: float = 4.0,
-                       alpha_grading_order: float = 1.0) -> None:
-        """Open axes (PML fields, absorbing particles) as the reference's non-periodic boundaries
-        with fields/absorber/pml; sigma_max None: 0.8 (m + 1) c / cell edge per axis."""
+    def set_boundaries(self, open_axes=(False, False, False), thickness=((0, 0), (0, 0), (0, 0)), absorber="PML",
+                       sigma_max=None, kappa_max=(1.0, 1.0, 1.0), alpha_max=(0.0, 0.0, 0.0), grading_order: float = 4.0,
+                       alpha_grading_order: float = 1.0, strength=((1e-3, 1e-3),) * 3) -> None:
+        """Open axes (absorbing layers, absorbing particles) as the reference's non-periodic
+        boundaries; absorber "PML" (fields/absorber/pml; sigma_max None: 0.8 (m + 1) c / cell edge)
+        or "Exponential" (fields/absorber/exponential, damping strength per face)."""
+        if absorber not in ("PML", "Exponential"):
+            raise ValueError(f"unknown absorber {absorber!r}: 'PML' or 'Exponential'")
         b = L.BoundaryConfig()
+        b.absorber = 0 if absorber == "PML" else 1
         for a in range(3):
             b.open[a] = int(bool(open_axes[a]))
-            b.pml_cells[a][0], b.pml_cells[a][1] = int(pml_cells[a][0]), int(pml_cells[a][1])
+            b.thickness[a][0], b.thickness[a][1] = int(thickness[a][0]), int(thickness[a][1])
             b.sigma_max[a] = -1.0 if sigma_max is None else float(sigma_max[a])
             b.kappa_max[a] = float(kappa_max[a])
             b.alpha_max[a] = float(alpha_max[a])
+            b.strength[a][0], b.strength[a][1] = float(strength[a][0]), float(strength[a][1])
         b.grading_order = grading_order
         b.alpha_grading_order = alpha_grading_order
         L.call("picgb_set_boundaries", self.handle, ctypes.byref(b))

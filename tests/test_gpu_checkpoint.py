@@ -146,7 +146,7 @@ def test_restart_with_open_boundaries_is_exact(tmp_path):
     d = str(tmp_path / "ckpt")
     g = pg.Grid(8, 96, 8)
     E, B = _pulse(g.as_dict(), y0=70.0)
-    bnd = dict(open_axes=(False, True, False), pml_cells=((0, 0), (12, 12), (0, 0)), alpha_max=(0.0, 0.2, 0.0))
+    bnd = dict(open_axes=(False, True, False), thickness=((0, 0), (12, 12), (0, 0)), alpha_max=(0.0, 0.2, 0.0))
     with pg.Simulation(g) as a:
         a.set_boundaries(**bnd)
         a.set_field("E", E)

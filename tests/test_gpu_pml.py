@@ -1,4 +1,4 @@
-"""Open boundaries on the GPU (the reference's non-periodic axes with fields/absorber/pml): the
+"""Open boundaries on the GPU (the reference's non-periodic axes with fields/absorber): the
 PML Yee updates are bit-exact with the oracle, a plane pulse is absorbed, and particles that
 leave through an open face are absorbed while the others push and deposit as in the oracle."""
 import numpy as np
@@ -33,7 +33,7 @@ def test_pml_updates_match_oracle(orc):
     rng = np.random.default_rng(21)
     E, B = random_field(gd, rng, 0.1), random_field(gd, rng, 0.1)
     with pg.Simulation(g) as sim:
-        sim.set_boundaries(open_axes=(True, True, False), pml_cells=cells, sigma_max=sigma, kappa_max=kappa,
+        sim.set_boundaries(open_axes=(True, True, False), thickness=cells, sigma_max=sigma, kappa_max=kappa,
                            alpha_max=alpha, grading_order=3.0, alpha_grading_order=1.0)
         sim.set_field("E", E)
         sim.set_field("B", B)
@@ -63,7 +63,7 @@ def test_pml_absorbs_a_plane_pulse():
     E, B = _pulse(g.as_dict())
     e0 = _energy(E, B)
     with pg.Simulation(g) as sim:
-        sim.set_boundaries(open_axes=(False, True, False), pml_cells=((0, 0), (12, 12), (0, 0)))
+        sim.set_boundaries(open_axes=(False, True, False), thickness=((0, 0), (12, 12), (0, 0)))
         sim.set_field("E", E)
         sim.set_field("B", B)
         sim.run(200)
@@ -85,7 +85,7 @@ def test_particles_absorbed_at_open_faces_and_the_rest_match_oracle(orc):
     E, B = random_field(gd, rng, 0.05), random_field(gd, rng, 0.05)
     sp = pg.Species("e", -1.0, 1.0, shape="TSC", with_ids=True)
     with pg.Simulation(g) as sim:
-        sim.set_boundaries(open_axes=(True, False, False), pml_cells=((4, 4), (0, 0), (0, 0)))
+        sim.set_boundaries(open_axes=(True, False, False), thickness=((4, 4), (0, 0), (0, 0)))
         sim.add_species(sp)
         sim.set_particles("e", p)
         sim.set_field("E", E)
@@ -111,6 +111,56 @@ def test_particles_absorbed_at_open_faces_and_the_rest_match_oracle(orc):
 def test_ensemble_boxes_stay_periodic():
     ens = pg.Ensemble([(16, 16, 16)])
     with pytest.raises(pg.PicError) as e:
-        ens.box(0).set_boundaries(open_axes=(True, False, False), pml_cells=((4, 4), (0, 0), (0, 0)))
+        ens.box(0).set_boundaries(open_axes=(True, False, False), thickness=((4, 4), (0, 0), (0, 0)))
     assert e.value.code == pg._lib.ERR_UNSUPPORTED
     ens.close()
+
+
+def _exp_damp(n, thick, strength):
+    """Damping factors of one axis (Exponential.kernel:50-90) rounded from double to float."""
+    d = np.ones(n)
+    i = np.arange(n)
+    f_neg = thick[0] - 1 - i
+    d = np.where(f_neg > 0, d * np.exp(-float(np.float32(strength[0])) * f_neg), d)
+    f_pos = i - n + thick[1]
+    d = np.where(f_pos > 0, d * np.exp(-float(np.float32(strength[1])) * f_pos), d)
+    return d.astype(np.float32)
+
+
+def test_exponential_absorber_matches_restatement(orc):
+    """fields/absorber/exponential: the plain open-face Yee updates, then E and B multiplied by
+    exp(-strength f) in the layers, factor by factor in x, y, z order (bit-exact)."""
+    g = pg.Grid(24, 32, 16)
+    gd = g.as_dict()
+    gd["open"] = 3
+    thick, strength = ((5, 3), (6, 6), (0, 0)), ((0.1, 0.2), (0.05, 0.3), (0.0, 0.0))
+    rng = np.random.default_rng(5)
+    E, B = random_field(gd, rng, 0.1), random_field(gd, rng, 0.1)
+    with pg.Simulation(g) as sim:
+        sim.set_boundaries(open_axes=(True, True, False), thickness=thick, absorber="Exponential", strength=strength)
+        sim.set_field("E", E)
+        sim.set_field("B", B)
+        for _ in range(4):
+            sim.stage("current_reset")
+            sim.stage("field_before")
+            sim.stage("field_after")
+        Eg, Bg = sim.get_field("E"), sim.get_field("B")
+    p = orc.pml(((0, 0),) * 3, [0.0] * 3, [1.0] * 3, [0.0] * 3)
+    psi = np.zeros((6,) + E.shape[1:], np.float32)
+    dx, dy = _exp_damp(24, thick[0], strength[0]), _exp_damp(32, thick[1], strength[1])
+
+    def damp(F):
+        for c in range(3):
+            v = F[c]
+            m = dx != 1.0
+            v[:, :, m] = v[:, :, m] * dx[m][None, None, :]
+            m = dy != 1.0
+            v[:, m, :] = v[:, m, :] * dy[m][None, :, None]
+
+    for _ in range(4):
+        orc.yee_b_half_open(gd, p, E, B, psi, update=False)
+        orc.yee_e_open(gd, p, B, E, psi)
+        damp(E)
+        orc.yee_b_half_open(gd, p, E, B, psi, update=True)
+        damp(B)
+    assert np.array_equal(Eg, E) and np.array_equal(Bg, B)
