@@ -164,3 +164,22 @@ def test_exponential_absorber_matches_restatement(orc):
         orc.yee_b_half_open(gd, p, E, B, psi, update=True)
         damp(B)
     assert np.array_equal(Eg, E) and np.array_equal(Bg, B)
+
+
+def test_invalid_boundaries_are_rejected():
+    with pg.Simulation(pg.Grid(16, 16, 8)) as sim:
+        with pytest.raises(pg.PicError) as e:  # layers thicker than the axis
+            sim.set_boundaries(open_axes=(True, False, False), thickness=((10, 10), (0, 0), (0, 0)))
+        assert e.value.code == pg._lib.ERR_INVALID
+        with pytest.raises(pg.PicError) as e:
+            sim.set_boundaries(open_axes=(True, False, False), thickness=((4, 4), (0, 0), (0, 0)),
+                               absorber="Exponential", strength=((-1.0, 0.1), (0, 0), (0, 0)))
+        assert e.value.code == pg._lib.ERR_INVALID
+        with pytest.raises(pg.PicError) as e:
+            sim.set_boundaries(open_axes=(True, False, False), thickness=((4, 4), (0, 0), (0, 0)), kappa_max=(0.5, 1, 1))
+        assert e.value.code == pg._lib.ERR_INVALID
+        with pytest.raises(ValueError):
+            sim.set_boundaries(open_axes=(True, False, False), absorber="Mur")
+        sim.set_boundaries()  # all periodic again
+        sim.run(1)
+        assert sim.device_status() == 0

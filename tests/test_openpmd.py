@@ -23,7 +23,7 @@ def _state(seed=3):
     pi = random_particles(gd, 2, rng, u_th=0.01, mass=1836.0)
     del pi["id"]
     se = pg.Species("e", -1.0, 1.0, pusher="Vay", shape="TSC", with_ids=True)
-    si = pg.Species("i", 1.0, 1836.0, pusher="Boris", shape="PQS")
+    si = pg.Species("i", 1.0, 1836.0, pusher="HigueraCary", shape="PQS", current="EmZ")
     return g, E, B, [(se, pe), (si, pi)]
 
 
@@ -64,7 +64,7 @@ def test_index_attributes_and_numpy_reader(tmp_path):
         s = it["particles"][sp.name]
         assert _attr(s, "particlePush") == sp.pusher
         assert _attr(s, "particleShape") == {"TSC": 2, "PQS": 3}[sp.shape]
-        assert _attr(s, "currentDeposition") == "Esirkepov"
+        assert _attr(s, "currentDeposition") == sp.current
         assert _attr(s["position"], "unitDimension") == [1, 0, 0, 0, 0, 0, 0]
         assert [_attr(s["position"][c], "unitSI") for c in "xyz"] == [1.0, 0.5, 0.25]
         assert _attr(s["momentum"], "macroWeighted") == 1 and _attr(s["momentum"], "weightingPower") == 1
