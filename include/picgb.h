@@ -67,7 +67,7 @@ extern "C"
         PICGB_SHAPE_CIC = 1,
         PICGB_SHAPE_TSC = 2,
         PICGB_SHAPE_PQS = 3,
-        PICGB_SHAPE_PCS = 4 /* oracle only */
+        PICGB_SHAPE_PCS = 4 /* particles/shapes/PCS.hpp; single-box path */
     };
     enum picgb_current
     {

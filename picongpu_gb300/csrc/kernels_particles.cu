@@ -53,6 +53,12 @@ namespace picgb
     PICGB_DECL_SHAPE(CIC)
     PICGB_DECL_SHAPE(TSC)
     PICGB_DECL_SHAPE(PQS)
+    cudaError_t launchPushPCS(int, SpeciesDev const&, float const*, float const*, float*, GridParams const&, PushParams const&,
+                              unsigned*, cudaStream_t);
+    cudaError_t launchPushPCSAlt(int, SpeciesDev const&, float const*, float const*, float*, GridParams const&,
+                                 PushParams const&, unsigned*, cudaStream_t);
+    cudaError_t launchDepositPCS(int, SpeciesDev const&, float*, GridParams const&, PushParams const&, unsigned*, cudaStream_t);
+    cudaError_t launchChargeDensityPCS(int, SpeciesDev const&, float*, GridParams const&, float, float, cudaStream_t);
 
     cudaError_t launchPush(
         int shape,
@@ -81,6 +87,10 @@ namespace picgb
             return launchPushPQS(scId, sp, E, B, J, g, pp, status, stream);
         case 7:
             return launchPushPQSAlt(scId, sp, E, B, J, g, pp, status, stream);
+        case 8:
+            return launchPushPCS(scId, sp, E, B, J, g, pp, status, stream);
+        case 9:
+            return launchPushPCSAlt(scId, sp, E, B, J, g, pp, status, stream);
         }
         return cudaErrorInvalidValue;
     }
@@ -134,6 +144,8 @@ namespace picgb
             return launchDepositTSC(scId, sp, J, g, pp, status, stream);
         case 3:
             return launchDepositPQS(scId, sp, J, g, pp, status, stream);
+        case 4:
+            return launchDepositPCS(scId, sp, J, g, pp, status, stream);
         }
         return cudaErrorInvalidValue;
     }
@@ -156,6 +168,8 @@ namespace picgb
             return launchChargeDensityTSC(scId, sp, rho, g, charge, cellVolume, stream);
         case 3:
             return launchChargeDensityPQS(scId, sp, rho, g, charge, cellVolume, stream);
+        case 4:
+            return launchChargeDensityPCS(scId, sp, rho, g, charge, cellVolume, stream);
         }
         return cudaErrorInvalidValue;
     }

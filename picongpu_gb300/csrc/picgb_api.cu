@@ -515,8 +515,8 @@ extern "C"
             return fail(PICGB_ERR_INVALID, "species needs a name");
         if(cfg->pusher < PICGB_PUSHER_BORIS || cfg->pusher > PICGB_PUSHER_VAY)
             return fail(PICGB_ERR_INVALID, "unknown pusher %d", int(cfg->pusher));
-        if(cfg->shape < PICGB_SHAPE_CIC || cfg->shape > PICGB_SHAPE_PQS)
-            return fail(PICGB_ERR_UNSUPPORTED, "shape %d has no CUDA kernel (CIC, TSC, PQS are available)",
+        if(cfg->shape < PICGB_SHAPE_CIC || cfg->shape > PICGB_SHAPE_PCS)
+            return fail(PICGB_ERR_UNSUPPORTED, "shape %d has no CUDA kernel (CIC, TSC, PQS, PCS are available)",
                         int(cfg->shape));
         if(cfg->current < PICGB_CURRENT_NONE || cfg->current > PICGB_CURRENT_EMZ)
             return fail(PICGB_ERR_INVALID, "unknown current solver %d", int(cfg->current));

@@ -409,6 +409,8 @@ extern "C"
             return r;
         if(cfg && cfg->current == PICGB_CURRENT_EMZ)
             return fail(PICGB_ERR_UNSUPPORTED, "the batched push deposits with Esirkepov only; EmZ runs on the single-box path");
+        if(cfg && cfg->shape == PICGB_SHAPE_PCS)
+            return fail(PICGB_ERR_UNSUPPORTED, "the batched push has CIC, TSC and PQS kernels; PCS runs on the single-box path");
         for(auto* b : e->boxes)
             if(int r = picgb_add_species(b, cfg, index))
                 return r;

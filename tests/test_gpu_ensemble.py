@@ -121,3 +121,14 @@ def test_autotune_times_every_candidate():
     sc, th, rates = pg.autotune(dims, sp, inits, warmup=1, steps=2)
     assert len(rates) == 9 and all(r > 0 for r in rates.values()), rates
     assert rates[(sc, th)] == max(rates.values())
+
+
+def test_ensemble_refuses_what_the_batched_push_lacks():
+    """The batched push instantiates CIC, TSC and PQS with Esirkepov; PCS and EmZ species run on
+    the single-box path."""
+    ens = pg.Ensemble([(16, 16, 16)])
+    for sp in (pg.Species("e", -1.0, 1.0, shape="PCS"), pg.Species("e", -1.0, 1.0, current="EmZ")):
+        with pytest.raises(pg.PicError) as e:
+            ens.add_species(sp)
+        assert e.value.code == pg._lib.ERR_UNSUPPORTED
+    ens.close()

@@ -80,7 +80,7 @@ def test_yee_bit_exact(orc):
     assert np.array_equal(Bg, B)
 
 
-@pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS"])
+@pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS", "PCS"])
 @pytest.mark.parametrize("sc", [(8, 8, 4), (4, 4, 4), (8, 8, 8)])
 def test_push_and_deposit_one_step(orc, shape, sc):
     """Gather + Boris + move + sort bit-exact; fused Esirkepov deposit within 1e-6."""
@@ -88,14 +88,14 @@ def test_push_and_deposit_one_step(orc, shape, sc):
 
 
 @pytest.mark.parametrize("pusher", ["HigueraCary", "Vay"])
-@pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS"])
+@pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS", "PCS"])
 def test_higuera_cary_and_vay_one_step(orc, pusher, shape):
     """The HigueraCary and Vay pushers (square-root stages in double) bit-exact with the oracle."""
     _push_and_deposit(orc, shape, (8, 8, 4), pusher, amp=0.3)
 
 
 @pytest.mark.parametrize("pusher", ["Boris", "HigueraCary"])
-@pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS"])
+@pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS", "PCS"])
 def test_emz_one_step(orc, pusher, shape):
     """The EmZ deposit (fields/currentDeposition/EmZ/EmZ.hpp) fused into the push, within 1e-6."""
     _push_and_deposit(orc, shape, (8, 8, 4), pusher, current="EmZ")
