@@ -59,7 +59,8 @@ extern "C"
         PICGB_PUSHER_FREE = 1, /* particles/pusher/particlePusherFree.hpp */
         PICGB_PUSHER_NONE = 2, /* species without the particlePusher<> flag: not pushed (immobile) */
         PICGB_PUSHER_HIGUERA_CARY = 3, /* particles/pusher/particlePusherHigueraCary.hpp, square roots in double */
-        PICGB_PUSHER_VAY = 4 /* particles/pusher/particlePusherVay.hpp, square roots in double */
+        PICGB_PUSHER_VAY = 4, /* particles/pusher/particlePusherVay.hpp, square roots in double */
+        PICGB_PUSHER_PHOTON = 5 /* particles/pusher/particlePusherPhoton.hpp: |v| = c along the momentum */
     };
     enum picgb_shape
     {

@@ -108,7 +108,8 @@ namespace orc
         BORIS = 0,
         FREE = 1,
         HIGUERA_CARY = 3,
-        VAY = 4
+        VAY = 4,
+        PHOTON = 5
     };
 
     struct SpeciesParam
@@ -725,6 +726,15 @@ namespace orc
                     higueraCaryPush<T, double>(g, charge, mass, Ev, Bv, mom, pos);
                 else
                     vayPush<T, double>(g, charge, mass, Ev, Bv, mom, pos);
+            }
+            else if(sp.pusher == PHOTON)
+            {
+                // Photon (particles/pusher/particlePusherPhoton.hpp:66-74): vel = mom * (c / |mom|)
+                T const normMom = std::sqrt(l2norm2(mom));
+                T const f = T(g.c) / normMom;
+                T const cs[3] = {T(g.dx), T(g.dy), T(g.dz)};
+                for(int d = 0; d < 3; ++d)
+                    pos[d] += (mom[d] * f * T(g.dt)) / cs[d];
             }
             else
                 freePush(g, mass, mom, pos);

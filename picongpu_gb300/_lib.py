@@ -20,7 +20,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_OVERFLOW, ERR_NOT_FOUND, ERR_DUPLICATE, ERR_TIMEO
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "OVERFLOW", 4: "NOT_FOUND", 5: "DUPLICATE", 6: "TIMEOUT",
                 7: "UNSUPPORTED", 8: "LOST", 9: "IO"}
 
-PUSHER_BORIS, PUSHER_FREE, PUSHER_NONE, PUSHER_HIGUERA_CARY, PUSHER_VAY = 0, 1, 2, 3, 4
+PUSHER_BORIS, PUSHER_FREE, PUSHER_NONE, PUSHER_HIGUERA_CARY, PUSHER_VAY, PUSHER_PHOTON = 0, 1, 2, 3, 4, 5
 SHAPE_NGP, SHAPE_CIC, SHAPE_TSC, SHAPE_PQS, SHAPE_PCS = range(5)
 CURRENT_NONE, CURRENT_ESIRKEPOV, CURRENT_EMZ = 0, 1, 2
 SOLVER_YEE = 0

@@ -288,7 +288,7 @@ namespace picgb
         scCoords(sc, g, scx, scy, scz);
         int const ox = scx * SX, oy = scy * SY, oz = scz * SZ;
         size_t const ncell = size_t(g.nx) * g.ny * g.nz;
-        bool const useFields = (pp.pusher != kPusherFree); // Boris, HigueraCary, Vay
+        bool const useFields = pp.pusher != kPusherFree && pp.pusher != kPusherPhoton; // Boris, HigueraCary, Vay
         if(useFields)
         {
             loadTile<TG::GX, TG::GY, TG::GT>(Es, E, ox - SH::gLo, oy - SH::gLo, oz - SH::gLo, g, ncell);
@@ -346,6 +346,14 @@ namespace picgb
                         mom[2] = r.z;
                         velocity(mom, mass, pp.rc2, vel);
                     }
+                }
+                else if(pp.pusher == kPusherPhoton)
+                {
+                    // Photon (particlePusherPhoton.hpp:66-74): vel = mom * (c / |mom|)
+                    float const f = fdv(pp.c, fsq(l2n2(mom[0], mom[1], mom[2])));
+#pragma unroll
+                    for(int d = 0; d < 3; ++d)
+                        vel[d] = fm(mom[d], f);
                 }
                 else
                     velocity(mom, mass, pp.rc2, vel);

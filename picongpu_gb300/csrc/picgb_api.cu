@@ -513,7 +513,7 @@ extern "C"
             return r;
         if(!cfg || !cfg->name || !cfg->name[0])
             return fail(PICGB_ERR_INVALID, "species needs a name");
-        if(cfg->pusher < PICGB_PUSHER_BORIS || cfg->pusher > PICGB_PUSHER_VAY)
+        if(cfg->pusher < PICGB_PUSHER_BORIS || cfg->pusher > PICGB_PUSHER_PHOTON)
             return fail(PICGB_ERR_INVALID, "unknown pusher %d", int(cfg->pusher));
         if(cfg->shape < PICGB_SHAPE_CIC || cfg->shape > PICGB_SHAPE_PCS)
             return fail(PICGB_ERR_UNSUPPORTED, "shape %d has no CUDA kernel (CIC, TSC, PQS, PCS are available)",

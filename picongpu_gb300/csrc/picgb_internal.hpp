@@ -75,6 +75,7 @@ namespace picgb
     constexpr int kPusherFree = 1;
     constexpr int kPusherHigueraCary = 3;
     constexpr int kPusherVay = 4;
+    constexpr int kPusherPhoton = 5;
     // PushParams::current values (the C-ABI's enum picgb_current)
     constexpr int kCurrentNone = 0;
     constexpr int kCurrentEsirkepov = 1;
@@ -89,7 +90,7 @@ namespace picgb
         float rc2; // 1 / (c * c)
         float invVdt; // 1 / (dx * dy * dz * dt)
         float c; // speed of light (HigueraCary and Vay)
-        int pusher; // 0 Boris, 1 Free, 3 HigueraCary, 4 Vay (2 = not pushed, never launched)
+        int pusher; // 0 Boris, 1 Free, 3 HigueraCary, 4 Vay, 5 Photon (2 = not pushed, never launched)
         int current; // 1 Esirkepov, 2 EmZ (0: no current, the deposit is off)
         int deposit; // deposit the current inside the push kernel
         unsigned long long* kindCount; // profiling only: [0] deposits with the short footprint, [1] general; or nullptr

@@ -20,7 +20,7 @@ from . import _lib as L
 
 # .param policy names -> C-ABI enums (param/species.param:49-90, param/fieldSolver.param:57)
 PUSHERS = {"Boris": L.PUSHER_BORIS, "Free": L.PUSHER_FREE, "HigueraCary": L.PUSHER_HIGUERA_CARY,
-           "Vay": L.PUSHER_VAY, None: L.PUSHER_NONE}
+           "Vay": L.PUSHER_VAY, "Photon": L.PUSHER_PHOTON, None: L.PUSHER_NONE}
 SHAPES = {"CIC": L.SHAPE_CIC, "TSC": L.SHAPE_TSC, "PQS": L.SHAPE_PQS, "PCS": L.SHAPE_PCS}
 CURRENTS = {"Esirkepov": L.CURRENT_ESIRKEPOV, "EmZ": L.CURRENT_EMZ, None: L.CURRENT_NONE}
 SOLVERS = {"Yee": L.SOLVER_YEE}

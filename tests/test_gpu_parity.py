@@ -94,6 +94,24 @@ def test_higuera_cary_and_vay_one_step(orc, pusher, shape):
     _push_and_deposit(orc, shape, (8, 8, 4), pusher, amp=0.3)
 
 
+def test_photon_push_bit_exact(orc):
+    """Photon species (particlePusherPhoton.hpp, no charge, no current): positions bit-exact."""
+    g = make_grid((32, 32, 32))
+    gd = g.as_dict()
+    rng = np.random.default_rng(41)
+    p = random_particles(gd, 2, rng, u_th=1.0, weight=0.01)
+    sp = pg.Species("ph", charge=0.0, mass=0.0, pusher="Photon", shape="TSC", current=None, with_ids=True)
+    zero = np.zeros((3, g.nz, g.ny, g.nx), np.float32)
+    with pg.Simulation(g) as sim:
+        sim.add_species(sp)
+        sim.set_particles("ph", p)
+        sim.stage("push")
+        q = sorted_by_id(sim.get_particles("ph"))
+    orc.push(gd, sp.as_dict(), p, zero, zero)
+    for k in ("pos", "mom", "sc", "lcell"):
+        assert np.array_equal(q[k], p[k]), k
+
+
 @pytest.mark.parametrize("pusher", ["Boris", "HigueraCary"])
 @pytest.mark.parametrize("shape", ["CIC", "TSC", "PQS", "PCS"])
 def test_emz_one_step(orc, pusher, shape):

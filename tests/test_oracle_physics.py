@@ -175,3 +175,21 @@ def test_yee_matches_numpy_restatement(orc):
     En2 = (En + coeff * J).astype(np.float32)
     orc.add_current(g, J, Eo)
     assert np.array_equal(Eo, En2)
+
+
+def test_photon_pusher_moves_at_c(orc):
+    """particlePusherPhoton.hpp: free streaming at |v| = c along the momentum, whatever |p|."""
+    g = grid(n=(16, 16, 16), sc=(8, 8, 4), dt=0.5)
+    rng = np.random.default_rng(4)
+    n = 256
+    mom = rng.normal(size=(3, n)).astype(np.float32) * np.float32(10.0) ** rng.uniform(-3, 3, n).astype(np.float32)
+    p = dict(pos=np.full((3, n), 0.5, np.float32), mom=mom, w=np.ones(n, np.float32),
+             sc=np.zeros(n, np.int32), lcell=np.zeros(n, np.uint16))
+    sp = dict(charge=0.0, mass=0.0, shape=2, pusher=5, current=0)
+    zero = np.zeros((3, 16, 16, 16), np.float32)
+    before = global_cells(g, p) + p["pos"].astype(np.float64)
+    orc.push(g, sp, p, zero, zero)
+    after = global_cells(g, p) + p["pos"].astype(np.float64)
+    d = (after - before + 8) % 16 - 8  # periodic unwrap
+    speed = np.sqrt((d ** 2).sum(axis=0)) / g["dt"]
+    assert np.allclose(speed, g["c"], rtol=1e-5)
