@@ -33,9 +33,9 @@ def max_rel(a, b):
     return float(np.abs(a.astype(np.float64) - b).max()) / scale
 
 
-def species(shape="TSC", ids=True, capacity=0):
-    return [pg.Species("e", -1.0, 1.0, shape=shape, with_ids=ids, capacity=capacity),
-            pg.Species("i", 1.0, 1836.0, shape=shape, with_ids=ids, capacity=capacity)]
+def species(shape="TSC", ids=True, capacity=0, pusher="Boris"):
+    return [pg.Species("e", -1.0, 1.0, pusher=pusher, shape=shape, with_ids=ids, capacity=capacity),
+            pg.Species("i", 1.0, 1836.0, pusher=pusher, shape=shape, with_ids=ids, capacity=capacity)]
 
 
 def box_inputs(dims, seed):
@@ -53,9 +53,9 @@ def box_inputs(dims, seed):
     return out
 
 
-def make_ensemble(dims, inputs, shape="TSC", threads=256, fields=True):
+def make_ensemble(dims, inputs, shape="TSC", threads=256, fields=True, pusher="Boris"):
     ens = pg.Ensemble(dims, threads=threads)
-    for sp in species(shape):
+    for sp in species(shape, pusher=pusher):
         ens.add_species(sp)
     for b, (pe, pi, E, B) in enumerate(inputs):
         box = ens.box(b)
@@ -132,3 +132,18 @@ def test_ensemble_refuses_what_the_batched_push_lacks():
             ens.add_species(sp)
         assert e.value.code == pg._lib.ERR_UNSUPPORTED
     ens.close()
+
+
+@pytest.mark.parametrize("pusher", ["HigueraCary", "Vay"])
+def test_batched_higuera_cary_and_vay_match_single_box(pusher):
+    """The batched push's HigueraCary/Vay kernel variant against the single-box path."""
+    inputs = box_inputs(DIMS[:2], 23)
+    with make_ensemble(DIMS[:2], inputs, "PQS", 512, pusher=pusher) as a, \
+            make_ensemble(DIMS[:2], inputs, "PQS", pusher=pusher) as b:
+        a.run(1)
+        b.run_sequential(1)
+        for i in range(2):
+            for name in ("e", "i"):
+                pa, pb = sorted_by_id(a.box(i).get_particles(name)), sorted_by_id(b.box(i).get_particles(name))
+                for k in ("pos", "mom", "sc", "lcell"):
+                    assert np.array_equal(pa[k], pb[k]), (pusher, i, name, k)
