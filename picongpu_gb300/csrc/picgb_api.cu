@@ -520,8 +520,11 @@ extern "C"
                         int(cfg->shape));
         if(cfg->current < PICGB_CURRENT_NONE || cfg->current > PICGB_CURRENT_EMZ)
             return fail(PICGB_ERR_INVALID, "unknown current solver %d", int(cfg->current));
-        if(!(cfg->mass > 0.0f))
-            return fail(PICGB_ERR_INVALID, "species mass must be positive");
+        // massless species (photons, massRatio 0) only with a pusher that does not divide by the mass
+        bool const massless = cfg->pusher == PICGB_PUSHER_PHOTON || cfg->pusher == PICGB_PUSHER_FREE
+            || cfg->pusher == PICGB_PUSHER_NONE;
+        if(!(cfg->mass > 0.0f) && !(massless && cfg->mass == 0.0f))
+            return fail(PICGB_ERR_INVALID, "species mass must be positive (0 only with the Photon, Free or no pusher)");
         if(cfg->capacity > 65504)
             return fail(PICGB_ERR_INVALID, "capacity %u exceeds 65504 slots per supercell", cfg->capacity);
         auto sp = std::make_unique<Species>();
