@@ -264,6 +264,8 @@ def test_invalid_configs_are_rejected():
         assert e.value.code == pg._lib.ERR_INVALID
         with pytest.raises(ValueError):
             sim.add_species(pg.Species("x", -1.0, 1.0, pusher="Axel"))
-        cfg = pg._lib.SpeciesConfig(b"y", -1.0, 1.0, 5, pg._lib.SHAPE_TSC, 1, 0, 0)
+        cfg = pg._lib.SpeciesConfig(b"y", -1.0, 1.0, 9, pg._lib.SHAPE_TSC, 1, 0, 0)  # no pusher 9
         idx = ctypes.c_int32()
+        assert pg.load().picgb_add_species(sim.handle, ctypes.byref(cfg), ctypes.byref(idx)) == pg._lib.ERR_INVALID
+        cfg = pg._lib.SpeciesConfig(b"z", -1.0, 0.0, pg._lib.PUSHER_BORIS, pg._lib.SHAPE_TSC, 1, 0, 0)  # massless Boris
         assert pg.load().picgb_add_species(sim.handle, ctypes.byref(cfg), ctypes.byref(idx)) == pg._lib.ERR_INVALID
