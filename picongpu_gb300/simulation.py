@@ -163,8 +163,12 @@ class Simulation:
     def add_species(self, sp: Species) -> int:
         if sp.pusher not in PUSHERS:
             raise ValueError(f"unknown pusher {sp.pusher!r}; available: {[k for k in PUSHERS if k]} or None")
+        if sp.shape not in SHAPES:
+            raise ValueError(f"unknown shape {sp.shape!r}; available: {list(SHAPES)}")
+        if sp.current not in CURRENTS:
+            raise ValueError(f"unknown current solver {sp.current!r}; available: {[k for k in CURRENTS if k]} or None")
         pusher = PUSHERS[sp.pusher]
-        cfg = L.SpeciesConfig(sp.name.encode(), sp.charge, sp.mass, pusher, SHAPES[sp.shape],
+        cfg =L.SpeciesConfig(sp.name.encode(), sp.charge, sp.mass, pusher, SHAPES[sp.shape],
                               CURRENTS[sp.current], sp.capacity, int(sp.with_ids))
         idx = ctypes.c_int32()
         L.call("picgb_add_species", self.handle, ctypes.byref(cfg), ctypes.byref(idx))

@@ -264,6 +264,10 @@ def test_invalid_configs_are_rejected():
         assert e.value.code == pg._lib.ERR_INVALID
         with pytest.raises(ValueError):
             sim.add_species(pg.Species("x", -1.0, 1.0, pusher="Axel"))
+        with pytest.raises(ValueError):
+            sim.add_species(pg.Species("x", -1.0, 1.0, shape="NGP"))
+        with pytest.raises(ValueError):
+            sim.add_species(pg.Species("x", -1.0, 1.0, current="None"))
         cfg = pg._lib.SpeciesConfig(b"y", -1.0, 1.0, 9, pg._lib.SHAPE_TSC, 1, 0, 0)  # no pusher 9
         idx = ctypes.c_int32()
         assert pg.load().picgb_add_species(sim.handle, ctypes.byref(cfg), ctypes.byref(idx)) == pg._lib.ERR_INVALID
