@@ -303,9 +303,11 @@ def run_e2e(args, wl, sim, pg, torch, local_rank, world):
     sim2.set_field("B", B0)
     for name in ("e", "i"):
         sim2.set_particles(name, host[name])
+    t_up = time.perf_counter()
     for _ in range(args.steps):
         sim2.step()
         sim2.energies()
+    t_steps = time.perf_counter()
     d2h = 0
     for name in ("e", "i"):
         out = sim2.get_particles(name, out=host[name])
@@ -319,7 +321,9 @@ def run_e2e(args, wl, sim, pg, torch, local_rank, world):
     del keep
     return {"value": world * npart * args.steps / dt, "unit": "particle-steps/s",
             "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
-            "wall_s": round(dt, 4)}
+            "wall_s": round(dt, 4),
+            "phases_s": {"upload": round(t_up - t0, 4), "steps_with_energies": round(t_steps - t_up, 4),
+                         "download": round(t1 - t_steps, 4)}}
 
 
 # ---------------------------------------------------------------------- batched ensemble

@@ -386,6 +386,21 @@ namespace picgb
     // Occupancy per supercell; also validates the input: supercell and cell
     // indices in range and in-cell positions in [0, 1) (the kernels assume a
     // particle moves at most one cell per step from a valid in-cell position).
+    // counter[key] += 1 for every lane of the warp with take set, as one atomic per group of
+    // lanes with the same key: the group's lowest lane adds the group's size, and each lane
+    // gets the old value plus its rank in the group.  Called by all 32 lanes together.
+    __device__ __forceinline__ uint32_t warpAggregatedInc(uint32_t* counter, int key, bool take)
+    {
+        unsigned const lane = threadIdx.x & 31u;
+        unsigned const takers = __ballot_sync(0xffffffffu, take);
+        unsigned const peers = __match_any_sync(0xffffffffu, take ? key : -1) & takers;
+        uint32_t old = 0u;
+        if(take && lane == unsigned(__ffs(peers) - 1))
+            old = atomicAdd(counter + key, unsigned(__popc(peers)));
+        old = __shfl_sync(0xffffffffu, old, take ? __ffs(peers) - 1 : int(lane));
+        return old + unsigned(__popc(peers & ((1u << lane) - 1u)));
+    }
+
     __global__ void kHistogram(
         uint64_t n,
         int32_t const* __restrict__ sc,
@@ -398,21 +413,28 @@ namespace picgb
         int vol,
         unsigned* status)
     {
-        for(uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+        // warp-uniform trip count (blockDim.x is a multiple of 32), so the warp-wide
+        // aggregation below has every lane present
+        uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+        for(uint64_t i0 = blockIdx.x * uint64_t(blockDim.x) + (threadIdx.x & ~31u); i0 < n; i0 += stride)
         {
-            int const s = sc[i];
-            bool bad = s < 0 || s >= nsc || int(lcell[i]) >= vol;
-            if(px)
+            uint64_t const i = i0 + (threadIdx.x & 31u);
+            bool const valid = i < n;
+            int s = -1;
+            bool bad = false;
+            if(valid)
             {
-                float const x = px[i], y = py[i], z = pz[i];
-                bad |= !(x >= 0.0f && x < 1.0f && y >= 0.0f && y < 1.0f && z >= 0.0f && z < 1.0f);
+                s = sc[i];
+                bad = s < 0 || s >= nsc || int(lcell[i]) >= vol;
+                if(px)
+                {
+                    float const x = px[i], y = py[i], z = pz[i];
+                    bad |= !(x >= 0.0f && x < 1.0f && y >= 0.0f && y < 1.0f && z >= 0.0f && z < 1.0f);
+                }
+                if(bad)
+                    atomicOr(status, ST_BAD_CELL);
             }
-            if(bad)
-            {
-                atomicOr(status, ST_BAD_CELL);
-                continue;
-            }
-            atomicAdd(count + s, 1u);
+            warpAggregatedInc(count, s, valid && !bad);
         }
     }
 
@@ -481,10 +503,18 @@ namespace picgb
         SpeciesDev sp,
         unsigned* status)
     {
-        for(uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+        // warp-uniform trip count (blockDim.x is a multiple of 32); the input's supercell
+        // indices were checked by kHistogram.  The lanes of a warp that share a supercell take
+        // consecutive slots in lane order.
+        uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+        for(uint64_t i0 = blockIdx.x * uint64_t(blockDim.x) + (threadIdx.x & ~31u); i0 < n; i0 += stride)
         {
-            int const s = sc[i];
-            uint32_t const slot = atomicAdd(sp.count + s, 1u);
+            uint64_t const i = i0 + (threadIdx.x & 31u);
+            bool const valid = i < n;
+            int const s = valid ? sc[i] : -1;
+            uint32_t const slot = warpAggregatedInc(sp.count, s, valid);
+            if(!valid)
+                continue;
             if(slot >= sp.cap)
             {
                 atomicOr(status, ST_LOST);
