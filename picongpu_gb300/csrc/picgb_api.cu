@@ -346,14 +346,11 @@ namespace picgb::host
         return PICGB_OK;
     }
 
-    // After a step: a set overflow bit means arrivals were parked in the spill
-    // buffer; they are re-inserted with a larger capacity before anything else runs.
-    int afterStep(picgb_sim* s)
+    // A set overflow bit in the status word `bits` means that arrivals were parked in the
+    // spill buffer; they are re-inserted with a larger capacity before anything else reads
+    // the particles.  ST_LOST is an error.
+    int reinsertSpilled(picgb_sim* s, unsigned bits)
     {
-        unsigned bits = 0;
-        if(int r = readStatus(s, &bits, false))
-            return r;
-        CUDA_TRY(profFlush(s));
         if(bits & ST_LOST)
             return fail(PICGB_ERR_LOST, "particles were lost: the spill buffer overflowed");
         if(bits & ST_OVERFLOW)
@@ -371,9 +368,52 @@ namespace picgb::host
         return PICGB_OK;
     }
 
+    // After a step: the profiling events are read and spilled arrivals re-inserted.
+    int afterStep(picgb_sim* s)
+    {
+        unsigned bits = 0;
+        if(int r = readStatus(s, &bits, false))
+            return r;
+        CUDA_TRY(profFlush(s));
+        return reinsertSpilled(s, bits);
+    }
+
+    // The status word read and spilled arrivals re-inserted (synchronises the stream).
+    int settleParticles(picgb_sim* s)
+    {
+        unsigned bits = 0;
+        if(int r = readStatus(s, &bits, false))
+            return r;
+        return reinsertSpilled(s, bits);
+    }
+
     bool hasCurrent(Species const& sp)
     {
         return sp.cfg.current == PICGB_CURRENT_ESIRKEPOV || sp.cfg.current == PICGB_CURRENT_EMZ;
+    }
+
+    // The push kernel of every pushed species (with the fused deposit), then their compaction.
+    int pushLaunches(picgb_sim* s)
+    {
+        bool const fuse = s->cfg.fuse_deposit != 0;
+        for(auto& sp : s->species)
+        {
+            if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE)
+                continue;
+            PushParams const pp = s->pushParams(*sp, fuse && hasCurrent(*sp));
+            Species& x = *sp;
+            CUDA_TRY(timedLaunch(s, PICGB_KERNEL_PUSH, [&] {
+                return launchPush(x.cfg.shape, s->cfg.supercell, x.dev, s->E, s->B, s->J, s->g, pp, s->status, s->stream);
+            }));
+        }
+        for(auto& sp : s->species)
+        {
+            if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE)
+                continue;
+            Species& x = *sp;
+            CUDA_TRY(timedLaunch(s, PICGB_KERNEL_COMPACT, [&] { return launchCompact(x.dev, s->nsc, s->stream); }));
+        }
+        return PICGB_OK;
     }
 } // namespace
 
@@ -867,25 +907,11 @@ extern "C"
     {
         if(int r = checkSim(s))
             return r;
-        bool const fuse = s->cfg.fuse_deposit != 0;
-        for(auto& sp : s->species)
-        {
-            if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE)
-                continue;
-            PushParams const pp = s->pushParams(*sp, fuse && hasCurrent(*sp));
-            Species& x = *sp;
-            CUDA_TRY(timedLaunch(s, PICGB_KERNEL_PUSH, [&] {
-                return launchPush(x.cfg.shape, s->cfg.supercell, x.dev, s->E, s->B, s->J, s->g, pp, s->status, s->stream);
-            }));
-        }
-        for(auto& sp : s->species)
-        {
-            if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE)
-                continue;
-            Species& x = *sp;
-            CUDA_TRY(timedLaunch(s, PICGB_KERNEL_COMPACT, [&] { return launchCompact(x.dev, s->nsc, s->stream); }));
-        }
-        return PICGB_OK;
+        if(int r = pushLaunches(s))
+            return r;
+        // arrivals parked in the spill buffer go back into the supercells before a
+        // later stage or a download reads the particles
+        return settleParticles(s);
     }
 
     int picgb_stage_field_before(picgb_sim* s, uint32_t step)
@@ -1074,8 +1100,13 @@ extern "C"
             return r;
         if(int r = picgb_stage_current_reset(s))
             return r;
-        if(int r = picgb_stage_push(s, step))
+        if(int r = pushLaunches(s))
             return r;
+        // with the deposit fused into the push every particle has deposited, and the spilled
+        // arrivals can wait for the end of the step; the separate deposit stage reads them
+        if(s->cfg.fuse_deposit == 0)
+            if(int r = settleParticles(s))
+                return r;
         if(int r = picgb_stage_field_before(s, step))
             return r;
         if(int r = picgb_stage_deposit(s, step))
