@@ -192,3 +192,42 @@ def test_empty_and_sparse_species(orc):
     assert energies["none"] == 0.0
     ke = orc.kinetic_energy(gd, se.as_dict(), p)
     assert energies["e"] == pytest.approx(ke, rel=1e-6)
+
+
+def test_overflow_before_separate_deposit(orc):
+    """Arrivals that overflow their destination supercell are parked and re-inserted inside the
+    push stage, so the separate deposit stage (fuse_deposit off) deposits every particle."""
+    g = pg.Grid(32, 32, 16, supercell=(8, 8, 4), fuse_deposit=False)
+    gd = g.as_dict()
+    rng = np.random.default_rng(64)
+    n = 60
+    # 60 particles in the last x column of supercell 0 leave along +x into supercell 1, which
+    # holds 60 particles of its own; 64 slots per supercell
+    movers = [np.full(n, 7), rng.integers(0, 8, n), rng.integers(0, 4, n)]
+    stayers = [rng.integers(9, 15, n), rng.integers(1, 7, n), rng.integers(1, 3, n)]
+    cells = np.concatenate([np.stack(movers), np.stack(stayers)], axis=1)
+    pos = np.concatenate([np.stack([rng.uniform(0.8, 0.99, n), rng.uniform(0.2, 0.8, n), rng.uniform(0.2, 0.8, n)]),
+                          rng.uniform(0.2, 0.8, (3, n))], axis=1)
+    u = np.concatenate([np.stack([np.full(n, 3.0), np.zeros(n), np.zeros(n)]), np.zeros((3, n))], axis=1)
+    p = _particles(g, cells, pos, u)
+    E, B = random_field(gd, rng, 0.01), random_field(gd, rng, 0.01)
+    sp = pg.Species("e", -1.0, 1.0, shape="TSC", capacity=64, with_ids=True)
+    with pg.Simulation(g) as sim:
+        sim.add_species(sp)
+        sim.set_particles("e", p)
+        sim.set_field("E", E)
+        sim.set_field("B", B)
+        sim.stage("current_reset")
+        sim.stage("push")
+        sim.stage("deposit")
+        q = _sorted(sim.get_particles("e"))
+        Jg = sim.get_field("J")
+        assert sim.device_status() == 0
+    ref = {k: v.copy() for k, v in p.items()}
+    orc.push(gd, sp.as_dict(), ref, E, B)
+    assert np.bincount(ref["sc"])[1] == 2 * n  # the destination holds more than its 64 slots
+    for k in ("pos", "mom", "sc", "lcell"):
+        assert np.array_equal(q[k], ref[k]), k
+    Jo = np.zeros_like(E)
+    orc.deposit(gd, sp.as_dict(), ref, Jo)
+    assert _max_rel(Jg, Jo) <= REL
