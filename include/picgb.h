@@ -218,7 +218,9 @@ extern "C"
     int picgb_stage_current_reset(picgb_sim* sim);
     /* ParticlePush (simulation/stage/ParticlePush.x.cpp:141): gather + push + move of all species
      * with a pusher, then the supercell migration.  With fuse_deposit the current of species with
-     * current<> is deposited in the same kernel (J complete after this stage). */
+     * current<> is deposited in the same kernel (J complete after this stage).  Synchronises the
+     * stream: arrivals that overflowed their supercell are re-inserted with a larger capacity
+     * before it returns (PICGB_ERR_LOST if the spill buffer overflowed as well). */
     int picgb_stage_push(picgb_sim* sim, uint32_t step);
     /* fieldSolver.update_beforeCurrent (FDTD.hpp:69; FDTDBase.hpp:97-121): B half step, E step */
     int picgb_stage_field_before(picgb_sim* sim, uint32_t step);
