@@ -638,7 +638,11 @@ namespace picgb
         uint32_t const n = sp.count[sc];
         size_t const base = size_t(sc) * sp.cap;
         float const c2 = fm(c, c);
-        double acc = 0.0;
+        // per thread a compensated float sum (Neumaier's improved Kahan-Babuska summation:
+        // the rounding error of every addition is collected in `comp`), as the reference sums
+        // per thread in float_X; FP64 from the thread sums on.  An FP64 add per particle runs
+        // on this GPU's narrow FP64 pipe.
+        float sum = 0.0f, comp = 0.0f;
         for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
         {
             size_t const s = base + k;
@@ -657,9 +661,11 @@ namespace picgb
                 else
                     e = fm(fm(fs(gamma, 1.0f), m), c2);
             }
-            acc += double(e);
+            float const t = fa(sum, e);
+            comp = fa(comp, fabsf(sum) >= fabsf(e) ? fa(fs(sum, t), e) : fa(fs(e, t), sum));
+            sum = t;
         }
-        double const s = blockSumD(acc);
+        double const s = blockSumD(double(sum) + double(comp));
         if(threadIdx.x == 0 && s != 0.0)
             atomicAdd(out, s);
     }
