@@ -6,8 +6,7 @@ plugins/EnergyFields.x.cpp, plugins/EnergyParticles.x.cpp), over many steps.
   eps0 div E = rho at the start, and a charge-conserving deposit (Esirkepov, EmZ) keeps
   max |eps0 div E - rho| within 1e-5 of max |rho_e| at every step, for every shape.
 * Energy: field plus kinetic energy of a thermal plasma drifts by less than 3 % over the run
-  (the Debye length is 0.3 cells, so CIC heats by about 1 % in 30 steps; a wrong sign or factor
-  in the deposit or the J add changes the energy by far more).
+  (the Debye length is 0.3 cells, and CIC heats by about 1 % in 30 steps).
 """
 import numpy as np
 import pytest
