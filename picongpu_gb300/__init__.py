@@ -6,6 +6,7 @@ from ._lib import PicError, load
 from .adjoint import DiffPIC, DiffSpecies
 from .ensemble import Ensemble, autotune, plasma_init
 from .simulation import DataConnector, Grid, Simulation, Species
+from .start import quiet_start
 
 __all__ = ["DataConnector", "DiffPIC", "DiffSpecies", "Ensemble", "Grid", "PicError", "Simulation", "Species", "autotune", "load", "plasma_init",
-           "adjoint", "_lib"]
+           "quiet_start", "adjoint", "_lib"]
