@@ -273,13 +273,16 @@ extern "C"
      * arrays with each species' charge per real particle and shape (CIC, TSC, PQS).  Outputs
      * are host doubles: max|eps0 div E - rho| and max|rho|, the same quantities as
      * picgb_charge_residual.  The charge density is accumulated in a file-scope device array
-     * of at most picgb_noalloc_max_cells() = 2^22 cells (16 MiB), which every GPU that loads
-     * this library holds until the process exits; larger grids are rejected with
-     * PICGB_ERR_INVALID.  The first call on a device looks up that array's device address
-     * (cudaGetSymbolAddress) and should come before any stream capture.  All calls share the
-     * array (each call clears it first), so calls that overlap on the GPU race.  Work is
-     * enqueued on `stream` (cudaStream_t, NULL = default stream) and the call waits for it.
-     * Errors are reported by picgb_noalloc_last_error(). */
+     * of at most picgb_noalloc_max_cells() = 2^22 cells (16 MiB); larger grids are rejected
+     * with PICGB_ERR_INVALID.  CUDA loads device code lazily by default, so that array is
+     * reserved on a device by the first call there (which also looks up its device address
+     * with cudaGetSymbolAddress) and held until the process exits: a host that reserves
+     * device memory for itself should make one call per device before doing so, and the
+     * first call should come before any stream capture.  The call makes grid->device
+     * current while it works and gives the calling thread its previous current device
+     * back.  All calls share the array (each call clears it first), so calls that overlap
+     * on the GPU race.  Work is enqueued on `stream` (cudaStream_t, NULL = default stream)
+     * and the call waits for it.  Errors are reported by picgb_noalloc_last_error(). */
     uint64_t picgb_noalloc_max_cells(void);
     const char* picgb_noalloc_last_error(void);
     int picgb_charge_residual_noalloc(

@@ -6,8 +6,11 @@
 // reference sizes its frame heap), or a caller in a memory-pool-restricted
 // process -- cannot call cudaMalloc for a temporary charge-density grid.  This
 // entry point therefore keeps its scratch (the charge density and two maxima)
-// in file-scope static device arrays of a fixed maximum size, which every GPU
-// that loads this library holds until the process exits.
+// in file-scope static device arrays of a fixed maximum size.  CUDA loads a
+// library's device code lazily by default: the arrays are reserved on a device
+// when this file's device code is first used there, i.e. by the first call on
+// that device, and held until the process exits.  A host that reserves device
+// memory for itself should make that first call before it does so.
 #include "picgb.h"
 #include "picgb_device.cuh"
 #include "picgb_internal.hpp"
@@ -16,14 +19,12 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 namespace
 {
     // largest grid (cells) the scratch holds: 2^22 floats = 16 MiB
     constexpr size_t kMaxCells = size_t(1) << 22;
-    constexpr int kMaxDevices = 64;
 
     __device__ __align__(256) float g_rho[kMaxCells];
     __device__ __align__(256) unsigned g_max[2];
@@ -34,11 +35,29 @@ namespace
         unsigned* max = nullptr;
     };
 
-    // device addresses of the scratch arrays, looked up once per device
-    ScratchPtrs g_ptrs[kMaxDevices];
-    std::mutex g_ptrsMutex;
-
     thread_local std::string g_err;
+
+    // Makes `device` current for the lifetime of the guard and gives the calling
+    // thread its previous current device back on every return path.
+    struct DeviceGuard
+    {
+        int previous = -1;
+        cudaError_t err = cudaSuccess;
+
+        explicit DeviceGuard(int device)
+        {
+            err = cudaGetDevice(&previous);
+            if(err == cudaSuccess && previous != device)
+                err = cudaSetDevice(device);
+        }
+
+        ~DeviceGuard()
+        {
+            int now = -1;
+            if(previous >= 0 && cudaGetDevice(&now) == cudaSuccess && now != previous)
+                cudaSetDevice(previous);
+        }
+    };
 
     int failNa(int code, char const* fmt, ...)
     {
@@ -141,30 +160,19 @@ namespace
         }
     }
 
-    // Address of the scratch on the current device (looked up on the first call
-    // on that device, with the device current).
-    int scratchFor(int device, ScratchPtrs* out)
+    // Device addresses of the scratch arrays on the current device.  Looked up on every
+    // call (cheap once the device code is loaded), so a context that the host tore down
+    // and created again never sees a stale address.  The first lookup on a device loads
+    // this file's device code there, which reserves the arrays.
+    int scratchOnCurrentDevice(ScratchPtrs* out)
     {
-        if(device < 0 || device >= kMaxDevices)
-            return failNa(PICGB_ERR_INVALID, "device %d outside the supported range 0..%d", device, kMaxDevices - 1);
-        std::lock_guard<std::mutex> lock(g_ptrsMutex);
-        ScratchPtrs& p = g_ptrs[device];
-        if(!p.rho)
-        {
-            cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p.rho), g_rho);
-            if(e != cudaSuccess)
-            {
-                p.rho = nullptr;
-                return failNa(PICGB_ERR_CUDA, "cudaGetSymbolAddress(rho scratch) failed: %s", cudaGetErrorString(e));
-            }
-            e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p.max), g_max);
-            if(e != cudaSuccess)
-            {
-                p.rho = nullptr;
-                p.max = nullptr;
-                return failNa(PICGB_ERR_CUDA, "cudaGetSymbolAddress(max scratch) failed: %s", cudaGetErrorString(e));
-            }
-        }
+        ScratchPtrs p;
+        cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p.rho), g_rho);
+        if(e != cudaSuccess)
+            return failNa(PICGB_ERR_CUDA, "cudaGetSymbolAddress(rho scratch) failed: %s", cudaGetErrorString(e));
+        e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p.max), g_max);
+        if(e != cudaSuccess)
+            return failNa(PICGB_ERR_CUDA, "cudaGetSymbolAddress(max scratch) failed: %s", cudaGetErrorString(e));
         *out = p;
         return PICGB_OK;
     }
@@ -213,10 +221,15 @@ extern "C"
         for(int s = 0; s < nspecies; ++s)
             if(shape[s] < PICGB_SHAPE_CIC || shape[s] > PICGB_SHAPE_PQS)
                 return failNa(PICGB_ERR_UNSUPPORTED, "species %d: shape %d has no kernel", s, int(shape[s]));
-        NA_TRY(cudaSetDevice(cfg->device));
+        if(cfg->device < 0)
+            return failNa(PICGB_ERR_INVALID, "device %d is not a device index", int(cfg->device));
+        DeviceGuard guard(cfg->device); // the caller's current device comes back on return
+        NA_TRY(guard.err);
         ScratchPtrs p;
-        if(int r = scratchFor(cfg->device, &p))
+        if(int r = scratchOnCurrentDevice(&p))
             return r;
+        int sms = 0;
+        NA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg->device));
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         picgb::GridParams g{};
         g.nx = cfg->nx;
@@ -241,7 +254,8 @@ extern "C"
             picgb_particles const& q = species[s];
             if(q.n == 0)
                 continue;
-            int const blocks = int(std::min<uint64_t>((q.n + 255) / 256, 152 * 32));
+            // grid-stride loop: 8 blocks of 256 threads per SM of this device at most
+            int const blocks = int(std::min<uint64_t>((q.n + 255) / 256, uint64_t(sms) * 8));
             // the first maximum word doubles as the status word of the density pass;
             // it is read and cleared before the residual pass
             unsigned* status = p.max;
