@@ -43,6 +43,9 @@ WORKLOADS = {
     # the two-stream workload on 64^3 cells (8.4e6 particles, 270 MB of particle arrays): profiling case
     "two_stream_64": dict(n=(64, 64, 64), ppc=16, shape="TSC", u_th=0.005, drift=0.2, split=True,
                           sample_n=(64, 64, 64)),
+    # on 128^3 cells (6.7e7 particles, 2.5 GB): the DRAM-traffic capture, working set ~20x L2
+    "two_stream_128": dict(n=(128, 128, 128), ppc=16, shape="TSC", u_th=0.005, drift=0.2, split=True,
+                           sample_n=(64, 64, 64)),
 }
 DT = float(np.float32(0.99 / np.sqrt(3.0)))
 MASS_P = 1836.0
@@ -260,7 +263,11 @@ def run_gpu(args, wl, rank, world, local_rank):
     roof = {"kernel": "kPush (gather+Boris+move+Esirkepov+migration, per species)", "bound": "hbm",
             "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
-            "traffic": traffic, "algorithmic_bytes_per_launch": (B_PARTICLE * npart + 2 * B_PUSH_CELL * ncell) / 2,
+            "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one kPush launch on the 128^3 "
+                              "two-stream case (33.5e6 particles, 57.76 B each), scaled by the particle count "
+                              "(profiles/push_tsc_two_stream_128_dram.md)",
+            "algorithmic_bytes_per_launch": (B_PARTICLE * npart + 2 * B_PUSH_CELL * ncell) / 2,
             "mean_launch_ms": push_ms / max(push_n, 1),
             "step_frac_of_peak": round(value / world * (B_PARTICLE + B_CELL / (2 * wl["ppc"])) / (peak * 1e9), 4),
             "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]},
@@ -274,8 +281,9 @@ def run_gpu(args, wl, rank, world, local_rank):
 
 
 def push_traffic(n_per_launch, ncell):
-    """DRAM bytes per push launch from the committed ncu summary (bytes per particle), scaled; else None."""
-    p = os.path.join(ROOT, "profiles", "push_tsc_two_stream.md")
+    """DRAM bytes per push launch from the committed ncu summary of one 128^3 launch (bytes per
+    particle), scaled to the launch's particle count; else None."""
+    p = os.path.join(ROOT, "profiles", "push_tsc_two_stream_128_dram.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -665,9 +673,14 @@ def main():
         if rank != 0:
             return
         val, cores, sample = cpu_sample_rate(wl, args.steps, args.warmup, budget_s=60.0)
+        sn = wl["sample_n"]
+        ref_config = dict(config, workload=f"{config['workload']}; the CPU arm times a bounded sample of it: "
+                                           f"{sn[0]}x{sn[1]}x{sn[2]} cells with the same ppc, shape, solvers and "
+                                           f"distribution (particle-steps/s is per particle, so the rates compare)",
+                          sample_cells=list(sn))
         print(json.dumps({"impl": "reference", "metric": metric, "value": val, "unit": metric, "n_gpus": args.gpus,
                           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-                          "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                          "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": ref_config,
                           "cpu_baseline": {"value": val, "unit": metric, "cores": cores, "kind": "port",
                                            "sample": sample},
                           "e2e": {"value": val, "unit": metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),

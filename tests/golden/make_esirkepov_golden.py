@@ -103,8 +103,9 @@ def run_case(grid, order, pos0, beta_vec, dt, charge):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    grid = load_reference(ref_root)
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {os.path.basename(__file__)} <path of a PIConGPU source tree>")
+    grid = load_reference(sys.argv[1])
     cases = []
     beta = 0.999
     dt = 0.5
