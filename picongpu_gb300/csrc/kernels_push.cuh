@@ -33,6 +33,12 @@ namespace picgb
 #    define PICGB_QUEUE_CAP 32
 #endif
     constexpr int kQueueCap = PICGB_QUEUE_CAP;
+
+#ifndef PICGB_TILE_PITCH_MIN
+    // smallest row and plane pitch (words) of the E/B tiles of 8 x 8 supercell planes
+    // (TileGeom); 0 keeps the unpadded widths
+#    define PICGB_TILE_PITCH_MIN 12
+#endif
     static_assert(kQueueCap >= 32, "a warp drains 32 jobs at a time");
     constexpr int kJobWords = 9;
 
@@ -42,7 +48,15 @@ namespace picgb
         static constexpr int GX = SC::SX + SH::gLo + SH::gHi;
         static constexpr int GY = SC::SY + SH::gLo + SH::gHi;
         static constexpr int GZ = SC::SZ + SH::gLo + SH::gHi;
-        static constexpr int GT = GX * GY * GZ;
+        // Row and plane pitch of the E/B tiles.  With 8 x 8 supercell planes the 32 lanes of
+        // a warp gather from 32 cells of an 8 x 4 patch, each shifted by its particle's
+        // sub-cell position; a bank-conflict model of that access (random in-cell
+        // positions) gives 2.1 shared-memory wavefronts per load with a pitch of 12 words
+        // against 2.3 to 2.4 with the unpadded 10 (CIC) and 11 (TSC); PQS (12) and PCS (13)
+        // keep their widths, and so do the small 4 x 4 x 4 supercells.
+        static constexpr int PX = (SC::SX == 8 && GX < PICGB_TILE_PITCH_MIN) ? PICGB_TILE_PITCH_MIN : GX;
+        static constexpr int PY = (SC::SY == 8 && GY < PICGB_TILE_PITCH_MIN) ? PICGB_TILE_PITCH_MIN : GY;
+        static constexpr int GT = PX * PY * GZ; // words of one component's tile
         static constexpr int JX = SC::SX + SH::jLo + SH::jHi;
         static constexpr int JY = SC::SY + SH::jLo + SH::jHi;
         static constexpr int JZ = SC::SZ + SH::jLo + SH::jHi;
@@ -61,8 +75,9 @@ namespace picgb
         z = sc / (g.nscx * g.nscy);
     }
 
-    // Stage a (S + lo + hi)^3 tile of a 3-component SoA field with periodic wrap.
-    template<int TX, int TY, int TT>
+    // Stage a TX x TY x TZ tile of a 3-component SoA field with periodic wrap, stored with
+    // row pitch PX and plane pitch PX * PY (component stride PT words).
+    template<int TX, int TY, int TZ, int PX, int PY, int PT>
     __device__ __forceinline__ void loadTile(
         float* __restrict__ dst,
         float const* __restrict__ src,
@@ -73,9 +88,11 @@ namespace picgb
         size_t ncell)
     {
         bool const anyOpen = g.open != 0; // uniform: the periodic box takes the plain wrap
-        for(int t = threadIdx.x; t < TT; t += blockDim.x)
+        for(int e = threadIdx.x; e < TX * TY * TZ; e += blockDim.x)
         {
-            int const tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
+            int const tx = e % TX, ty = (e / TX) % TY, tz = e / (TX * TY);
+            int const t = tx + PX * (ty + PY * tz);
+            constexpr int TT = PT;
             int gx, gy, gz;
             if(!anyOpen)
             {
@@ -291,8 +308,10 @@ namespace picgb
         bool const useFields = pp.pusher != kPusherFree && pp.pusher != kPusherPhoton; // Boris, HigueraCary, Vay
         if(useFields)
         {
-            loadTile<TG::GX, TG::GY, TG::GT>(Es, E, ox - SH::gLo, oy - SH::gLo, oz - SH::gLo, g, ncell);
-            loadTile<TG::GX, TG::GY, TG::GT>(Bs, B, ox - SH::gLo, oy - SH::gLo, oz - SH::gLo, g, ncell);
+            loadTile<TG::GX, TG::GY, TG::GZ, TG::PX, TG::PY, TG::GT>(Es, E, ox - SH::gLo, oy - SH::gLo, oz - SH::gLo, g,
+                                                                  ncell);
+            loadTile<TG::GX, TG::GY, TG::GZ, TG::PX, TG::PY, TG::GT>(Bs, B, ox - SH::gLo, oy - SH::gLo, oz - SH::gLo, g,
+                                                                  ncell);
         }
         if(pp.deposit)
             for(int t = threadIdx.x; t < TG::JWords; t += blockDim.x)
@@ -326,12 +345,12 @@ namespace picgb
                     GatherWeights<SH> gw;
                     gw.compute(pos);
                     // Yee positions (fields/YeeCell.hpp:70-131): E_x (1/2,0,0) ... B_x (0,1/2,1/2) ...
-                    Bv[0] = gw.template gather<TG::GX, TG::GY, 0, 1, 1>(Bs, lx, ly, lz);
-                    Bv[1] = gw.template gather<TG::GX, TG::GY, 1, 0, 1>(Bs + TG::GT, lx, ly, lz);
-                    Bv[2] = gw.template gather<TG::GX, TG::GY, 1, 1, 0>(Bs + 2 * TG::GT, lx, ly, lz);
-                    Ev[0] = gw.template gather<TG::GX, TG::GY, 1, 0, 0>(Es, lx, ly, lz);
-                    Ev[1] = gw.template gather<TG::GX, TG::GY, 0, 1, 0>(Es + TG::GT, lx, ly, lz);
-                    Ev[2] = gw.template gather<TG::GX, TG::GY, 0, 0, 1>(Es + 2 * TG::GT, lx, ly, lz);
+                    Bv[0] = gw.template gather<TG::PX, TG::PY, 0, 1, 1>(Bs, lx, ly, lz);
+                    Bv[1] = gw.template gather<TG::PX, TG::PY, 1, 0, 1>(Bs + TG::GT, lx, ly, lz);
+                    Bv[2] = gw.template gather<TG::PX, TG::PY, 1, 1, 0>(Bs + 2 * TG::GT, lx, ly, lz);
+                    Ev[0] = gw.template gather<TG::PX, TG::PY, 1, 0, 0>(Es, lx, ly, lz);
+                    Ev[1] = gw.template gather<TG::PX, TG::PY, 0, 1, 0>(Es + TG::GT, lx, ly, lz);
+                    Ev[2] = gw.template gather<TG::PX, TG::PY, 0, 0, 1>(Es + 2 * TG::GT, lx, ly, lz);
                     if constexpr(!ALT)
                         boris(charge, mass, Ev, Bv, pp.dt, pp.c2, pp.rc2, mom, vel);
                     else

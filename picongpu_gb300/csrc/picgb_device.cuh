@@ -542,6 +542,47 @@ namespace picgb
         // word stride of real axis a (0 x, 1 y, 2 z)
         __device__ __forceinline__ static int stride(int a) { return a == 0 ? 1 : (a == 1 ? TX : TX * TY); }
 
+        // T * cum at tile word idx (component offset included by the caller); cumHi =
+        // cum * 2^-k (exact).  In fixed point the high part a = rint(T cum 2^-k) comes from
+        // one fused multiply-add on the exact product, the low part r = T cum - a 2^k from
+        // another (one rounding), so a 2^k + rint(r) is the value rounded to a unit.
+        __device__ __forceinline__ void addProduct(int idx, float T, float cum, float cumHi, float magicHi) const
+        {
+#if PICGB_J_FIXED
+            constexpr float kMagic = 12582912.0f; // 1.5 * 2^23
+            constexpr int kMagicBits = 0x4B400000;
+            int* w = reinterpret_cast<int*>(J);
+            float const t = __fmaf_rn(T, cumHi, kMagic); // kMagic + a
+            float const na = __fmaf_rn(-t, f.hiUnit, magicHi); // -a 2^k, exact
+            float const r = __fmaf_rn(T, cum, na);
+            atomicAdd(w + idx, __float_as_int(t) - kMagicBits);
+            atomicAdd(w + 3 * TT + idx, __float_as_int(__fadd_rn(r, kMagic)) - kMagicBits);
+#else
+            (void) cumHi;
+            (void) magicHi;
+            atomicAdd(J + idx, fm(T, cum));
+#endif
+        }
+
+        // kMagic * 2^k, the constant of addProduct
+        __device__ __forceinline__ float magicHi() const
+        {
+#if PICGB_J_FIXED
+            return fm(12582912.0f, f.hiUnit);
+#else
+            return 0.0f;
+#endif
+        }
+
+        __device__ __forceinline__ float hiStep() const
+        {
+#if PICGB_J_FIXED
+            return f.hiStep;
+#else
+            return 1.0f;
+#endif
+        }
+
         // v at tile word idx of the first plane (component offset included by the caller)
         __device__ __forceinline__ void addAt(int idx, float v) const
         {
@@ -688,9 +729,16 @@ namespace picgb
         }
 
         // The short footprint (the particle stays in its assignment cell along every axis) of
-        // the three rotated components in one runtime loop, so the particle loop holds one
-        // copy of the unrolled (i, j, k) body instead of three.  Same arithmetic as
-        // cpt1D<C, false>; the rotation maps rotated axes i, j, k to real axes C+1, C+2, C.
+        // the three rotated components.  The on-support weights S0 (start) and S1 (end) of
+        // each axis are evaluated once and shared by the components (ChargeAssignment of
+        // the shape, TSC.hpp:85 etc.; the reference evaluates the same functions per node).
+        // The Esirkepov weight of node (i, j) (Esirkepov.hpp:214-215),
+        //   S0i S0j + 1/2 (dSi S0j + S0i dSj) + 1/3 dSi dSj = Ai Aj + dSi dSj / 12,
+        // with A = (S0 + S1) / 2 and dS = S1 - S0, is one product and one fused
+        // multiply-add; the running sum along k is the prefix sum of dSk.  The three
+        // components run in one runtime loop, so the particle loop holds one copy of the
+        // unrolled (i, j, k) body, and pick their axes' weights by selects.  J agrees with
+        // the per-node evaluation to rounding (the tile sums in another order anyway).
         template<typename Acc>
         __device__ __forceinline__ static void runShort(
             Acc const& acc,
@@ -699,48 +747,67 @@ namespace picgb
             float const csd[3],
             int tileTT)
         {
-            auto sel = [](float const* p, int a) { return a == 0 ? p[0] : (a == 1 ? p[1] : p[2]); };
+            float A[3][S], D[3][S];
+#pragma unroll
+            for(int d = 0; d < 3; ++d)
+            {
+                float s0[S + 1], s1[S + 1];
+                SH::caArray(p0[d], false, s0);
+                SH::caArray(p1[d], false, s1);
+#pragma unroll
+                for(int m = 0; m < S; ++m)
+                {
+                    D[d][m] = fs(s1[m], s0[m]);
+                    A[d][m] = fm(0.5f, fa(s0[m], s1[m]));
+                }
+            }
+            float const magicHi = acc.magicHi(), hiStep = acc.hiStep();
 #pragma unroll 1
             for(int C = 0; C < 3; ++C)
             {
+                // rotated axes: i -> C + 1, j -> C + 2, k -> C (mod 3)
+                bool const c0 = C == 0, c1 = C == 1;
+                if(c0 ? p0[0] == p1[0] : (c1 ? p0[1] == p1[1] : p0[2] == p1[2]))
+                    continue; // no motion along k: no current
                 int const ai = C == 2 ? 0 : C + 1;
-                int const aj = C == 0 ? 2 : C - 1;
-                float const q0[3] = {sel(p0, ai), sel(p0, aj), sel(p0, C)};
-                float const q1[3] = {sel(p1, ai), sel(p1, aj), sel(p1, C)};
-                if(q0[2] == q1[2])
-                    continue;
+                int const aj = c0 ? 2 : C - 1;
+                auto pick = [](float const (&X)[3][S], int a, int m)
+                { return a == 0 ? X[0][m] : (a == 1 ? X[1][m] : X[2][m]); };
                 int const si = Acc::stride(ai), sj = Acc::stride(aj), sk = Acc::stride(C);
-                int const base = acc.base + C * tileTT;
-                float sj0[S + 1], sj1[S + 1], sk0[S + 1], sk1[S + 1];
-                SH::caArray(q0[1], false, sj0);
-                SH::caArray(q1[1], false, sj1);
-                SH::caArray(q0[2], false, sk0);
-                SH::caArray(q1[2], false, sk1);
-                float dsk[S];
-#pragma unroll
-                for(int k = 0; k < S; ++k)
-                    dsk[k] = fs(sk1[k], sk0[k]);
-                float const ncsd = -sel(csd, C);
-#pragma unroll
-                for(int i = begin; i < end; ++i)
+                float const ncsd = -(c0 ? csd[0] : (c1 ? csd[1] : csd[2]));
+                float const ncsd12 = fm(ncsd, 1.0f / 12.0f);
+                float cum[S - 1], cumHi[S - 1];
                 {
-                    float const s0i = SH::ca(fs(float(i), q0[0]));
-                    float const dsi = fs(SH::ca(fs(float(i), q1[0])), s0i);
+                    float run = 0.0f;
 #pragma unroll
-                    for(int j = begin; j < end; ++j)
+                    for(int k = 0; k < S - 1; ++k)
                     {
-                        float const s0j = sj0[j - begin];
-                        float const dsj = fs(sj1[j - begin], s0j);
-                        float const half = fm(0.5f, __fmaf_rn(dsi, s0j, fm(s0i, dsj)));
-                        float const tmp = fm(ncsd, __fmaf_rn(fm(1.0f / 3.0f, dsj), dsi, __fmaf_rn(s0i, s0j, half)));
-                        float run = 0.0f;
+                        run = fa(run, pick(D, C, k));
+                        cum[k] = run;
+                        cumHi[k] = fm(run, hiStep);
+                    }
+                }
+                float Aj[S], Dj[S];
+#pragma unroll
+                for(int m = 0; m < S; ++m)
+                {
+                    Aj[m] = pick(A, aj, m);
+                    Dj[m] = pick(D, aj, m);
+                }
+                int const base = acc.base + C * tileTT + begin * (si + sj + sk);
+#pragma unroll
+                for(int i = 0; i < S; ++i)
+                {
+                    float const ai_ = fm(ncsd, pick(A, ai, i));
+                    float const di_ = fm(ncsd12, pick(D, ai, i));
+#pragma unroll
+                    for(int j = 0; j < S; ++j)
+                    {
+                        float const T = __fmaf_rn(ai_, Aj[j], fm(di_, Dj[j]));
                         int const row = base + i * si + j * sj;
 #pragma unroll
-                        for(int k = begin; k < end - 1; ++k)
-                        {
-                            run = __fmaf_rn(dsk[k - begin], tmp, run);
-                            acc.addAt(row + k * sk, run);
-                        }
+                        for(int k = 0; k < S - 1; ++k)
+                            acc.addProduct(row + k * sk, T, cum[k], cumHi[k], magicHi);
                     }
                 }
             }
