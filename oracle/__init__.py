@@ -58,6 +58,17 @@ class OrcField(ctypes.Structure):
     _fields_ = [("c", ctypes.c_void_p * 3)]
 
 
+class OrcParticles64(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_uint64),
+        ("pos", ctypes.c_void_p * 3),
+        ("mom", ctypes.c_void_p * 3),
+        ("w", ctypes.c_void_p),
+        ("sc", ctypes.c_void_p),
+        ("lcell", ctypes.c_void_p),
+    ]
+
+
 class OrcParticles(ctypes.Structure):
     _fields_ = [
         ("n", ctypes.c_uint64),
@@ -115,6 +126,8 @@ def lib() -> ctypes.CDLL:
             P(OrcField),
             ctypes.c_int,
         ]
+        L.orc_step_f64.argtypes = [P(OrcGrid), ctypes.c_int, P(OrcSpecies), P(OrcParticles64), P(OrcField),
+                                   P(OrcField), P(OrcField), ctypes.c_int]
         L.orc_charge_density.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), vp]
         L.orc_charge_residual.restype = ctypes.c_double
         L.orc_charge_residual.argtypes = [P(OrcGrid), P(OrcField), vp, vp]
@@ -236,6 +249,37 @@ def step(g, species_list, plist, E, B, J, threads: int = 1):
     S = (OrcSpecies * n)(*[species(s) for s in species_list])
     P = (OrcParticles * n)(*[particles(p) for p in plist])
     lib().orc_step(grid(g), n, S, P, field(E), field(B), field(J), int(threads))
+
+
+def _field64(F: np.ndarray) -> OrcField:
+    assert F.dtype == np.float64 and F.shape[0] == 3 and F.flags["C_CONTIGUOUS"]
+    f = OrcField()
+    for d in range(3):
+        f.c[d] = F[d].ctypes.data
+    return f
+
+
+def _particles64(p: dict) -> OrcParticles64:
+    for k, dt in (("pos", np.float64), ("mom", np.float64), ("w", np.float64), ("sc", np.int32),
+                  ("lcell", np.uint16)):
+        assert p[k].dtype == dt and p[k].flags["C_CONTIGUOUS"], k
+    o = OrcParticles64()
+    o.n = p["w"].shape[0]
+    for d in range(3):
+        o.pos[d] = p["pos"][d].ctypes.data
+        o.mom[d] = p["mom"][d].ctypes.data
+    o.w = _ptr(p["w"])
+    o.sc = _ptr(p["sc"])
+    o.lcell = _ptr(p["lcell"])
+    return o
+
+
+def step_f64(g, species_list, plist, E, B, J, threads: int = 1):
+    """One step of the FP64 instantiation: particles and fields as float64 arrays (in place)."""
+    n = len(species_list)
+    S = (OrcSpecies * n)(*[species(s) for s in species_list])
+    P = (OrcParticles64 * n)(*[_particles64(p) for p in plist])
+    lib().orc_step_f64(grid(g), n, S, P, _field64(E), _field64(B), _field64(J), int(threads))
 
 
 def gather(g, shape, F, is_b, cell, pos):

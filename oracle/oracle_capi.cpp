@@ -39,6 +39,20 @@ extern "C"
         int32_t* sc;
         uint16_t* lcell;
     };
+    // the FP64 instantiation's exchange format (reference gradients of the differentiable run)
+    struct orc_field64
+    {
+        double* c[3];
+    };
+    struct orc_particles64
+    {
+        uint64_t n;
+        double* pos[3];
+        double* mom[3];
+        double* w;
+        int32_t* sc;
+        uint16_t* lcell;
+    };
 }
 
 namespace
@@ -240,6 +254,39 @@ extern "C"
             P[i] = toP(&p[i]);
         }
         auto Ef = toF(E), Bf = toF(B), Jf = toF(J);
+        orc::step(toGrid(g), nspecies, sp.data(), P.data(), Ef, Bf, Jf, depositThreads);
+    }
+
+    // One PIC step of the FP64 instantiation (every float_X operation in double; the grid's
+    // cell sizes, dt, c and eps0 as given in orc_grid).
+    void orc_step_f64(
+        orc_grid const* g,
+        int nspecies,
+        orc_species const* s,
+        orc_particles64* p,
+        orc_field64* E,
+        orc_field64* B,
+        orc_field64* J,
+        int depositThreads)
+    {
+        std::vector<orc::SpeciesParam> sp(nspecies);
+        std::vector<orc::Particles<double>> P(nspecies);
+        for(int i = 0; i < nspecies; ++i)
+        {
+            sp[i] = toSp(&s[i]);
+            orc::Particles<double>& r = P[i];
+            r.n = p[i].n;
+            for(int d = 0; d < 3; ++d)
+            {
+                r.pos[d] = p[i].pos[d];
+                r.mom[d] = p[i].mom[d];
+            }
+            r.w = p[i].w;
+            r.sc = p[i].sc;
+            r.lcell = p[i].lcell;
+        }
+        orc::Field3<double> Ef{{E->c[0], E->c[1], E->c[2]}}, Bf{{B->c[0], B->c[1], B->c[2]}},
+            Jf{{J->c[0], J->c[1], J->c[2]}};
         orc::step(toGrid(g), nspecies, sp.data(), P.data(), Ef, Bf, Jf, depositThreads);
     }
 
