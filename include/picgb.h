@@ -173,7 +173,12 @@ extern "C"
      * ppc particles per cell at uniform random in-cell positions, momenta
      * u = drift + u_th * N(0,1) per component (u = gamma*beta, macro momentum = u m w c),
      * weighting w = density * cell volume / ppc.  Species given the same
-     * position_seed get identical positions (a quasi-neutral start). */
+     * position_seed get identical positions (a quasi-neutral start).
+     * quiet[0..2] > 0 selects startPosition::Quiet instead (particles/startPosition/QuietImpl.hpp:40-110):
+     * quiet[0] x quiet[1] x quiet[2] particles per cell on the in-cell lattice
+     * i * s + s / 2, s = 1 / quiet[d] (float, two roundings, as the reference evaluates it);
+     * ppc must then be 0 or that product.  The reference's MIN_WEIGHTING reduction of the
+     * lattice works on SI real-particle counts and is left to the caller's choice of quiet. */
     typedef struct picgb_plasma_init
     {
         uint32_t ppc;
@@ -185,6 +190,7 @@ extern "C"
         int32_t split_cell;
         uint64_t seed;
         uint64_t position_seed;
+        uint32_t quiet[3]; /* lattice per axis of the quiet start; all 0: random start */
     } picgb_plasma_init;
     int picgb_species_init_plasma(picgb_sim* sim, int32_t species, const picgb_plasma_init* init);
     /* Copies all particles out (supercell order; order inside a supercell is not defined). */
@@ -237,12 +243,18 @@ extern "C"
      * plane y = surface (total side) and the B plane below it; the field solver stages add the
      * incident E (B half steps, at times step*dt and (step+1)*dt) and the incident B (E step,
      * at (step+1/2)*dt) on that surface.  The pulse travels along +y (axis 1, the only axis
-     * supported), polarised along x (0) or z (1):
-     *   E = E0 exp(-r^2/waist^2) exp(-(tau - t_center)^2 / (2 sigma^2)) sin(omega (tau - t_center) + phase),
-     *   tau = t - (y - surface*dy)/c, r the distance from (center_x, center_z) in cells,
-     *   omega = 2 pi c / wavelength, E0 = a0 omega c / e_over_m, sigma = duration_fwhm / (2 sqrt(ln 2))
-     * (duration_fwhm of the intensity).  There is no focusing: the waist is the same at every y.
-     * enabled = 0 switches it off. */
+     * supported), polarised along x (0) or z (1), as the focused Gaussian beam of
+     * profiles/GaussianPulse.hpp:223-290 (fundamental mode, B from E by the slowly varying
+     * envelope approximation, incidentField::detail::ApproximateIncidentB):
+     *   E = E0 (w0/w) exp(-r^2/w^2) exp(-(tau - t_center - r_c/c)^2 / (2 sigma^2))
+     *       sin(omega (tau - t_center) - k r_c + xi + phase),
+     *   tau = t - (y - surface*dy)/c, r the distance from (center_x, center_z),
+     *   z_f = (surface + focus) dy - y the distance to the focus, z_R = pi w0^2 / wavelength,
+     *   w = w0 sqrt(1 + (z_f/z_R)^2), r_c = r^2/2 * (-z_f / (z_R^2 + z_f^2)) (wavefront curvature),
+     *   xi = atan(-z_f / z_R) (Gouy phase), w0 = waist,
+     *   omega = 2 pi c / wavelength, k = omega / c, E0 = a0 omega c / e_over_m,
+     *   sigma = duration_fwhm / (2 sqrt(ln 2)) (duration_fwhm of the intensity).
+     * focus = 0 puts the focus on the surface.  enabled = 0 switches it off. */
     typedef struct picgb_incident_field
     {
         int32_t enabled;
@@ -250,6 +262,7 @@ extern "C"
         int32_t surface;
         int32_t polarisation;
         float a0, e_over_m, wavelength, waist, duration_fwhm, t_center, center_x, center_z, phase;
+        float focus; /* distance of the focus beyond the surface along +y, in cells */
     } picgb_incident_field;
     int picgb_set_incident_field(picgb_sim* sim, const picgb_incident_field* field);
 
@@ -387,9 +400,12 @@ extern "C"
      * state) from dL/d(final state): transposed curls for the field update, the transposed
      * Jacobian of the Boris rotation and of Velocity for the push, a deposit of the adjoint
      * force for the gather and a gather of the adjoint current with the derivatives of the
-     * Esirkepov weights for the deposit.  The forward keeps a state every checkpoint_every
-     * steps; the backward replays each segment from its checkpoint.  T = float (precision 4)
-     * or double (precision 8); all arrays are device memory the caller owns. */
+     * Esirkepov weights for the deposit.  The forward keeps the particles every
+     * checkpoint_every steps and the fields E, B of every step (when 2 x nsteps field copies
+     * fit in a quarter of the free device memory); the backward replays each segment from its
+     * checkpoint, moving only the particles through the stored fields (without the stored
+     * fields it replays whole steps).  T = float (precision 4) or double (precision 8); all
+     * arrays are device memory the caller owns. */
 #define PICGB_DIFF_MAX_SPECIES 4
     typedef struct picgb_diff picgb_diff;
     typedef struct picgb_diff_config

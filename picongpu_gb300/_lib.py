@@ -65,13 +65,14 @@ class BufferDesc(ctypes.Structure):
 class PlasmaInit(ctypes.Structure):
     _fields_ = [("ppc", c_uint32), ("density", c_float), ("u_th", c_float), ("drift_lo", c_float * 3),
                 ("drift_hi", c_float * 3), ("split_axis", c_int), ("split_cell", c_int), ("seed", c_uint64),
-                ("position_seed", c_uint64)]
+                ("position_seed", c_uint64), ("quiet", c_uint32 * 3)]
 
 
 class IncidentField(ctypes.Structure):
     _fields_ = [("enabled", c_int), ("axis", c_int), ("surface", c_int), ("polarisation", c_int), ("a0", c_float),
                 ("e_over_m", c_float), ("wavelength", c_float), ("waist", c_float), ("duration_fwhm", c_float),
-                ("t_center", c_float), ("center_x", c_float), ("center_z", c_float), ("phase", c_float)]
+                ("t_center", c_float), ("center_x", c_float), ("center_z", c_float), ("phase", c_float),
+                ("focus", c_float)]
 
 
 class EnsembleConfig(ctypes.Structure):

@@ -1,6 +1,7 @@
 // Seeded plasma initialisation directly into the supercell layout: uniform
 // random in-cell positions (startPosition::Random,
-// particles/startPosition/RandomImpl.hpp), Maxwellian momenta plus a drift
+// particles/startPosition/RandomImpl.hpp) or the in-cell lattice of
+// startPosition::Quiet (particles/startPosition/QuietImpl.hpp:40-110), Maxwellian momenta plus a drift
 // (manipulators Temperature/Drift, particles/manipulators/unary/Temperature.hpp:61-108).
 // Counter-based random numbers: the value of every attribute depends only on
 // (seed, global cell, particle-in-cell, attribute), not on the launch shape.
@@ -50,9 +51,28 @@ namespace picgb
             uint64_t const gc = uint64_t(c[0]) + uint64_t(g.nx) * (uint64_t(c[1]) + uint64_t(g.ny) * c[2]);
             uint64_t const pid = gc * ip.ppc + p;
             size_t const s = base + k;
-            sp.px[s] = uniform01(ip.position_seed, 3 * pid);
-            sp.py[s] = uniform01(ip.position_seed, 3 * pid + 1);
-            sp.pz[s] = uniform01(ip.position_seed, 3 * pid + 2);
+            if(ip.quiet[0] == 0u)
+            {
+                sp.px[s] = uniform01(ip.position_seed, 3 * pid);
+                sp.py[s] = uniform01(ip.position_seed, 3 * pid + 1);
+                sp.pz[s] = uniform01(ip.position_seed, 3 * pid + 2);
+            }
+            else
+            {
+                // lattice coordinate of particle p (x fastest, pmacc::math::mapToND) and
+                // position coordinate * spacing + spacing * 0.5 in float_X
+                uint32_t const q[3] = {p % ip.quiet[0], (p / ip.quiet[0]) % ip.quiet[1], p / (ip.quiet[0] * ip.quiet[1])};
+                float pos[3];
+#pragma unroll
+                for(int d = 0; d < 3; ++d)
+                {
+                    float const spacing = fdv(1.0f, float(ip.quiet[d]));
+                    pos[d] = fa(fm(float(q[d]), spacing), fm(spacing, 0.5f));
+                }
+                sp.px[s] = pos[0];
+                sp.py[s] = pos[1];
+                sp.pz[s] = pos[2];
+            }
             bool const hi = ip.split_axis >= 0 && c[ip.split_axis] >= ip.split_cell;
             float const* drift = hi ? ip.drift_hi : ip.drift_lo;
             float const mw = ip.mass * ip.weight * ip.c; // u (units of c) -> macro momentum

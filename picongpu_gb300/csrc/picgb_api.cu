@@ -664,13 +664,21 @@ extern "C"
     {
         if(int r = checkSpecies(s, si))
             return r;
-        if(!init || init->ppc == 0)
+        if(!init)
+            return fail(PICGB_ERR_INVALID, "null plasma init");
+        bool const quiet = init->quiet[0] || init->quiet[1] || init->quiet[2];
+        uint64_t const lattice = uint64_t(init->quiet[0]) * init->quiet[1] * init->quiet[2];
+        if(quiet && (lattice == 0 || lattice > 65504 || (init->ppc != 0 && init->ppc != lattice)))
+            return fail(PICGB_ERR_INVALID, "quiet start %ux%ux%u: every axis needs particles, and ppc must be 0 or "
+                        "their product", unsigned(init->quiet[0]), unsigned(init->quiet[1]), unsigned(init->quiet[2]));
+        uint32_t const ppc = quiet ? uint32_t(lattice) : init->ppc;
+        if(ppc == 0)
             return fail(PICGB_ERR_INVALID, "plasma init needs ppc > 0");
         if(init->split_axis > 2 || !(init->u_th >= 0.0f) || !(init->density >= 0.0f))
             return fail(PICGB_ERR_INVALID, "invalid plasma init parameters");
         Species& sp = *s->species[si];
         CUDA_TRY(cudaSetDevice(s->cfg.device));
-        uint64_t const perSc = uint64_t(init->ppc) * s->sc[0] * s->sc[1] * s->sc[2];
+        uint64_t const perSc = uint64_t(ppc) * s->sc[0] * s->sc[1] * s->sc[2];
         uint64_t cap = sp.cfg.capacity ? sp.cfg.capacity : uint64_t(std::ceil(1.25 * perSc));
         cap = (std::max<uint64_t>(cap, 32) + 31) / 32 * 32;
         if(cap < perSc || cap > 65504)
@@ -682,8 +690,8 @@ extern "C"
                 return r;
         }
         InitParams ip{};
-        ip.ppc = init->ppc;
-        ip.weight = init->density * s->cellVolume() / float(init->ppc);
+        ip.ppc = ppc;
+        ip.weight = init->density * s->cellVolume() / float(ppc);
         sp.wmax = std::fabs(ip.weight);
         ip.mass = sp.cfg.mass;
         ip.c = s->cfg.c;
@@ -697,6 +705,8 @@ extern "C"
         ip.split_cell = init->split_cell;
         ip.seed = init->seed;
         ip.position_seed = init->position_seed;
+        for(int d = 0; d < 3; ++d)
+            ip.quiet[d] = quiet ? init->quiet[d] : 0u;
         CUDA_TRY(cudaMemsetAsync(sp.dev.sp_count, 0, sizeof(uint32_t), s->stream));
         CUDA_TRY(launchInitPlasma(sp.dev, s->g, ip, s->sc, s->stream));
         ++s->launches;
@@ -1090,6 +1100,11 @@ extern "C"
         p.cx = f->center_x;
         p.cz = f->center_z;
         p.phase = f->phase;
+        if(!(f->focus == f->focus))
+            return fail(PICGB_ERR_INVALID, "incident field: focus is not a number");
+        p.yf = float(f->surface) + f->focus;
+        p.zR = float(3.14159265358979323846 * double(f->waist) * double(f->waist) / double(f->wavelength));
+        p.k = float(omega / s->cfg.c);
         s->inc = p;
         return PICGB_OK;
     }

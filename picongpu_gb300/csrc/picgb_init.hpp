@@ -22,6 +22,7 @@ namespace picgb
         int split_cell;
         uint64_t seed; // momenta
         uint64_t position_seed; // positions (species sharing it get identical positions)
+        uint32_t quiet[3]; // lattice per axis (startPosition::Quiet); quiet[0] == 0: random positions
     };
 
     cudaError_t launchInitPlasma(

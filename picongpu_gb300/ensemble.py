@@ -36,11 +36,12 @@ def _species_config(sp: Species) -> L.SpeciesConfig:
 
 
 def plasma_init(ppc: int, density: float, u_th: float, drift_lo=(0.0, 0.0, 0.0), drift_hi=None, split_axis: int = -1,
-                split_cell: int = 0, seed: int = 42, position_seed: int = 42) -> L.PlasmaInit:
-    """One box's seeded plasma (the fields of picgb_plasma_init)."""
+                split_cell: int = 0, seed: int = 42, position_seed: int = 42, quiet=None) -> L.PlasmaInit:
+    """One box's seeded plasma (the fields of picgb_plasma_init); quiet=(nx, ny, nz) selects the
+    lattice start."""
     return L.PlasmaInit(ppc, density, u_th, (ctypes.c_float * 3)(*drift_lo),
                         (ctypes.c_float * 3)(*(drift_hi if drift_hi is not None else drift_lo)), split_axis,
-                        split_cell, seed, position_seed)
+                        split_cell, seed, position_seed, (ctypes.c_uint32 * 3)(*(quiet or (0, 0, 0))))
 
 
 class Ensemble:

@@ -200,10 +200,13 @@ class Simulation:
         L.call("picgb_species_set", self.handle, i, ctypes.byref(d))
 
     def init_plasma(self, name: str, ppc: int, density: float, u_th: float, drift_lo=(0, 0, 0), drift_hi=None,
-                    split_axis: int = -1, split_cell: int = 0, seed: int = 42, position_seed: int = 42) -> None:
+                    split_axis: int = -1, split_cell: int = 0, seed: int = 42, position_seed: int = 42,
+                    quiet=None) -> None:
+        """Seeded plasma on the device: random in-cell positions (startPosition::Random), or with
+        quiet=(nx, ny, nz) the in-cell lattice of startPosition::Quiet (ppc 0 or nx*ny*nz)."""
         ip = L.PlasmaInit(ppc, density, u_th, (ctypes.c_float * 3)(*drift_lo),
                           (ctypes.c_float * 3)(*(drift_hi if drift_hi is not None else drift_lo)), split_axis,
-                          split_cell, seed, position_seed)
+                          split_cell, seed, position_seed, (ctypes.c_uint32 * 3)(*(quiet or (0, 0, 0))))
         L.call("picgb_species_init_plasma", self.handle, self.species_index(name), ctypes.byref(ip))
 
     def particle_count(self, name: str) -> int:
@@ -294,12 +297,13 @@ class Simulation:
     # ------------------------------------------------------------ stepping
     def set_incident_field(self, a0: float, wavelength: float, waist: float, duration_fwhm: float, t_center: float,
                            surface: int, polarisation: int = 0, center=None, phase: float = 0.0,
-                           e_over_m: float = 1.0) -> None:
-        """Gaussian pulse entering along +y through the TF/SF surface y = surface
-        (fields/incidentField/Solver.hpp); see picgb_set_incident_field."""
+                           e_over_m: float = 1.0, focus: float = 0.0) -> None:
+        """Focused Gaussian pulse entering along +y through the TF/SF surface y = surface
+        (fields/incidentField/Solver.hpp, profiles/GaussianPulse.hpp), its focus `focus`
+        cells beyond the surface; see picgb_set_incident_field."""
         cx, cz = center if center is not None else (self.grid.nx / 2.0, self.grid.nz / 2.0)
         f = L.IncidentField(1, 1, surface, polarisation, a0, e_over_m, wavelength, waist, duration_fwhm, t_center, cx, cz,
-                            phase)
+                            phase, focus)
         L.call("picgb_set_incident_field", self.handle, ctypes.byref(f))
 
     def clear_incident_field(self) -> None:
