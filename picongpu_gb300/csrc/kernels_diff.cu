@@ -130,7 +130,8 @@ namespace picgb::diff
             return;
         ParticleStep<SHAPE, T> st;
         st.run(sp, p, E, B, g, nullptr, gathered);
-        esirkepovDeposit(st.traj, st.qvdt(g), g, J);
+        if(J) // the replay of the backward pass moves the particles only
+            esirkepovDeposit(st.traj, st.qvdt(g), g, J);
         for(int d = 0; d < 3; ++d)
         {
             sp.cellOut[d * sp.n + p] = st.newCell[d];

@@ -2,6 +2,12 @@
 // arrays with checkpoints every K steps, and the backward pass that replays
 // each segment from its checkpoint and runs the adjoint steps in reverse.
 //
+// Checkpoints: the particles every K steps, the fields (E, B: a few MB per step) at
+// every step when they fit in a quarter of the free device memory.  The replay of a
+// segment then only moves the particles through the stored fields (gather, push,
+// move: no deposit, no field update), and the adjoint steps read the forward's own
+// fields.  Otherwise the replay runs the whole step from the segment's checkpoint.
+//
 // Adjoint of one step (forward: J = push(x, u, E, B); B1 = B - dt/2 Cf E;
 // E1 = E + c^2 dt Cb B1 + coeff J; B2 = B1 - dt/2 Cf E1, with Cf / Cb the
 // forward / backward difference curls of FDTDBase.hpp:97-183 and Cf^T = Cb):
@@ -47,10 +53,18 @@ struct picgb_diff
     std::vector<void*> ckpts; // state at steps 0, K, 2K, ...
     std::vector<void*> seg; // states of one segment during the backward pass
     std::vector<void*> gathered; // per step of a segment: the particles' gathered E, B and gradients ([24][n])
+    void* fieldHist = nullptr; // E and B at the start of every forward step (histSteps entries)
+    size_t histSteps = 0;
+    bool denseFields = false; // the last forward stored its fields at every step
     uint32_t nsteps = 0;
     bool haveForward = false;
 
     size_t fieldBytes() const { return 3 * nc * esz; }
+    size_t fieldStride() const { return (fieldBytes() + 255) / 256 * 256; }
+
+    // E and B of forward step i in the dense field history
+    void* histE(size_t i) const { return static_cast<char*>(fieldHist) + 2 * i * fieldStride(); }
+    void* histB(size_t i) const { return static_cast<char*>(fieldHist) + (2 * i + 1) * fieldStride(); }
 
     // offsets of a state blob: E, B, then per species cell, pos, mom (256-byte aligned)
     StatePtrs blobPtrs(void* blob) const
@@ -167,6 +181,46 @@ namespace
         CUDA_TRY(launchDiffAxpby(d->prec, s2.E, -dt / d->g.eps0, d->J, 1.0, 3 * d->nc, st));
         CUDA_TRY(launchDiffCurlAdd(d->prec, s2.B, s2.E, -0.5 * dt, true, d->g, st));
         return PICGB_OK;
+    }
+
+    // Replay of forward step i for the particles only, through the stored fields of that step:
+    // particles of state s -> state o, the gathered fields to `gathered`.
+    int stepReplayParticles(picgb_diff* d, size_t i, StatePtrs const& s, StatePtrs const& o, cudaStream_t st, void* gathered)
+    {
+        for(size_t k = 0; k < d->species.size(); ++k)
+        {
+            DiffSpeciesPtr sp = d->speciesPtr(s, k);
+            sp.cellOut = o.cell[k];
+            sp.posOut = o.pos[k];
+            sp.momOut = o.mom[k];
+            CUDA_TRY(launchDiffPush(d->prec, d->cfg.shape, sp, d->histE(i), d->histB(i), nullptr,
+                                    d->gatheredPtr(gathered, k), d->g, st));
+        }
+        return PICGB_OK;
+    }
+
+    // Room for the fields of every step of an n-step forward, if it fits in a quarter of the
+    // free device memory; false otherwise (the backward pass then replays whole steps).
+    bool ensureFieldHistory(picgb_diff* d, size_t n)
+    {
+        if(d->fieldHist && d->histSteps >= n)
+            return true;
+        size_t const bytes = 2 * n * d->fieldStride();
+        size_t freeB = 0, total = 0;
+        if(cudaMemGetInfo(&freeB, &total) != cudaSuccess || bytes > freeB / 4)
+            return false;
+        if(d->fieldHist)
+            cudaFree(d->fieldHist);
+        d->fieldHist = nullptr;
+        d->histSteps = 0;
+        if(cudaMalloc(&d->fieldHist, bytes) != cudaSuccess)
+        {
+            cudaGetLastError();
+            d->fieldHist = nullptr;
+            return false;
+        }
+        d->histSteps = n;
+        return true;
     }
 
     // Adjoint of the step that started in state s; lam holds dL/d(state after) on entry.
@@ -292,6 +346,8 @@ extern "C"
             cudaFree(p);
         for(void* p : d->gathered)
             cudaFree(p);
+        if(d->fieldHist)
+            cudaFree(d->fieldHist);
         if(d->J)
             cudaFree(d->J);
         if(d->lamJ)
@@ -315,11 +371,17 @@ extern "C"
         if(int r = ensureBlobs(d, nckpt))
             return r;
         StatePtrs const s = callerPtrs(d, state);
+        d->denseFields = ensureFieldHistory(d, nsteps);
         for(uint32_t i = 0; i < nsteps; ++i)
         {
             if(i % K == 0)
                 if(int r = copyState(d, d->blobPtrs(d->ckpts[i / K]), s, st))
                     return r;
+            if(d->denseFields)
+            {
+                CUDA_TRY(cudaMemcpyAsync(d->histE(i), s.E, d->fieldBytes(), cudaMemcpyDeviceToDevice, st));
+                CUDA_TRY(cudaMemcpyAsync(d->histB(i), s.B, d->fieldBytes(), cudaMemcpyDeviceToDevice, st));
+            }
             if(int r = stepForward(d, s, s, st))
                 return r;
         }
@@ -350,12 +412,25 @@ extern "C"
             if(int r = copyState(d, d->blobPtrs(d->seg[0]), d->blobPtrs(d->ckpts[sidx]), st))
                 return r;
             for(size_t i = a; i + 1 < b; ++i)
-                if(int r = stepForward(d, d->blobPtrs(d->seg[i - a]), d->blobPtrs(d->seg[i - a + 1]), st, d->gathered[i - a]))
+            {
+                StatePtrs const in = d->blobPtrs(d->seg[i - a]), out = d->blobPtrs(d->seg[i - a + 1]);
+                int const r = d->denseFields ? stepReplayParticles(d, i, in, out, st, d->gathered[i - a])
+                                             : stepForward(d, in, out, st, d->gathered[i - a]);
+                if(r)
                     return r;
+            }
             // the last step of the segment was not replayed: its adjoint gathers the fields itself
             for(size_t i = b; i-- > a;)
-                if(int r = stepAdjoint(d, d->blobPtrs(d->seg[i - a]), lam, st, i + 1 < b ? d->gathered[i - a] : nullptr))
+            {
+                StatePtrs s = d->blobPtrs(d->seg[i - a]);
+                if(d->denseFields)
+                {
+                    s.E = d->histE(i);
+                    s.B = d->histB(i);
+                }
+                if(int r = stepAdjoint(d, s, lam, st, i + 1 < b ? d->gathered[i - a] : nullptr))
                     return r;
+            }
         }
         return PICGB_OK;
     }
