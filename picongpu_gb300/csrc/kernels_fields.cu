@@ -101,13 +101,22 @@ namespace picgb
     }
 
     // ------------------------------------------------------------ incident field (TF/SF)
-    // Incident pulse value at (x, y, z) in cell units and time t (see IncidentParams).
+    // Incident pulse value at (x, y, z) in cell units and time t: the focused Gaussian beam of
+    // profiles/GaussianPulse.hpp:223-290 in its fundamental mode (waist w(z_f), wavefront
+    // curvature, Gouy phase, amplitude w0/w, the envelope shifted by the curvature's delay).
     __device__ __forceinline__ float incidentValue(IncidentParams const& p, GridParams const& g, float x, float y, float z, float t)
     {
         float const rx = (x - p.cx) * g.dx, rz = (z - p.cz) * g.dz;
+        float const r2 = rx * rx + rz * rz;
         float const tau = t - (y - float(p.j0)) * g.dy / g.c - p.tc;
-        float const env = expf(-(rx * rx + rz * rz) / (p.w0 * p.w0)) * expf(-(tau * tau) / (2.0f * p.sigma * p.sigma));
-        return p.E0 * env * sinf(p.omega * tau + p.phase);
+        float const zf = (p.yf - y) * g.dy; // distance to the focus along the propagation
+        float const q = zf / p.zR;
+        float const w2 = p.w0 * p.w0 * (1.0f + q * q);
+        float const rc = 0.5f * r2 * (-zf / (p.zR * p.zR + zf * zf)); // r^2/2 times the inverse curvature radius
+        float const xi = atanf(-q); // Gouy phase
+        float const ts = tau - rc / g.c;
+        float const env = sqrtf(p.w0 * p.w0 / w2) * expf(-r2 / w2) * expf(-(ts * ts) / (2.0f * p.sigma * p.sigma));
+        return p.E0 * env * sinf(p.omega * tau - p.k * rc + xi + p.phase);
     }
 
     // After B -= dt/2 curl E: the B plane j0 - 1 (scattered side) used the total E of plane j0;

@@ -108,6 +108,9 @@ namespace picgb
         int j0; // first E plane of the total-field region
         int pol;
         float E0, omega, w0, sigma, tc, cx, cz, phase;
+        float yf; // focus plane (cells)
+        float zR; // Rayleigh length pi w0^2 / wavelength
+        float k; // wave number omega / c
     };
 
     // ---- launchers (kernels_*.cu); all asynchronous on `stream`
