@@ -312,6 +312,15 @@ extern "C"
     /* ------------------------------------------------------------ execution control */
     /* Enqueue on a caller's CUDA stream (cudaStream_t passed as void*); NULL = own stream. */
     int picgb_set_stream(picgb_sim* sim, void* stream);
+    /* Every `steps` steps (default 20; 0 = never) the step restores each pushed species'
+     * interleaved cell order inside every supercell after the compaction: round r holds the
+     * r-th particle of every cell with more than r, cells in index order.  Particles keep their
+     * slot while they move between cells, which spreads a warp's particles over the supercell and
+     * raises the push kernel's shared-memory bank conflicts (two-stream 256^3: 6 % after 200
+     * steps); the reorder moves every particle once (about 3 ms per species there).  The
+     * reference's particle order inside a supercell is not specified either
+     * (pmacc/particles/ParticlesBase.kernel:183-359 fills gaps in arbitrary order). */
+    int picgb_set_sort_interval(picgb_sim* sim, uint32_t steps);
     int picgb_synchronize(picgb_sim* sim);
     /* Device-side kernel launches issued by this handle since creation (own kernels only). */
     int picgb_launch_count(picgb_sim* sim, uint64_t* n);
@@ -330,7 +339,8 @@ extern "C"
         PICGB_KERNEL_YEE_E = 3, /* E step (+ J) */
         PICGB_KERNEL_DEPOSIT = 4, /* separate deposit (fuse_deposit = 0) */
         PICGB_KERNEL_ADD_CURRENT = 5, /* separate J add (fuse_deposit = 0) */
-        PICGB_KERNEL_CLASSES = 6
+        PICGB_KERNEL_REORDER = 6, /* interleaved cell order restored (picgb_set_sort_interval) */
+        PICGB_KERNEL_CLASSES = 7
     };
     int picgb_profile_enable(picgb_sim* sim, int32_t on);
     /* Total device milliseconds and launch count of one kernel class; synchronises. */
@@ -369,6 +379,9 @@ extern "C"
     /* nsteps batched steps; one graph launch per step, then a status check (an overflowing
      * supercell is re-laid out before the next step, as in picgb_step). */
     int picgb_ensemble_run(picgb_ensemble* ens, uint32_t nsteps);
+    /* picgb_set_sort_interval for every box and for the batched step (one batched reorder per
+     * species after every `steps`-th batched step); default 20, 0 = never. */
+    int picgb_ensemble_set_sort_interval(picgb_ensemble* ens, uint32_t steps);
     /* nsteps steps of the single-box path, box after box (picgb_run on each box). */
     int picgb_ensemble_run_sequential(picgb_ensemble* ens, uint32_t nsteps);
     /* Kernels launched by batched steps so far (nodes of the step graph times replays). */

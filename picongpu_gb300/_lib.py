@@ -128,6 +128,8 @@ SIGNATURES = [
     ("picgb_energies", c_int, [c_void_p, P(c_double), ctypes.c_size_t]),
     ("picgb_charge_residual", c_int, [c_void_p, P(c_double), P(c_double)]),
     ("picgb_set_stream", c_int, [c_void_p, c_void_p]),
+    ("picgb_set_sort_interval", c_int, [c_void_p, c_uint32]),
+    ("picgb_ensemble_set_sort_interval", c_int, [c_void_p, c_uint32]),
     ("picgb_synchronize", c_int, [c_void_p]),
     ("picgb_launch_count", c_int, [c_void_p, P(c_uint64)]),
     ("picgb_device_status", c_int, [c_void_p, P(c_uint32), c_int]),
@@ -165,7 +167,7 @@ SIGNATURES = [
     ("picgb_diff_kinetic_energy", c_int, [c_void_p, P(DiffState), c_int, P(c_double), c_void_p]),
 ]
 
-KERNEL_CLASSES = {"push": 0, "compact": 1, "yee_b": 2, "yee_e": 3, "deposit": 4, "add_current": 5}
+KERNEL_CLASSES = {"push": 0, "compact": 1, "yee_b": 2, "yee_e": 3, "deposit": 4, "add_current": 5, "reorder": 6}
 
 _lib = None
 

@@ -23,7 +23,7 @@ namespace picgb
         return THREADS >= 512 ? 2 : (THREADS >= 256 ? PICGB_BATCH_MIN_BLOCKS : 2 * PICGB_BATCH_MIN_BLOCKS);
     }
 
-    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT>
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT, bool EMZ>
     __global__ void __launch_bounds__(THREADS, batchMinBlocks<THREADS>()) kPushBatch(
         BatchSpecies const* __restrict__ table,
         uint32_t const* __restrict__ items,
@@ -50,7 +50,7 @@ namespace picgb
             for(int i = threadIdx.x; i < kWords; i += THREADS)
                 reinterpret_cast<uint32_t*>(&s_box)[i] = __ldg(src + i);
             __syncthreads();
-            pushSupercell<SHAPE, SX, SY, SZ, THREADS, ALT, false>(
+            pushSupercell<SHAPE, SX, SY, SZ, THREADS, ALT, EMZ>(
                 s_box.sp,
                 s_box.E,
                 s_box.B,
@@ -65,7 +65,7 @@ namespace picgb
         }
     }
 
-    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT>
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT, bool EMZ>
     cudaError_t launchPushBatchT(
         BatchSpecies const* table,
         uint32_t const* items,
@@ -75,7 +75,7 @@ namespace picgb
         cudaStream_t stream)
     {
         using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>, THREADS>;
-        auto k = kPushBatch<SHAPE, SX, SY, SZ, THREADS, ALT>;
+        auto k = kPushBatch<SHAPE, SX, SY, SZ, THREADS, ALT, EMZ>;
         size_t const smem = TG::pushSmem;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if(e != cudaSuccess)
@@ -96,34 +96,34 @@ namespace picgb
         return cudaGetLastError();
     }
 
-// Instantiates the batched launcher of one shape and pusher variant (ALT: HigueraCary
-// and Vay) for the supercell sizes 8x8x4, 4x4x4, 8x8x8 and 128, 256 or 512 threads per
-// supercell.  Each (shape, variant) pair has its own translation unit, so the
-// heaviest instantiations compile in parallel.
-#define PICGB_BATCH_CASES(F, SHAPE, ALT, ...)                                                                         \
+// Instantiates the batched launcher of one shape, pusher variant (ALT: HigueraCary and Vay)
+// and current scheme (EMZ: EmZ, else Esirkepov) for the supercell sizes 8x8x4, 4x4x4,
+// 8x8x8 and 128, 256 or 512 threads per supercell.  Each combination has its own
+// translation unit, so the heaviest instantiations compile in parallel.
+#define PICGB_BATCH_CASES(F, SHAPE, ALT, EMZ, ...)                                                                    \
     switch(scId * 3 + (threads == 128 ? 0 : (threads == 256 ? 1 : 2)))                                               \
     {                                                                                                                 \
     case 0:                                                                                                           \
-        return F<SHAPE, 8, 8, 4, 128, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 8, 8, 4, 128, ALT, EMZ>(__VA_ARGS__);                                                         \
     case 1:                                                                                                           \
-        return F<SHAPE, 8, 8, 4, 256, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 8, 8, 4, 256, ALT, EMZ>(__VA_ARGS__);                                                         \
     case 2:                                                                                                           \
-        return F<SHAPE, 8, 8, 4, 512, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 8, 8, 4, 512, ALT, EMZ>(__VA_ARGS__);                                                         \
     case 3:                                                                                                           \
-        return F<SHAPE, 4, 4, 4, 128, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 4, 4, 4, 128, ALT, EMZ>(__VA_ARGS__);                                                         \
     case 4:                                                                                                           \
-        return F<SHAPE, 4, 4, 4, 256, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 4, 4, 4, 256, ALT, EMZ>(__VA_ARGS__);                                                         \
     case 5:                                                                                                           \
-        return F<SHAPE, 4, 4, 4, 512, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 4, 4, 4, 512, ALT, EMZ>(__VA_ARGS__);                                                         \
     case 6:                                                                                                           \
-        return F<SHAPE, 8, 8, 8, 128, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 8, 8, 8, 128, ALT, EMZ>(__VA_ARGS__);                                                         \
     case 7:                                                                                                           \
-        return F<SHAPE, 8, 8, 8, 256, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 8, 8, 8, 256, ALT, EMZ>(__VA_ARGS__);                                                         \
     case 8:                                                                                                           \
-        return F<SHAPE, 8, 8, 8, 512, ALT>(__VA_ARGS__);                                                              \
+        return F<SHAPE, 8, 8, 8, 512, ALT, EMZ>(__VA_ARGS__);                                                         \
     }
 
-#define PICGB_BATCH_LAUNCHERS(SHAPE, NAME, ALT)                                                                       \
+#define PICGB_BATCH_LAUNCHERS(SHAPE, NAME, ALT, EMZ)                                                                  \
     cudaError_t launchPushBatch##NAME(                                                                                \
         int scId,                                                                                                     \
         int threads,                                                                                                  \
@@ -136,7 +136,7 @@ namespace picgb
     {                                                                                                                 \
         if(threads != 128 && threads != 256 && threads != 512)                                                        \
             return cudaErrorInvalidValue;                                                                             \
-        PICGB_BATCH_CASES(launchPushBatchT, SHAPE, ALT, table, items, nitems, counter, status, stream)                \
+        PICGB_BATCH_CASES(launchPushBatchT, SHAPE, ALT, EMZ, table, items, nitems, counter, status, stream)           \
         return cudaErrorInvalidValue;                                                                                 \
     }
 } // namespace picgb

@@ -1,0 +1,7 @@
+// Batched (ensemble) push kernels instantiated for the PCS shape, Boris and Free pushers, Esirkepov deposit.
+#include "kernels_batch.cuh"
+
+namespace picgb
+{
+    PICGB_BATCH_LAUNCHERS(4, PCS, false, false)
+} // namespace picgb

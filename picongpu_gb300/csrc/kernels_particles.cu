@@ -9,18 +9,20 @@
 
 namespace picgb
 {
-#define PICGB_DECL_SHAPE(NAME)                                                                                        \
+#define PICGB_DECL_BATCH(NAME)                                                                                        \
     cudaError_t launchPushBatch##NAME(int, int, BatchSpecies const*, uint32_t const*, uint32_t, uint32_t*, unsigned*, \
-                                      cudaStream_t);                                                                  \
-    cudaError_t launchPushBatch##NAME##Alt(                                                                           \
-        int,                                                                                                          \
-        int,                                                                                                          \
-        BatchSpecies const*,                                                                                          \
-        uint32_t const*,                                                                                              \
-        uint32_t,                                                                                                     \
-        uint32_t*,                                                                                                    \
-        unsigned*,                                                                                                    \
-        cudaStream_t);                                                                                                \
+                                      cudaStream_t);
+#define PICGB_DECL_BATCH_SHAPE(NAME)                                                                                  \
+    PICGB_DECL_BATCH(NAME)                                                                                            \
+    PICGB_DECL_BATCH(NAME##Alt)                                                                                       \
+    PICGB_DECL_BATCH(NAME##EmZ)                                                                                       \
+    PICGB_DECL_BATCH(NAME##AltEmZ)
+    PICGB_DECL_BATCH_SHAPE(CIC)
+    PICGB_DECL_BATCH_SHAPE(TSC)
+    PICGB_DECL_BATCH_SHAPE(PQS)
+    PICGB_DECL_BATCH_SHAPE(PCS)
+
+#define PICGB_DECL_SHAPE(NAME)                                                                                        \
     cudaError_t launchPush##NAME(                                                                                     \
         int,                                                                                                          \
         SpeciesDev const&,                                                                                            \
@@ -100,6 +102,7 @@ namespace picgb
         int scId,
         int threads,
         int pusher,
+        int current,
         BatchSpecies const* table,
         uint32_t const* items,
         uint32_t nitems,
@@ -108,21 +111,24 @@ namespace picgb
         cudaStream_t stream)
     {
         bool const alt = pusher == kPusherHigueraCary || pusher == kPusherVay;
-        switch(shape * 2 + (alt ? 1 : 0))
+        bool const emz = current == kCurrentEmZ;
+#define PICGB_BATCH_DISPATCH(NAME)                                                                                    \
+    return emz ? (alt ? launchPushBatch##NAME##AltEmZ(scId, threads, table, items, nitems, counter, status, stream)    \
+                      : launchPushBatch##NAME##EmZ(scId, threads, table, items, nitems, counter, status, stream))      \
+               : (alt ? launchPushBatch##NAME##Alt(scId, threads, table, items, nitems, counter, status, stream)       \
+                      : launchPushBatch##NAME(scId, threads, table, items, nitems, counter, status, stream));
+        switch(shape)
         {
+        case 1:
+            PICGB_BATCH_DISPATCH(CIC)
         case 2:
-            return launchPushBatchCIC(scId, threads, table, items, nitems, counter, status, stream);
+            PICGB_BATCH_DISPATCH(TSC)
         case 3:
-            return launchPushBatchCICAlt(scId, threads, table, items, nitems, counter, status, stream);
+            PICGB_BATCH_DISPATCH(PQS)
         case 4:
-            return launchPushBatchTSC(scId, threads, table, items, nitems, counter, status, stream);
-        case 5:
-            return launchPushBatchTSCAlt(scId, threads, table, items, nitems, counter, status, stream);
-        case 6:
-            return launchPushBatchPQS(scId, threads, table, items, nitems, counter, status, stream);
-        case 7:
-            return launchPushBatchPQSAlt(scId, threads, table, items, nitems, counter, status, stream);
+            PICGB_BATCH_DISPATCH(PCS)
         }
+#undef PICGB_BATCH_DISPATCH
         return cudaErrorInvalidValue;
     }
 
@@ -366,6 +372,193 @@ namespace picgb
                 return e;
         }
         kCompactBatch<<<nitems, 256, smem, stream>>>(boxes, items);
+        return cudaGetLastError();
+    }
+
+    // ------------------------------------------------------------ re-interleave
+    // The push keeps a particle in its slot while it moves between the cells of its supercell,
+    // so the cells of a warp's 32 particles drift away from the 8 x 4 patches that the tile
+    // pitches are chosen for, and the shared-memory bank conflicts of the gather and the deposit
+    // grow (two-stream 256^3: 25.5 ms per push launch after the initialisation, 27.0 ms 200
+    // steps later).  kReorder restores the interleaved order of the initialisation in place:
+    // round r holds the r-th particle of every cell with more than r particles, cells in
+    // index order, so slot k of a supercell whose cells all hold m particles is in cell
+    // k mod vol for k < m vol.  A counting sort in shared memory: per-cell ranks by shared
+    // atomics, one bitmap of occupied cells per round, positions from popcounts, then every
+    // attribute moved once through shared memory.  A supercell with a cell of more than
+    // kReorderRounds particles keeps its order.
+    constexpr int kReorderRounds = 64;
+    constexpr int kReorderThreads = 512;
+
+    struct ReorderSmem
+    {
+        // word offsets of the parts of the dynamic shared memory
+        __host__ __device__ static int cnt(int) { return 0; }
+        __host__ __device__ static int bm(int vol) { return vol; }
+        __host__ __device__ static int starts(int vol) { return vol + kReorderRounds * (vol / 32); }
+        __host__ __device__ static int rank(int vol) { return starts(vol) + kReorderRounds + 1; } // uint16 [cap]
+        __host__ __device__ static int inv(int vol, uint32_t cap) { return rank(vol) + int((cap + 1) / 2); } // uint16 [cap]
+        __host__ __device__ static int buf(int vol, uint32_t cap) { return inv(vol, cap) + int((cap + 1) / 2); } // uint32 [cap]
+        __host__ __device__ static size_t bytes(int vol, uint32_t cap) { return sizeof(uint32_t) * (size_t(buf(vol, cap)) + cap); }
+    };
+
+    template<typename T>
+    __device__ __forceinline__ void permuteInPlace(T* __restrict__ a, uint32_t n, uint32_t* buf, uint16_t const* inv)
+    {
+        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+            buf[k] = uint32_t(a[k]);
+        __syncthreads();
+        for(uint32_t j = threadIdx.x; j < n; j += blockDim.x)
+            a[j] = T(buf[inv[j]]);
+        __syncthreads();
+    }
+
+    __device__ __forceinline__ void permuteInPlaceF(float* __restrict__ a, uint32_t n, uint32_t* buf, uint16_t const* inv)
+    {
+        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+            buf[k] = __float_as_uint(a[k]);
+        __syncthreads();
+        for(uint32_t j = threadIdx.x; j < n; j += blockDim.x)
+            a[j] = __uint_as_float(buf[inv[j]]);
+        __syncthreads();
+    }
+
+    // Reorder of supercell sc by one block (rsm: ReorderSmem::bytes(vol, sp.cap) of shared memory).
+    __device__ void reorderSupercell(SpeciesDev const& sp, int sc, int vol, uint32_t* rsm, int& s_tooFull)
+    {
+        uint32_t const n = sp.count[sc];
+        if(n < 2)
+            return;
+        int const words = vol / 32;
+        uint32_t* cnt = rsm + ReorderSmem::cnt(vol);
+        uint32_t* bm = rsm + ReorderSmem::bm(vol);
+        uint32_t* starts = rsm + ReorderSmem::starts(vol);
+        uint16_t* rank = reinterpret_cast<uint16_t*>(rsm + ReorderSmem::rank(vol));
+        uint16_t* inv = reinterpret_cast<uint16_t*>(rsm + ReorderSmem::inv(vol, sp.cap));
+        uint32_t* buf = rsm + ReorderSmem::buf(vol, sp.cap);
+        size_t const base = size_t(sc) * sp.cap;
+        for(int i = threadIdx.x; i < ReorderSmem::starts(vol); i += blockDim.x)
+            rsm[i] = 0u;
+        if(threadIdx.x == 0)
+            s_tooFull = 0;
+        __syncthreads();
+        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        {
+            uint32_t const lc = sp.lcell[base + k];
+            buf[k] = lc;
+            if(lc >= uint32_t(vol)) // not a cell of this supercell: leave the order alone
+            {
+                s_tooFull = 1;
+                continue;
+            }
+            uint32_t const r = atomicAdd(cnt + lc, 1u);
+            rank[k] = uint16_t(r < 65535u ? r : 65535u);
+            if(r < uint32_t(kReorderRounds))
+                atomicOr(bm + r * words + lc / 32, 1u << (lc % 32));
+            else
+                s_tooFull = 1;
+        }
+        __syncthreads();
+        if(s_tooFull)
+            return; // uniform: every thread read it after the barrier
+        // first slot of every round: a prefix over the rounds' occupied cells
+        if(threadIdx.x < 32)
+        {
+            uint32_t carry = 0;
+            for(int r0 = 0; r0 < kReorderRounds; r0 += 32)
+            {
+                int const r = r0 + int(threadIdx.x);
+                uint32_t tot = 0;
+                for(int w = 0; w < words; ++w)
+                    tot += __popc(bm[r * words + w]);
+                uint32_t incl = tot;
+#pragma unroll
+                for(int o = 1; o < 32; o <<= 1)
+                {
+                    uint32_t const v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if(threadIdx.x >= unsigned(o))
+                        incl += v;
+                }
+                starts[r] = carry + incl - tot;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
+            }
+            if(threadIdx.x == 0)
+                starts[kReorderRounds] = carry;
+        }
+        __syncthreads();
+        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        {
+            uint32_t const lc = buf[k], r = rank[k];
+            uint32_t const* row = bm + r * words;
+            uint32_t before = 0;
+            for(uint32_t w = 0; w < lc / 32; ++w)
+                before += __popc(row[w]);
+            before += __popc(row[lc / 32] & ((1u << (lc % 32)) - 1u));
+            inv[starts[r] + before] = uint16_t(k);
+        }
+        __syncthreads();
+        permuteInPlaceF(sp.px + base, n, buf, inv);
+        permuteInPlaceF(sp.py + base, n, buf, inv);
+        permuteInPlaceF(sp.pz + base, n, buf, inv);
+        permuteInPlaceF(sp.ux + base, n, buf, inv);
+        permuteInPlaceF(sp.uy + base, n, buf, inv);
+        permuteInPlaceF(sp.uz + base, n, buf, inv);
+        permuteInPlaceF(sp.w + base, n, buf, inv);
+        permuteInPlace(sp.lcell + base, n, buf, inv);
+        if(sp.id)
+            permuteInPlace(sp.id + base, n, buf, inv);
+    }
+
+    __global__ void __launch_bounds__(kReorderThreads) kReorder(SpeciesDev sp, int vol)
+    {
+        extern __shared__ uint32_t rsm[];
+        __shared__ int s_tooFull;
+        reorderSupercell(sp, int(blockIdx.x), vol, rsm, s_tooFull);
+    }
+
+    // The reorder over the supercells of every box of an ensemble: block b handles work item b.
+    __global__ void __launch_bounds__(kReorderThreads)
+        kReorderBatch(BatchSpecies const* __restrict__ boxes, uint32_t const* __restrict__ items, int vol)
+    {
+        extern __shared__ uint32_t rsm[];
+        __shared__ int s_tooFull;
+        uint32_t const it = items[blockIdx.x];
+        reorderSupercell(boxes[batchBox(it)].sp, int(batchSc(it)), vol, rsm, s_tooFull);
+    }
+
+    size_t reorderSmemBytes(int vol, uint32_t cap) { return ReorderSmem::bytes(vol, cap); }
+
+    cudaError_t launchReorder(SpeciesDev const& sp, int nsc, int vol, cudaStream_t stream)
+    {
+        size_t const smem = ReorderSmem::bytes(vol, sp.cap);
+        if(smem > 48 * 1024)
+        {
+            cudaError_t e = cudaFuncSetAttribute(kReorder, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if(e != cudaSuccess)
+                return e;
+        }
+        kReorder<<<nsc, kReorderThreads, smem, stream>>>(sp, vol);
+        return cudaGetLastError();
+    }
+
+    cudaError_t launchReorderBatch(
+        BatchSpecies const* boxes,
+        uint32_t const* items,
+        uint32_t nitems,
+        int vol,
+        uint32_t maxCap,
+        cudaStream_t stream)
+    {
+        if(nitems == 0)
+            return cudaSuccess;
+        size_t const smem = ReorderSmem::bytes(vol, maxCap);
+        if(smem > 48 * 1024)
+        {
+            cudaError_t e = cudaFuncSetAttribute(kReorderBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if(e != cudaSuccess)
+                return e;
+        }
+        kReorderBatch<<<nitems, kReorderThreads, smem, stream>>>(boxes, items, vol);
         return cudaGetLastError();
     }
 

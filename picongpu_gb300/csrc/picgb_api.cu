@@ -413,6 +413,18 @@ namespace picgb::host
             Species& x = *sp;
             CUDA_TRY(timedLaunch(s, PICGB_KERNEL_COMPACT, [&] { return launchCompact(x.dev, s->nsc, s->stream); }));
         }
+        if(s->sortInterval && ++s->stepsSinceSort >= s->sortInterval)
+        {
+            s->stepsSinceSort = 0;
+            int const vol = s->sc[0] * s->sc[1] * s->sc[2];
+            for(auto& sp : s->species)
+            {
+                if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE || reorderSmemBytes(vol, sp->dev.cap) > 200 * 1024)
+                    continue;
+                Species& x = *sp;
+                CUDA_TRY(timedLaunch(s, PICGB_KERNEL_REORDER, [&] { return launchReorder(x.dev, s->nsc, vol, s->stream); }));
+            }
+        }
         return PICGB_OK;
     }
 } // namespace
@@ -1210,6 +1222,15 @@ extern "C"
     }
 
     // ------------------------------------------------------------ execution control
+    int picgb_set_sort_interval(picgb_sim* s, uint32_t steps)
+    {
+        if(int r = checkSim(s))
+            return r;
+        s->sortInterval = steps;
+        s->stepsSinceSort = 0;
+        return PICGB_OK;
+    }
+
     int picgb_set_stream(picgb_sim* s, void* stream)
     {
         if(int r = checkSim(s))

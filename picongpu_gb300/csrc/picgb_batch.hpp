@@ -47,11 +47,20 @@ namespace picgb
         int scId,
         int threads,
         int pusher, // selects the kernel variant (Boris/Free or HigueraCary/Vay)
+        int current, // Esirkepov or EmZ
         BatchSpecies const* table,
         uint32_t const* items,
         uint32_t nitems,
         uint32_t* counter,
         unsigned* status,
+        cudaStream_t stream);
+    // kReorder over every work item; maxCap = the largest slots per supercell of any box.
+    cudaError_t launchReorderBatch(
+        BatchSpecies const* boxes,
+        uint32_t const* items,
+        uint32_t nitems,
+        int vol,
+        uint32_t maxCap,
         cudaStream_t stream);
     cudaError_t launchCompactBatch(
         BatchSpecies const* boxes,

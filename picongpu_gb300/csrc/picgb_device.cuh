@@ -738,7 +738,9 @@ namespace picgb
         // multiply-add; the running sum along k is the prefix sum of dSk.  The three
         // components run in one runtime loop, so the particle loop holds one copy of the
         // unrolled (i, j, k) body, and pick their axes' weights by selects.  J agrees with
-        // the per-node evaluation to rounding (the tile sums in another order anyway).
+        // the per-node evaluation to rounding (the tile sums in another order anyway).  Used
+        // for the Esirkepov deposit of CIC and TSC, whose 2 x 3 x 3 weights fit the register
+        // budget beside the rest of the push.
         template<typename Acc>
         __device__ __forceinline__ static void runShort(
             Acc const& acc,
@@ -813,6 +815,67 @@ namespace picgb
             }
         }
 
+        // The short footprint with the weights evaluated per component and node, the
+        // arithmetic of cpt1D<C, false> (Esirkepov.hpp:200-241): fewer values live at once
+        // than in runShort, which keeps the register budget of the PQS and PCS kernels and of
+        // the EmZ variants (whose second virtual particle stays live across this deposit)
+        // without spills.  The three rotated components run in one runtime loop; the rotation
+        // maps rotated axes i, j, k to real axes C+1, C+2, C.
+        template<typename Acc>
+        __device__ __forceinline__ static void runShortPerNode(
+            Acc const& acc,
+            float const p0[3],
+            float const p1[3],
+            float const csd[3],
+            int tileTT)
+        {
+            auto sel = [](float const* p, int a) { return a == 0 ? p[0] : (a == 1 ? p[1] : p[2]); };
+#pragma unroll 1
+            for(int C = 0; C < 3; ++C)
+            {
+                int const ai = C == 2 ? 0 : C + 1;
+                int const aj = C == 0 ? 2 : C - 1;
+                float const q0[3] = {sel(p0, ai), sel(p0, aj), sel(p0, C)};
+                float const q1[3] = {sel(p1, ai), sel(p1, aj), sel(p1, C)};
+                if(q0[2] == q1[2])
+                    continue;
+                int const si = Acc::stride(ai), sj = Acc::stride(aj), sk = Acc::stride(C);
+                int const base = acc.base + C * tileTT;
+                float sj0[S + 1], sj1[S + 1], sk0[S + 1], sk1[S + 1];
+                SH::caArray(q0[1], false, sj0);
+                SH::caArray(q1[1], false, sj1);
+                SH::caArray(q0[2], false, sk0);
+                SH::caArray(q1[2], false, sk1);
+                float dsk[S];
+#pragma unroll
+                for(int k = 0; k < S; ++k)
+                    dsk[k] = fs(sk1[k], sk0[k]);
+                float const ncsd = -sel(csd, C);
+#pragma unroll
+                for(int i = begin; i < end; ++i)
+                {
+                    float const s0i = SH::ca(fs(float(i), q0[0]));
+                    float const dsi = fs(SH::ca(fs(float(i), q1[0])), s0i);
+#pragma unroll
+                    for(int j = begin; j < end; ++j)
+                    {
+                        float const s0j = sj0[j - begin];
+                        float const dsj = fs(sj1[j - begin], s0j);
+                        float const half = fm(0.5f, __fmaf_rn(dsi, s0j, fm(s0i, dsj)));
+                        float const tmp = fm(ncsd, __fmaf_rn(fm(1.0f / 3.0f, dsj), dsi, __fmaf_rn(s0i, s0j, half)));
+                        float run = 0.0f;
+                        int const row = base + i * si + j * sj;
+#pragma unroll
+                        for(int k = begin; k < end - 1; ++k)
+                        {
+                            run = __fmaf_rn(dsk[k - begin], tmp, run);
+                            acc.addAt(row + k * sk, run);
+                        }
+                    }
+                }
+            }
+        }
+
         // the three rotated calls; csd = charge * (1/(V*dt)) * cellEdgeLength (Esirkepov.hpp:188-190)
         template<bool kGeneral, typename Acc>
         __device__ __forceinline__ static void run(
@@ -832,7 +895,10 @@ namespace picgb
             if constexpr(!kGeneral)
             {
                 float const csd[3] = {fm(fm(qv, g.dx), u), fm(fm(qv, g.dy), u), fm(fm(qv, g.dz), u)};
-                runShort(acc, p0, p1, csd, Acc::kTT);
+                if constexpr(S <= 3)
+                    runShort(acc, p0, p1, csd, Acc::kTT);
+                else
+                    runShortPerNode(acc, p0, p1, csd, Acc::kTT);
                 return;
             }
 #endif
@@ -917,7 +983,7 @@ namespace picgb
             {
                 float const csd[3] = {fm(fdv(fm(g.dx, rho), g.dt), u), fm(fdv(fm(g.dy, rho), g.dt), u),
                                       fm(fdv(fm(g.dz, rho), g.dt), u)};
-                runShort(acc, p0, p1, csd, Acc::kTT);
+                runShortPerNode(acc, p0, p1, csd, Acc::kTT);
                 return;
             }
 #endif

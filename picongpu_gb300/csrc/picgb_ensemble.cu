@@ -43,6 +43,11 @@ struct picgb_ensemble
     uint64_t kernelsPerStep = 0;
     std::vector<uint64_t> signature; // state of the boxes the tables and the graph were built from
     uint64_t launches = 0;
+    uint32_t maxCap = 32; // largest slots per supercell of any box (shared memory of the reorder)
+    std::vector<int> pushed; // species pushed in the batched step
+    // interleaved order restored every sortInterval batched steps (0: never), as picgb_step does
+    uint32_t sortInterval = 20;
+    uint32_t stepsSinceSort = 0;
 };
 
 namespace
@@ -235,6 +240,7 @@ namespace
                     scId,
                     e->threads,
                     cfg.pusher,
+                    cfg.current,
                     e->dSpecies + k * nbox,
                     e->dItems,
                     e->nitems,
@@ -267,6 +273,28 @@ namespace
         CUDA_TRY(instErr);
         e->kernelsPerStep = kernels;
         e->signature = boxSignature(e);
+        e->maxCap = maxCap;
+        e->pushed = pushed;
+        return PICGB_OK;
+    }
+
+    // Every sortInterval batched steps: the interleaved order of every box's supercells.
+    int reorderBatched(picgb_ensemble* e)
+    {
+        if(!e->sortInterval || ++e->stepsSinceSort < e->sortInterval)
+            return PICGB_OK;
+        e->stepsSinceSort = 0;
+        int const* sc = e->boxes[0]->sc;
+        int const vol = sc[0] * sc[1] * sc[2];
+        if(reorderSmemBytes(vol, e->maxCap) > 200 * 1024)
+            return PICGB_OK;
+        size_t const nbox = e->boxes.size();
+        for(size_t k = 0; k < e->pushed.size(); ++k)
+            if(e->pushed[k])
+            {
+                CUDA_TRY(launchReorderBatch(e->dSpecies + k * nbox, e->dItems, e->nitems, vol, e->maxCap, e->stream));
+                ++e->launches;
+            }
         return PICGB_OK;
     }
 
@@ -407,10 +435,6 @@ extern "C"
     {
         if(int r = checkEns(e))
             return r;
-        if(cfg && cfg->current == PICGB_CURRENT_EMZ)
-            return fail(PICGB_ERR_UNSUPPORTED, "the batched push deposits with Esirkepov only; EmZ runs on the single-box path");
-        if(cfg && cfg->shape == PICGB_SHAPE_PCS)
-            return fail(PICGB_ERR_UNSUPPORTED, "the batched push has CIC, TSC and PQS kernels; PCS runs on the single-box path");
         for(auto* b : e->boxes)
             if(int r = picgb_add_species(b, cfg, index))
                 return r;
@@ -446,7 +470,21 @@ extern "C"
             e->launches += e->kernelsPerStep;
             if(int r = afterBatchedStep(e))
                 return r;
+            if(int r = reorderBatched(e))
+                return r;
         }
+        return PICGB_OK;
+    }
+
+    int picgb_ensemble_set_sort_interval(picgb_ensemble* e, uint32_t steps)
+    {
+        if(int r = checkEns(e))
+            return r;
+        e->sortInterval = steps;
+        e->stepsSinceSort = 0;
+        for(auto* b : e->boxes)
+            if(int r = picgb_set_sort_interval(b, steps))
+                return r;
         return PICGB_OK;
     }
 

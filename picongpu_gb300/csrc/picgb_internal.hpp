@@ -136,6 +136,10 @@ namespace picgb
         unsigned* status,
         cudaStream_t stream);
     cudaError_t launchCompact(SpeciesDev const& sp, int nsc, cudaStream_t stream);
+    // Interleaved cell order restored in every supercell (kReorder); vol = cells per supercell.
+    cudaError_t launchReorder(SpeciesDev const& sp, int nsc, int vol, cudaStream_t stream);
+    // Shared memory kReorder needs for slots of `cap` particles per supercell.
+    size_t reorderSmemBytes(int vol, uint32_t cap);
     cudaError_t launchMaxAbsBits(float const* w, uint64_t n, unsigned* bits, cudaStream_t stream);
     cudaError_t launchHistogram(
         int scId,

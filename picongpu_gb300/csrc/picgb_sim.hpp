@@ -152,6 +152,9 @@ struct picgb_sim
     std::vector<cudaEvent_t> eventPool;
     double profMs[PICGB_KERNEL_CLASSES] = {};
     uint64_t profN[PICGB_KERNEL_CLASSES] = {};
+    // interleaved order restored every sortInterval steps (0: never)
+    uint32_t sortInterval = 20;
+    uint32_t stepsSinceSort = 0;
 
     float coeffJ() const { return -(1.0f / cfg.eps0) * cfg.dt; } // FDTD.hpp:84
     float cellVolume() const

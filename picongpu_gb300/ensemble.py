@@ -102,6 +102,11 @@ class Ensemble:
     def run(self, n: int) -> None:
         L.call("picgb_ensemble_run", self.handle, n)
 
+    def set_sort_interval(self, steps: int) -> None:
+        """Restore the interleaved cell order every `steps` steps (0: never), in the batched step
+        and in every box's single-box step; see picgb_ensemble_set_sort_interval."""
+        L.call("picgb_ensemble_set_sort_interval", self.handle, int(steps))
+
     def run_sequential(self, n: int) -> None:
         L.call("picgb_ensemble_run_sequential", self.handle, n)
 

@@ -328,6 +328,11 @@ class Simulation:
     def synchronize(self) -> None:
         L.call("picgb_synchronize", self.handle)
 
+    def set_sort_interval(self, steps: int) -> None:
+        """Restore the interleaved cell order of every supercell every `steps` steps (0: never);
+        see picgb_set_sort_interval."""
+        L.call("picgb_set_sort_interval", self.handle, int(steps))
+
     def set_stream(self, stream_ptr: int | None) -> None:
         L.call("picgb_set_stream", self.handle, ctypes.c_void_p(stream_ptr) if stream_ptr else None)
 

@@ -33,9 +33,10 @@ def max_rel(a, b):
     return float(np.abs(a.astype(np.float64) - b).max()) / scale
 
 
-def species(shape="TSC", ids=True, capacity=0, pusher="Boris"):
-    return [pg.Species("e", -1.0, 1.0, pusher=pusher, shape=shape, with_ids=ids, capacity=capacity),
-            pg.Species("i", 1.0, 1836.0, pusher=pusher, shape=shape, with_ids=ids, capacity=capacity)]
+def species(shape="TSC", ids=True, capacity=0, pusher="Boris", current="Esirkepov"):
+    return [pg.Species("e", -1.0, 1.0, pusher=pusher, shape=shape, current=current, with_ids=ids, capacity=capacity),
+            pg.Species("i", 1.0, 1836.0, pusher=pusher, shape=shape, current=current, with_ids=ids,
+                       capacity=capacity)]
 
 
 def box_inputs(dims, seed):
@@ -53,9 +54,9 @@ def box_inputs(dims, seed):
     return out
 
 
-def make_ensemble(dims, inputs, shape="TSC", threads=256, fields=True, pusher="Boris"):
+def make_ensemble(dims, inputs, shape="TSC", threads=256, fields=True, pusher="Boris", current="Esirkepov"):
     ens = pg.Ensemble(dims, threads=threads)
-    for sp in species(shape, pusher=pusher):
+    for sp in species(shape, pusher=pusher, current=current):
         ens.add_species(sp)
     for b, (pe, pi, E, B) in enumerate(inputs):
         box = ens.box(b)
@@ -123,15 +124,24 @@ def test_autotune_times_every_candidate():
     assert rates[(sc, th)] == max(rates.values())
 
 
-def test_ensemble_refuses_what_the_batched_push_lacks():
-    """The batched push instantiates CIC, TSC and PQS with Esirkepov; PCS and EmZ species run on
-    the single-box path."""
-    ens = pg.Ensemble([(16, 16, 16)])
-    for sp in (pg.Species("e", -1.0, 1.0, shape="PCS"), pg.Species("e", -1.0, 1.0, current="EmZ")):
-        with pytest.raises(pg.PicError) as e:
-            ens.add_species(sp)
-        assert e.value.code == pg._lib.ERR_UNSUPPORTED
-    ens.close()
+@pytest.mark.parametrize("shape,pusher,current", [("PCS", "Boris", "Esirkepov"), ("TSC", "Boris", "EmZ"),
+                                                   ("PQS", "HigueraCary", "EmZ"), ("PCS", "Vay", "EmZ")])
+def test_batched_pcs_and_emz_match_single_box(shape, pusher, current):
+    """The PCS and EmZ variants of the batched push (the Thermal benchmark's policies) against the
+    single-box path: particles bit-exact, J, E, B within 1e-6."""
+    inputs = box_inputs(DIMS[:2], 29)
+    with make_ensemble(DIMS[:2], inputs, shape, 512, pusher=pusher, current=current) as a, \
+            make_ensemble(DIMS[:2], inputs, shape, pusher=pusher, current=current) as b:
+        a.run(1)
+        b.run_sequential(1)
+        for i in range(2):
+            ba, bb = a.box(i), b.box(i)
+            for name in ("e", "i"):
+                pa, pb = sorted_by_id(ba.get_particles(name)), sorted_by_id(bb.get_particles(name))
+                for k in ("pos", "mom", "sc", "lcell"):
+                    assert np.array_equal(pa[k], pb[k]), (shape, current, i, name, k)
+            for f in ("J", "E", "B"):
+                assert max_rel(ba.get_field(f), bb.get_field(f)) <= REL, (shape, current, i, f)
 
 
 @pytest.mark.parametrize("pusher", ["HigueraCary", "Vay"])
