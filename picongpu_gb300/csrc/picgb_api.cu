@@ -225,6 +225,9 @@ namespace picgb::host
     }
 
     // Contiguous device copy of particles in the host exchange format.
+    // Device arrays of n particles in the host exchange format, carved out of the simulation's
+    // staging buffer, which grows when needed and is kept for the next upload or download (a
+    // fresh cudaMalloc and cudaFree of several GB per call cost more than the copies).
     struct Staging
     {
         float* a[7] = {};
@@ -233,30 +236,61 @@ namespace picgb::host
         uint32_t* id = nullptr;
         uint64_t n = 0;
 
-        cudaError_t alloc(uint64_t count, bool ids)
+        cudaError_t alloc(picgb_sim* s, uint64_t count, bool ids)
         {
             n = count;
+            auto part = [&](size_t bytes) { return (bytes + 255) / 256 * 256; };
+            size_t const need = 7 * part(sizeof(float) * count) + part(sizeof(int32_t) * count)
+                + part(sizeof(uint16_t) * count) + (ids ? part(sizeof(uint32_t) * count) : 0);
+            if(need > s->ioBytes)
+            {
+                if(s->ioBuf)
+                {
+                    cudaError_t e = cudaStreamSynchronize(s->stream);
+                    if(e != cudaSuccess)
+                        return e;
+                    cudaFree(s->ioBuf);
+                }
+                s->ioBuf = nullptr;
+                s->ioBytes = 0;
+                cudaError_t e = cudaMalloc(&s->ioBuf, need);
+                if(e != cudaSuccess)
+                {
+                    s->ioBuf = nullptr;
+                    return e;
+                }
+                s->ioBytes = need;
+            }
+            char* b = static_cast<char*>(s->ioBuf);
             for(auto& p : a)
-                if(cudaError_t e = dalloc(p, count))
-                    return e;
-            if(cudaError_t e = dalloc(sc, count))
-                return e;
-            if(cudaError_t e = dalloc(lcell, count))
-                return e;
-            if(ids)
-                if(cudaError_t e = dalloc(id, count))
-                    return e;
+            {
+                p = reinterpret_cast<float*>(b);
+                b += part(sizeof(float) * count);
+            }
+            sc = reinterpret_cast<int32_t*>(b);
+            b += part(sizeof(int32_t) * count);
+            lcell = reinterpret_cast<uint16_t*>(b);
+            b += part(sizeof(uint16_t) * count);
+            id = ids ? reinterpret_cast<uint32_t*>(b) : nullptr;
             return cudaSuccess;
         }
-        ~Staging()
-        {
-            for(auto& p : a)
-                dfree(p);
-            dfree(sc);
-            dfree(lcell);
-            dfree(id);
-        }
     };
+
+    // Device address of host memory that kernels can write directly (page-locked memory
+    // registered with CUDA, e.g. from cudaHostAlloc), or nullptr (pageable memory).
+    template<typename T>
+    T* deviceView(T* host)
+    {
+        if(!host)
+            return nullptr;
+        cudaPointerAttributes at{};
+        if(cudaPointerGetAttributes(&at, host) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return at.type == cudaMemoryTypeHost ? static_cast<T*>(at.devicePointer) : nullptr;
+    }
 
     int readStatus(picgb_sim* s, unsigned* bits, bool reset)
     {
@@ -286,7 +320,7 @@ namespace picgb::host
             total += cnt[i];
         }
         Staging st;
-        CUDA_TRY(st.alloc(total + spill, sp.cfg.with_ids != 0));
+        CUDA_TRY(st.alloc(s, total + spill, sp.cfg.with_ids != 0));
         uint64_t* doff = nullptr;
         CUDA_TRY(dalloc(doff, size_t(s->nsc)));
         CUDA_TRY(cudaMemcpyAsync(doff, off.data(), sizeof(uint64_t) * s->nsc, cudaMemcpyHostToDevice, s->stream));
@@ -546,6 +580,8 @@ int picgb::host::destroySim(picgb_sim* s)
     dfree(s->pml.psiB);
     dfree(s->pmlTab);
     dfree(s->expDamp);
+    if(s->ioBuf)
+        cudaFree(s->ioBuf);
     if(s->hostStatus)
         cudaFreeHost(s->hostStatus);
     profFlush(s);
@@ -606,7 +642,7 @@ extern "C"
             return fail(PICGB_ERR_INVALID, "particle arrays must not be null");
         CUDA_TRY(cudaSetDevice(s->cfg.device));
         Staging st;
-        CUDA_TRY(st.alloc(n, sp.cfg.with_ids != 0 && h->id));
+        CUDA_TRY(st.alloc(s, n, sp.cfg.with_ids != 0 && h->id));
         float const* src[7] = {h->pos[0], h->pos[1], h->pos[2], h->mom[0], h->mom[1], h->mom[2], h->w};
         for(int k = 0; k < 7; ++k)
             CUDA_TRY(cudaMemcpyAsync(st.a[k], src[k], sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
@@ -767,20 +803,37 @@ extern "C"
         if(h->n < total)
             return fail(PICGB_ERR_INVALID, "host arrays hold %llu particles, %llu needed",
                         (unsigned long long) h->n, (unsigned long long) total);
-        Staging st;
-        CUDA_TRY(st.alloc(total, h->id != nullptr));
         uint64_t* doff = nullptr;
         CUDA_TRY(dalloc(doff, size_t(s->nsc)));
         CUDA_TRY(cudaMemcpyAsync(doff, off.data(), sizeof(uint64_t) * s->nsc, cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, st.a, st.sc, st.lcell, st.id, s->stream));
-        ++s->launches;
         float* dst[7] = {h->pos[0], h->pos[1], h->pos[2], h->mom[0], h->mom[1], h->mom[2], h->w};
+        // page-locked host arrays: the gather kernel writes them directly over the host link
+        float* direct[7];
+        bool zeroCopy = true;
         for(int k = 0; k < 7; ++k)
-            CUDA_TRY(cudaMemcpyAsync(dst[k], st.a[k], sizeof(float) * total, cudaMemcpyDeviceToHost, s->stream));
-        CUDA_TRY(cudaMemcpyAsync(h->sc, st.sc, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, s->stream));
-        CUDA_TRY(cudaMemcpyAsync(h->lcell, st.lcell, sizeof(uint16_t) * total, cudaMemcpyDeviceToHost, s->stream));
-        if(h->id)
-            CUDA_TRY(cudaMemcpyAsync(h->id, st.id, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost, s->stream));
+            zeroCopy = zeroCopy && (direct[k] = deviceView(dst[k])) != nullptr;
+        int32_t* dsc = deviceView(h->sc);
+        uint16_t* dlc = deviceView(h->lcell);
+        uint32_t* did = deviceView(h->id);
+        zeroCopy = zeroCopy && dsc && dlc && (!h->id || did);
+        if(zeroCopy)
+        {
+            CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, direct, dsc, dlc, did, s->stream));
+            ++s->launches;
+        }
+        else
+        {
+            Staging st;
+            CUDA_TRY(st.alloc(s, total, h->id != nullptr));
+            CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, st.a, st.sc, st.lcell, st.id, s->stream));
+            ++s->launches;
+            for(int k = 0; k < 7; ++k)
+                CUDA_TRY(cudaMemcpyAsync(dst[k], st.a[k], sizeof(float) * total, cudaMemcpyDeviceToHost, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(h->sc, st.sc, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(h->lcell, st.lcell, sizeof(uint16_t) * total, cudaMemcpyDeviceToHost, s->stream));
+            if(h->id)
+                CUDA_TRY(cudaMemcpyAsync(h->id, st.id, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost, s->stream));
+        }
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         dfree(doff);
         h->n = total;

@@ -128,6 +128,8 @@ struct picgb_sim
     float* rho = nullptr;
     unsigned* status = nullptr; // device status word
     unsigned* hostStatus = nullptr; // pinned
+    void* ioBuf = nullptr; // staging of species uploads and downloads, kept between calls
+    size_t ioBytes = 0;
     double* energy = nullptr; // device accumulators
     unsigned* maxBits = nullptr; // device: residual max, rho max
     unsigned long long* kindCount = nullptr; // device: deposits by footprint (profiling)
