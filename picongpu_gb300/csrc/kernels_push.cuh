@@ -39,6 +39,9 @@ namespace picgb
     // (TileGeom); 0 keeps the unpadded widths
 #    define PICGB_TILE_PITCH_MIN 12
 #endif
+#ifndef PICGB_J_PLANE_PAD
+#    define PICGB_J_PLANE_PAD 1
+#endif
     static_assert(kQueueCap >= 32, "a warp drains 32 jobs at a time");
     constexpr int kJobWords = 9;
 
@@ -60,7 +63,22 @@ namespace picgb
         static constexpr int JX = SC::SX + SH::jLo + SH::jHi;
         static constexpr int JY = SC::SY + SH::jLo + SH::jHi;
         static constexpr int JZ = SC::SZ + SH::jLo + SH::jHi;
-        static constexpr int JT = JX * JY * JZ;
+        // Plane pitch of the J tile.  A deposit instruction of a warp adds at one node
+        // offset for 32 particles, whose origins differ by their cells (an 8 x 4 patch in
+        // the interleaved order, random after a drift) and, for the odd shapes, by a
+        // random shift of 0 or 1 per axis.  With the unpadded planes (225 words for TSC,
+        // 1 mod 32) a shift along z lands in the bank of a shift along x.  A bank model
+        // of these accesses gives the fewest wavefronts per atomic for plane pitches of
+        // 8 mod 16 words: TSC 3.3 (patch) and 3.5 (random cells) against 4.2 and 4.0
+        // unpadded, PCS alike, CIC and PQS (no random shift) 3.5 against 3.6 and 4.1 for
+        // random cells.  The pitch is the smallest such one above the plane; 4 x 4 x 4
+        // supercells keep theirs.
+        static constexpr int JP = (SC::SX == 8 && SC::SY == 8 && PICGB_J_PLANE_PAD)
+            ? JX * JY + ((8 - JX * JY % 16) + 16) % 16
+            : JX * JY;
+        static constexpr int JT = JP * JZ;
+        // tile word of node (x, y, z), counted from the tile's corner
+        __device__ __forceinline__ static int jIndex(int x, int y, int z) { return x + JX * y + JP * z; }
         // E and B tiles, the J tile, the per-warp queues of deposit jobs
         static constexpr int JWords = (PICGB_J_FIXED ? 6 : 3) * JT; // words of the J tile
         static constexpr int QueueWords = (THREADS / 32) * kQueueCap * kJobWords;
@@ -122,7 +140,7 @@ namespace picgb
     // reference's guard add of FieldJ, FieldJ.x.cpp:156-169, folded in).  Beyond an
     // open face the current is dropped, as the reference's guard current at a
     // non-periodic boundary is.
-    template<int TX, int TY, int TT>
+    template<int TX, int TY, int TP, int TT>
     __device__ __forceinline__ void flushTile(
         float const* __restrict__ Js,
         float* __restrict__ J,
@@ -140,7 +158,9 @@ namespace picgb
                         vz = tileValue<TT>(Js, 2 * TT + t, f);
             if(vx == 0.0f && vy == 0.0f && vz == 0.0f)
                 continue;
-            int const tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
+            int const tz = t / TP, ty = (t - tz * TP) / TX, tx = t - tz * TP - ty * TX;
+            if(ty >= TY)
+                continue; // plane padding (never written)
             int gx, gy, gz;
             if(!anyOpen)
             {
@@ -227,7 +247,7 @@ namespace picgb
     // atomics and loads.  Out of line when PICGB_DRAIN_OUT_OF_LINE: the path runs once per
     // 32 queued jobs, and keeping its code out of the particle loop keeps the loop small
     // for the instruction cache.
-    template<typename SH, int TX, int TY, int TT, bool EMZ>
+    template<typename SH, int TX, int TP, int TT, bool EMZ>
 #if PICGB_DRAIN_OUT_OF_LINE
     __device__ __noinline__
 #else
@@ -248,7 +268,7 @@ namespace picgb
         g.dy = dy;
         g.dz = dz;
         g.dt = dt;
-        using Tile = TileJ<TX, TY, TT>;
+        using Tile = TileJ<TX, TP, TT>;
         if constexpr(EMZ)
             Esirkepov<SH>::runEmZ(Tile{smem + jOff, qo, jf}, q0, q1, qc, g);
         else
@@ -284,7 +304,7 @@ namespace picgb
         using SC = SuperCell<SX, SY, SZ>;
         using TG = TileGeom<SH, SC, THREADS>;
         using ES = Esirkepov<SH>;
-        using Tile = TileJ<TG::JX, TG::JY, TG::JT>;
+        using Tile = TileJ<TG::JX, TG::JP, TG::JT>;
         float* const Es = smem;
         float* const Bs = smem + 3 * TG::GT;
         float* const Js = smem + 6 * TG::GT;
@@ -391,10 +411,8 @@ namespace picgb
                     else if(pp.deposit)
                     {
                         // tile indices of the two virtual particles' cells
-                        org = (lx + mv[0] + sS[0] + SH::jLo)
-                            + TG::JX * ((ly + mv[1] + sS[1] + SH::jLo) + TG::JY * (lz + mv[2] + sS[2] + SH::jLo));
-                        orgB = (lx + mv[0] + sE[0] + SH::jLo)
-                            + TG::JX * ((ly + mv[1] + sE[1] + SH::jLo) + TG::JY * (lz + mv[2] + sE[2] + SH::jLo));
+                        org = TG::jIndex(lx + mv[0] + sS[0] + SH::jLo, ly + mv[1] + sS[1] + SH::jLo, lz + mv[2] + sS[2] + SH::jLo);
+                        orgB = TG::jIndex(lx + mv[0] + sE[0] + SH::jLo, ly + mv[1] + sE[1] + SH::jLo, lz + mv[2] + sE[2] + SH::jLo);
                         kind = two ? 1 : 0;
                     }
                 }
@@ -406,8 +424,7 @@ namespace picgb
                     else
                     {
                         // tile index of the Esirkepov origin; the new cell lies in [-1, S]
-                        org = (lx + mv[0] + gs[0] + SH::jLo)
-                            + TG::JX * ((ly + mv[1] + gs[1] + SH::jLo) + TG::JY * (lz + mv[2] + gs[2] + SH::jLo));
+                        org = TG::jIndex(lx + mv[0] + gs[0] + SH::jLo, ly + mv[1] + gs[1] + SH::jLo, lz + mv[2] + gs[2] + SH::jLo);
                         kind = (stat[0] == ES::kInCell && stat[1] == ES::kInCell && stat[2] == ES::kInCell) ? 0 : 1;
                     }
                 }
@@ -515,7 +532,7 @@ namespace picgb
             __syncwarp();
             if(queued >= 32)
             {
-                drainQueue<SH, TG::JX, TG::JY, TG::JT, EMZ>(
+                drainQueue<SH, TG::JX, TG::JP, TG::JT, EMZ>(
                     int(Js - smem), qOff, 32, pp.jf, g.dx, g.dy, g.dz, g.dt, pp.invVdt);
                 __syncwarp();
                 if(lane < queued - 32)
@@ -533,13 +550,13 @@ namespace picgb
         }
         // the jobs still queued
         if(pp.deposit && queued > 0)
-            drainQueue<SH, TG::JX, TG::JY, TG::JT, EMZ>(
+            drainQueue<SH, TG::JX, TG::JP, TG::JT, EMZ>(
                 int(Js - smem), qOff, queued, pp.jf, g.dx, g.dy, g.dz, g.dt, pp.invVdt);
         __syncthreads(); // every hole is recorded and every deposit done
         if(threadIdx.x == 0)
             sp.nhole[sc] = s_nhole;
         if(pp.deposit)
-            flushTile<TG::JX, TG::JY, TG::JT>(Js, J, ox - SH::jLo, oy - SH::jLo, oz - SH::jLo, g, ncell, pp.jf);
+            flushTile<TG::JX, TG::JY, TG::JP, TG::JT>(Js, J, ox - SH::jLo, oy - SH::jLo, oz - SH::jLo, g, ncell, pp.jf);
     }
 
     // Fused push kernel of one box: one block per supercell.
@@ -604,10 +621,9 @@ namespace picgb
                 }
                 float const q = fm(pp.charge, w);
                 Esirkepov<SH>::runEmZ(
-                    TileJ<TG::JX, TG::JY, TG::JT>{
+                    TileJ<TG::JX, TG::JP, TG::JT>{
                         Js,
-                        (cellRel[0] + gs[0] + SH::jLo)
-                            + TG::JX * ((cellRel[1] + gs[1] + SH::jLo) + TG::JY * (cellRel[2] + gs[2] + SH::jLo)),
+                        TG::jIndex(cellRel[0] + gs[0] + SH::jLo, cellRel[1] + gs[1] + SH::jLo, cellRel[2] + gs[2] + SH::jLo),
                         pp.jf},
                     p0,
                     p1,
@@ -615,10 +631,9 @@ namespace picgb
                     g);
                 if(two)
                     Esirkepov<SH>::runEmZ(
-                        TileJ<TG::JX, TG::JY, TG::JT>{
+                        TileJ<TG::JX, TG::JP, TG::JT>{
                             Js,
-                            (cellRel[0] + sE[0] + SH::jLo)
-                                + TG::JX * ((cellRel[1] + sE[1] + SH::jLo) + TG::JY * (cellRel[2] + sE[2] + SH::jLo)),
+                            TG::jIndex(cellRel[0] + sE[0] + SH::jLo, cellRel[1] + sE[1] + SH::jLo, cellRel[2] + sE[2] + SH::jLo),
                             pp.jf},
                         b0,
                         b1,
@@ -631,15 +646,14 @@ namespace picgb
                 atomicOr(status, ST_BAD_CELL);
                 continue;
             }
-            TileJ<TG::JX, TG::JY, TG::JT> const acc{
+            TileJ<TG::JX, TG::JP, TG::JT> const acc{
                 Js,
-                (cellRel[0] + gs[0] + SH::jLo)
-                    + TG::JX * ((cellRel[1] + gs[1] + SH::jLo) + TG::JY * (cellRel[2] + gs[2] + SH::jLo)),
+                TG::jIndex(cellRel[0] + gs[0] + SH::jLo, cellRel[1] + gs[1] + SH::jLo, cellRel[2] + gs[2] + SH::jLo),
                 pp.jf};
             Esirkepov<SH>::template run<true>(acc, p0, p1, stat, fm(pp.charge, w), g, pp.invVdt);
         }
         __syncthreads();
-        flushTile<TG::JX, TG::JY, TG::JT>(
+        flushTile<TG::JX, TG::JY, TG::JP, TG::JT>(
             Js,
             J,
             scx * SX - SH::jLo,

@@ -509,7 +509,8 @@ namespace picgb
 #    define PICGB_SHORT_LOOP 1
 #endif
 
-    template<int TX, int TY, int TT>
+    // TX: row pitch, TP: plane pitch, TT: words of one component's tile
+    template<int TX, int TP, int TT>
     struct TileJ
     {
         static constexpr int kTT = TT;
@@ -536,11 +537,11 @@ namespace picgb
         {
             int x, y, z;
             rotToReal<C>(ri, rj, rk, x, y, z);
-            addAt(C * TT + base + x + TX * (y + TY * z), v);
+            addAt(C * TT + base + x + TX * y + TP * z, v);
         }
 
         // word stride of real axis a (0 x, 1 y, 2 z)
-        __device__ __forceinline__ static int stride(int a) { return a == 0 ? 1 : (a == 1 ? TX : TX * TY); }
+        __device__ __forceinline__ static int stride(int a) { return a == 0 ? 1 : (a == 1 ? TX : TP); }
 
         // T * cum at tile word idx (component offset included by the caller); cumHi =
         // cum * 2^-k (exact).  In fixed point the high part a = rint(T cum 2^-k) comes from
