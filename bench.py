@@ -259,13 +259,13 @@ def run_gpu(args, wl, rank, world, local_rank):
     push_bytes = args.steps * (B_PARTICLE * npart + 2 * B_PUSH_CELL * ncell)
     peak, peak_kind = peaks()
     achieved = push_bytes / (push_ms / 1e3) / 1e9 if push_ms > 0 else None
-    traffic = push_traffic(npart / 2, ncell)
+    traffic, traffic_pp = push_traffic(npart / 2, ncell)
     roof = {"kernel": "kPush (gather+Boris+move+Esirkepov+migration, per species)", "bound": "hbm",
             "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
             "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one kPush launch on the 128^3 "
-                              "two-stream case (33.5e6 particles, 57.76 B each), scaled by the particle count "
+                              f"two-stream case (33.5e6 particles, {traffic_pp} B each), scaled by the particle count "
                               "(profiles/push_tsc_two_stream_128_dram.md)",
             "algorithmic_bytes_per_launch": (B_PARTICLE * npart + 2 * B_PUSH_CELL * ncell) / 2,
             "mean_launch_ms": push_ms / max(push_n, 1),
@@ -282,14 +282,15 @@ def run_gpu(args, wl, rank, world, local_rank):
 
 def push_traffic(n_per_launch, ncell):
     """DRAM bytes per push launch from the committed ncu summary of one 128^3 launch (bytes per
-    particle), scaled to the launch's particle count; else None."""
+    particle), scaled to the launch's particle count, and the bytes per particle; else (None, None)."""
     p = os.path.join(ROOT, "profiles", "push_tsc_two_stream_128_dram.md")
     if not os.path.exists(p):
-        return None
+        return None, None
     for line in open(p):
         if line.startswith("dram_bytes_per_particle:"):
-            return float(line.split(":")[1]) * n_per_launch
-    return None
+            pp = float(line.split(":")[1])
+            return pp * n_per_launch, pp
+    return None, None
 
 
 def run_e2e(args, wl, sim, pg, torch, local_rank, world):
