@@ -402,24 +402,39 @@ namespace picgb
         __host__ __device__ static size_t bytes(int vol, uint32_t cap) { return sizeof(uint32_t) * (size_t(buf(vol, cap)) + cap); }
     };
 
+    // Loads per thread issued before the first shared-memory store of a staging pass, so
+    // that a pass costs one memory latency instead of one per loop iteration.
+    constexpr int kReorderLoads = 8;
+
+    // a[j] = a_old[inv[j]] for j < n, staged through buf.  The bits of a 32-bit or 16-bit
+    // attribute pass through buf unchanged.
     template<typename T>
     __device__ __forceinline__ void permuteInPlace(T* __restrict__ a, uint32_t n, uint32_t* buf, uint16_t const* inv)
     {
-        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
-            buf[k] = uint32_t(a[k]);
+        static_assert(sizeof(T) == 4 || sizeof(T) == 2, "32-bit or 16-bit attributes");
+        using Bits = typename std::conditional<sizeof(T) == 4, uint32_t, uint16_t>::type;
+        Bits* const ab = reinterpret_cast<Bits*>(a);
+        uint32_t const step = blockDim.x * kReorderLoads;
+        for(uint32_t k0 = threadIdx.x; k0 < n; k0 += step)
+        {
+            Bits v[kReorderLoads];
+#pragma unroll
+            for(int u = 0; u < kReorderLoads; ++u)
+            {
+                uint32_t const k = k0 + u * blockDim.x;
+                v[u] = k < n ? ab[k] : Bits(0);
+            }
+#pragma unroll
+            for(int u = 0; u < kReorderLoads; ++u)
+            {
+                uint32_t const k = k0 + u * blockDim.x;
+                if(k < n)
+                    buf[k] = uint32_t(v[u]);
+            }
+        }
         __syncthreads();
         for(uint32_t j = threadIdx.x; j < n; j += blockDim.x)
-            a[j] = T(buf[inv[j]]);
-        __syncthreads();
-    }
-
-    __device__ __forceinline__ void permuteInPlaceF(float* __restrict__ a, uint32_t n, uint32_t* buf, uint16_t const* inv)
-    {
-        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
-            buf[k] = __float_as_uint(a[k]);
-        __syncthreads();
-        for(uint32_t j = threadIdx.x; j < n; j += blockDim.x)
-            a[j] = __uint_as_float(buf[inv[j]]);
+            ab[j] = Bits(buf[inv[j]]);
         __syncthreads();
     }
 
@@ -442,21 +457,35 @@ namespace picgb
         if(threadIdx.x == 0)
             s_tooFull = 0;
         __syncthreads();
-        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        for(uint32_t k0 = threadIdx.x; k0 < n; k0 += blockDim.x * kReorderLoads)
         {
-            uint32_t const lc = sp.lcell[base + k];
-            buf[k] = lc;
-            if(lc >= uint32_t(vol)) // not a cell of this supercell: leave the order alone
+            uint16_t lcs[kReorderLoads];
+#pragma unroll
+            for(int u = 0; u < kReorderLoads; ++u)
             {
-                s_tooFull = 1;
-                continue;
+                uint32_t const k = k0 + u * blockDim.x;
+                lcs[u] = k < n ? sp.lcell[base + k] : uint16_t(0);
             }
-            uint32_t const r = atomicAdd(cnt + lc, 1u);
-            rank[k] = uint16_t(r < 65535u ? r : 65535u);
-            if(r < uint32_t(kReorderRounds))
-                atomicOr(bm + r * words + lc / 32, 1u << (lc % 32));
-            else
-                s_tooFull = 1;
+#pragma unroll
+            for(int u = 0; u < kReorderLoads; ++u)
+            {
+                uint32_t const k = k0 + u * blockDim.x;
+                if(k >= n)
+                    break;
+                uint32_t const lc = lcs[u];
+                buf[k] = lc;
+                if(lc >= uint32_t(vol)) // not a cell of this supercell: leave the order alone
+                {
+                    s_tooFull = 1;
+                    continue;
+                }
+                uint32_t const r = atomicAdd(cnt + lc, 1u);
+                rank[k] = uint16_t(r < 65535u ? r : 65535u);
+                if(r < uint32_t(kReorderRounds))
+                    atomicOr(bm + r * words + lc / 32, 1u << (lc % 32));
+                else
+                    s_tooFull = 1;
+            }
         }
         __syncthreads();
         if(s_tooFull)
@@ -497,13 +526,13 @@ namespace picgb
             inv[starts[r] + before] = uint16_t(k);
         }
         __syncthreads();
-        permuteInPlaceF(sp.px + base, n, buf, inv);
-        permuteInPlaceF(sp.py + base, n, buf, inv);
-        permuteInPlaceF(sp.pz + base, n, buf, inv);
-        permuteInPlaceF(sp.ux + base, n, buf, inv);
-        permuteInPlaceF(sp.uy + base, n, buf, inv);
-        permuteInPlaceF(sp.uz + base, n, buf, inv);
-        permuteInPlaceF(sp.w + base, n, buf, inv);
+        permuteInPlace(sp.px + base, n, buf, inv);
+        permuteInPlace(sp.py + base, n, buf, inv);
+        permuteInPlace(sp.pz + base, n, buf, inv);
+        permuteInPlace(sp.ux + base, n, buf, inv);
+        permuteInPlace(sp.uy + base, n, buf, inv);
+        permuteInPlace(sp.uz + base, n, buf, inv);
+        permuteInPlace(sp.w + base, n, buf, inv);
         permuteInPlace(sp.lcell + base, n, buf, inv);
         if(sp.id)
             permuteInPlace(sp.id + base, n, buf, inv);
