@@ -239,22 +239,35 @@ extern "C"
     int picgb_stage_field_after(picgb_sim* sim, uint32_t step);
 
     /* Incident field (fields/incidentField/Solver.hpp:500-533 with profiles/GaussianPulse.hpp):
-     * a Gaussian pulse enters through the total-field/scattered-field surface between the E
-     * plane y = surface (total side) and the B plane below it; the field solver stages add the
-     * incident E (B half steps, at times step*dt and (step+1)*dt) and the incident B (E step,
-     * at (step+1/2)*dt) on that surface.  The pulse travels along +y (axis 1, the only axis
-     * supported), polarised along x (0) or z (1), as the focused Gaussian beam of
+     * a Gaussian pulse enters through one face of the total-field/scattered-field box and travels
+     * along the face's normal: axis 0, 1 or 2; direction +1 enters through the low face and
+     * travels +axis (the reference's XMin/YMin/ZMin profiles), -1 through the high face,
+     * travelling -axis (XMax/YMax/ZMax).  `surface` is the first (direction +1) or last
+     * (direction -1) E plane of the total-field region along the axis; the B plane just beyond it
+     * is on the scattered side (the reference's Huygens surface 0.75 cells inside its POSITION:
+     * surface = POSITION + 1 on a low face, POSITION - 1 on a high face).  The field solver stages
+     * add the incident E (B half steps, at times step*dt and (step+1)*dt) and the incident B (E
+     * step, at (step+1/2)*dt) on that surface.  The transverse axes are the two other axes in
+     * increasing order (for axis 1: x, then z); polarisation 0 or 1 puts E along the first or the
+     * second, and center_x, center_z are the beam centre on the first and the second.  The face
+     * spans a periodic transverse axis in full and an open one between its absorbers; on an open
+     * axis the surface must keep out of the absorber (Solver.hpp:113-168), which every field stage
+     * checks (PICGB_ERR_INVALID).  The pulse is the focused Gaussian beam of
      * profiles/GaussianPulse.hpp:223-290 (fundamental mode, B from E by the slowly varying
      * envelope approximation, incidentField::detail::ApproximateIncidentB):
      *   E = E0 (w0/w) exp(-r^2/w^2) exp(-(tau - t_center - r_c/c)^2 / (2 sigma^2))
      *       sin(omega (tau - t_center) - k r_c + xi + phase),
-     *   tau = t - (y - surface*dy)/c, r the distance from (center_x, center_z),
-     *   z_f = (surface + focus) dy - y the distance to the focus, z_R = pi w0^2 / wavelength,
+     *   zeta = direction (u - surface) the distance travelled beyond the surface (u the
+     *   coordinate along the axis, in cells), tau = t - zeta d/c, r the transverse distance from
+     *   the centre, z_f = (focus - zeta) d the distance to the focus, z_R = pi w0^2 / wavelength,
      *   w = w0 sqrt(1 + (z_f/z_R)^2), r_c = r^2/2 * (-z_f / (z_R^2 + z_f^2)) (wavefront curvature),
      *   xi = atan(-z_f / z_R) (Gouy phase), w0 = waist,
      *   omega = 2 pi c / wavelength, k = omega / c, E0 = a0 omega c / e_over_m,
      *   sigma = duration_fwhm / (2 sqrt(ln 2)) (duration_fwhm of the intensity).
-     * focus = 0 puts the focus on the surface.  enabled = 0 switches it off. */
+     * focus = 0 puts the focus on the surface.  Each of the six faces holds its own pulse:
+     * setting a face replaces that face's pulse, enabled = 0 switches the face (axis, direction)
+     * off, and a NULL field switches every face off.  Propagation oblique to the face (the
+     * reference's DIRECTION_{X,Y,Z} off the axis) is not supported. */
     typedef struct picgb_incident_field
     {
         int32_t enabled;
@@ -262,7 +275,8 @@ extern "C"
         int32_t surface;
         int32_t polarisation;
         float a0, e_over_m, wavelength, waist, duration_fwhm, t_center, center_x, center_z, phase;
-        float focus; /* distance of the focus beyond the surface along +y, in cells */
+        float focus; /* distance of the focus beyond the surface along the propagation, in cells */
+        int32_t direction; /* +1 (or 0): travels +axis from the low face; -1: travels -axis from the high face */
     } picgb_incident_field;
     int picgb_set_incident_field(picgb_sim* sim, const picgb_incident_field* field);
 

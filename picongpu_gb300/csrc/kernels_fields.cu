@@ -101,15 +101,22 @@ namespace picgb
     }
 
     // ------------------------------------------------------------ incident field (TF/SF)
+    __device__ __forceinline__ float pick3(float v0, float v1, float v2, int i) { return i == 0 ? v0 : (i == 1 ? v1 : v2); }
+
     // Incident pulse value at (x, y, z) in cell units and time t: the focused Gaussian beam of
     // profiles/GaussianPulse.hpp:223-290 in its fundamental mode (waist w(z_f), wavefront
-    // curvature, Gouy phase, amplitude w0/w, the envelope shifted by the curvature's delay).
+    // curvature, Gouy phase, amplitude w0/w, the envelope shifted by the curvature's delay),
+    // propagating along the face's axis in the face's direction.
     __device__ __forceinline__ float incidentValue(IncidentParams const& p, GridParams const& g, float x, float y, float z, float t)
     {
-        float const rx = (x - p.cx) * g.dx, rz = (z - p.cz) * g.dz;
-        float const r2 = rx * rx + rz * rz;
-        float const tau = t - (y - float(p.j0)) * g.dy / g.c - p.tc;
-        float const zf = (p.yf - y) * g.dy; // distance to the focus along the propagation
+        int const a = p.axis, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        float const da = pick3(g.dx, g.dy, g.dz, a);
+        float const r1 = (pick3(x, y, z, t1) - p.c1) * pick3(g.dx, g.dy, g.dz, t1);
+        float const r2_ = (pick3(x, y, z, t2) - p.c2) * pick3(g.dx, g.dy, g.dz, t2);
+        float const r2 = r1 * r1 + r2_ * r2_;
+        float const zeta = float(p.dir) * (pick3(x, y, z, a) - float(p.plane)); // cells beyond the surface
+        float const tau = t - zeta * da / g.c - p.tc;
+        float const zf = (p.focus - zeta) * da; // distance to the focus along the propagation
         float const q = zf / p.zR;
         float const w2 = p.w0 * p.w0 * (1.0f + q * q);
         float const rc = 0.5f * r2 * (-zf / (p.zR * p.zR + zf * zf)); // r^2/2 times the inverse curvature radius
@@ -119,53 +126,78 @@ namespace picgb
         return p.E0 * env * sinf(p.omega * tau - p.k * rc + xi + p.phase);
     }
 
-    // After B -= dt/2 curl E: the B plane j0 - 1 (scattered side) used the total E of plane j0;
-    // removing the incident part gives B_x += dt/2 E_z,inc / dy and B_z -= dt/2 E_x,inc / dy.
-    __global__ void kIncidentB(float* __restrict__ B, GridParams g, IncidentParams p, float t)
+    // Cell (i, j, k) of a face node: `planeIdx` along the axis, (u1, u2) on the transverse axes.
+    __device__ __forceinline__ void faceCell(int a, int planeIdx, int u1, int u2, int& i, int& j, int& k)
     {
-        int const i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
-        if(i >= g.nx)
-            return;
-        size_t const nc = size_t(g.nx) * g.ny * g.nz;
-        size_t const idx = size_t(i) + size_t(g.nx) * (size_t(p.j0 - 1) + size_t(g.ny) * k);
-        float const h = 0.5f * g.dt / g.dy;
-        if(p.pol == 0) // E_x at (i + 1/2, j0, k)
-            B[2 * nc + idx] -= h * incidentValue(p, g, i + 0.5f, float(p.j0), float(k), t);
-        else // E_z at (i, j0, k + 1/2)
-            B[idx] += h * incidentValue(p, g, float(i), float(p.j0), k + 0.5f, t);
+        i = a == 0 ? planeIdx : u1;
+        j = a == 1 ? planeIdx : (a == 0 ? u1 : u2);
+        k = a == 2 ? planeIdx : u2;
     }
 
-    // After E += c^2 dt curl B: the E plane j0 (total side) used the scattered B of plane j0 - 1;
-    // adding the incident part gives E_x -= c^2 dt B_z,inc / dy and E_z += c^2 dt B_x,inc / dy,
-    // with B_z,inc = -E_x,inc / c (pol 0) and B_x,inc = E_z,inc / c (pol 1) for a wave along +y.
+    // The incident E is polarised along axis p (first or second transverse axis); o is the other
+    // transverse axis; with (a, b, c) cyclic, dB_o/dt contains +dE_p/da when p = c and -dE_p/da
+    // when p = b.  After B -= dt/2 curl E the B plane on the scattered side of the surface
+    // (a-index plane - 1 for dir +1, plane for dir -1) used the total E_p of the E plane `plane`;
+    // removing its incident part adds sigma dt/2 E_p,inc / da to B_o, sigma = -dir (p = c) or
+    // +dir (p = b).  For a wave along +y: B_z -= dt/2 E_x,inc / dy, B_x += dt/2 E_z,inc / dy.
+    __global__ void kIncidentB(float* __restrict__ B, GridParams g, IncidentParams p, float t)
+    {
+        int const u1 = p.lo[0] + int(blockIdx.x * blockDim.x + threadIdx.x), u2 = p.lo[1] + int(blockIdx.y);
+        if(u1 >= p.hi[0])
+            return;
+        int const a = p.axis, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        int const pa = p.pol == 0 ? t1 : t2, oa = p.pol == 0 ? t2 : t1;
+        float const sigma = (pa == (a + 2) % 3) ? -float(p.dir) : float(p.dir);
+        int i, j, k;
+        faceCell(a, p.dir > 0 ? p.plane - 1 : p.plane, u1, u2, i, j, k);
+        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+        size_t const idx = size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * size_t(k));
+        float const h = 0.5f * g.dt / pick3(g.dx, g.dy, g.dz, a);
+        // E_p at the E plane, staggered by 1/2 along p
+        float const x = a == 0 ? float(p.plane) : float(i) + (pa == 0 ? 0.5f : 0.0f);
+        float const y = a == 1 ? float(p.plane) : float(j) + (pa == 1 ? 0.5f : 0.0f);
+        float const z = a == 2 ? float(p.plane) : float(k) + (pa == 2 ? 0.5f : 0.0f);
+        B[size_t(oa) * nc + idx] += sigma * h * incidentValue(p, g, x, y, z, t);
+    }
+
+    // After E += c^2 dt curl B: the E plane `plane` (total side) used the scattered B_o of the
+    // plane beyond it; adding the incident B_o = (dir e_a x E_inc)_o / c gives, for either
+    // direction and polarisation, E_p += c^2 dt / da * E_inc(at B_o) / c.  For a wave along +y:
+    // E_x -= c^2 dt B_z,inc / dy with B_z,inc = -E_x,inc / c, E_z += c^2 dt B_x,inc / dy with
+    // B_x,inc = E_z,inc / c.
     __global__ void kIncidentE(float* __restrict__ E, GridParams g, IncidentParams p, float t)
     {
-        int const i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
-        if(i >= g.nx)
+        int const u1 = p.lo[0] + int(blockIdx.x * blockDim.x + threadIdx.x), u2 = p.lo[1] + int(blockIdx.y);
+        if(u1 >= p.hi[0])
             return;
+        int const a = p.axis, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        int const pa = p.pol == 0 ? t1 : t2;
+        int i, j, k;
+        faceCell(a, p.plane, u1, u2, i, j, k);
         size_t const nc = size_t(g.nx) * g.ny * g.nz;
-        size_t const idx = size_t(i) + size_t(g.nx) * (size_t(p.j0) + size_t(g.ny) * k);
-        float const h = g.c * g.c * g.dt / g.dy;
-        float const yb = float(p.j0) - 0.5f;
-        if(p.pol == 0) // B_z at (i + 1/2, j0 - 1/2, k)
-            E[idx] -= h * (-incidentValue(p, g, i + 0.5f, yb, float(k), t) / g.c);
-        else // B_x at (i, j0 - 1/2, k + 1/2)
-            E[2 * nc + idx] += h * (incidentValue(p, g, float(i), yb, k + 0.5f, t) / g.c);
+        size_t const idx = size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * size_t(k));
+        float const h = g.c * g.c * g.dt / pick3(g.dx, g.dy, g.dz, a);
+        // B_o half a cell beyond the surface, staggered by 1/2 along a and along p
+        float const ab = float(p.plane) - 0.5f * float(p.dir);
+        float const x = a == 0 ? ab : float(i) + (pa == 0 ? 0.5f : 0.0f);
+        float const y = a == 1 ? ab : float(j) + (pa == 1 ? 0.5f : 0.0f);
+        float const z = a == 2 ? ab : float(k) + (pa == 2 ? 0.5f : 0.0f);
+        E[size_t(pa) * nc + idx] += h * (incidentValue(p, g, x, y, z, t) / g.c);
     }
 
     cudaError_t launchIncidentB(float* B, GridParams const& g, IncidentParams const& inc, float t, cudaStream_t stream)
     {
-        if(!inc.enabled)
+        if(!inc.enabled || inc.hi[0] <= inc.lo[0] || inc.hi[1] <= inc.lo[1])
             return cudaSuccess;
-        kIncidentB<<<dim3((g.nx + 127) / 128, g.nz), 128, 0, stream>>>(B, g, inc, t);
+        kIncidentB<<<dim3((inc.hi[0] - inc.lo[0] + 127) / 128, inc.hi[1] - inc.lo[1]), 128, 0, stream>>>(B, g, inc, t);
         return cudaGetLastError();
     }
 
     cudaError_t launchIncidentE(float* E, GridParams const& g, IncidentParams const& inc, float t, cudaStream_t stream)
     {
-        if(!inc.enabled)
+        if(!inc.enabled || inc.hi[0] <= inc.lo[0] || inc.hi[1] <= inc.lo[1])
             return cudaSuccess;
-        kIncidentE<<<dim3((g.nx + 127) / 128, g.nz), 128, 0, stream>>>(E, g, inc, t);
+        kIncidentE<<<dim3((inc.hi[0] - inc.lo[0] + 127) / 128, inc.hi[1] - inc.lo[1]), 128, 0, stream>>>(E, g, inc, t);
         return cudaGetLastError();
     }
 

@@ -124,6 +124,51 @@ namespace picgb::host
         return e;
     }
 
+    // Transverse extent of an incident-field face: a periodic transverse axis in full, an open one
+    // between its absorbers.  Along its own axis the surface must keep out of the absorber, as
+    // incidentField::detail::checkRequirements demands (Solver.hpp:113-168: the offset of the
+    // Huygens surface from an open boundary at least the absorber thickness).
+    int incidentExtent(picgb_sim* s, IncidentParams& p)
+    {
+        int const cells[3] = {s->cfg.nx, s->cfg.ny, s->cfg.nz};
+        int const a = p.axis;
+        if((s->g.open >> a) & 1)
+        {
+            // low face: POSITION >= thickness, surface = POSITION + 1; high face: cells - POSITION
+            // >= thickness, surface = POSITION - 1
+            bool const inside = p.dir > 0 ? p.plane < s->absorberThick[a][0] + 1
+                                          : p.plane > cells[a] - 1 - s->absorberThick[a][1];
+            if(inside)
+                return fail(PICGB_ERR_INVALID, "incident-field surface %d on axis %d lies in the absorber (%d + %d cells)",
+                            p.plane, a, s->absorberThick[a][0], s->absorberThick[a][1]);
+        }
+        int const tr[2] = {a == 0 ? 1 : 0, a == 2 ? 1 : 2};
+        for(int q = 0; q < 2; ++q)
+        {
+            int const d = tr[q];
+            bool const open = (s->g.open >> d) & 1;
+            p.lo[q] = open ? s->absorberThick[d][0] : 0;
+            p.hi[q] = open ? cells[d] - s->absorberThick[d][1] : cells[d];
+        }
+        return PICGB_OK;
+    }
+
+    // The incident-field correction of every enabled face: the B planes on the scattered side
+    // (bField) or the E planes on the total side.
+    int launchIncident(picgb_sim* s, bool bField, float t)
+    {
+        for(auto const& face : s->inc)
+        {
+            if(!face.enabled)
+                continue;
+            IncidentParams p = face;
+            if(int r = incidentExtent(s, p))
+                return r;
+            CUDA_TRY(bField ? launchIncidentB(s->B, s->g, p, t, s->stream) : launchIncidentE(s->E, s->g, p, t, s->stream));
+        }
+        return PICGB_OK;
+    }
+
     // Accumulate the completed event pairs (call after a stream synchronisation).
     cudaError_t profFlush(picgb_sim* s)
     {
@@ -999,14 +1044,16 @@ extern "C"
             return s->g.open ? launchYeeBHalfOpen(s->E, s->B, s->g, s->pml, false, s->stream)
                              : launchYeeBHalf(s->E, s->B, s->g, s->stream);
         }));
-        CUDA_TRY(launchIncidentB(s->B, s->g, s->inc, t, s->stream)); // incident E at t (Solver.hpp:500-533)
+        if(int r = launchIncident(s, true, t)) // incident E at t (Solver.hpp:500-533)
+            return r;
         // with the fused deposit J is complete here: E += curl B c^2 dt and E += coeff J in one pass
         float const* J = s->cfg.fuse_deposit ? s->J : nullptr;
         CUDA_TRY(timedLaunch(s, PICGB_KERNEL_YEE_E, [&] {
             return s->g.open ? launchYeeEOpen(s->B, s->E, J, s->coeffJ(), s->g, s->pml, s->stream)
                              : launchYeeE(s->B, s->E, J, s->coeffJ(), s->g, s->stream);
         }));
-        CUDA_TRY(launchIncidentE(s->E, s->g, s->inc, t + 0.5f * s->cfg.dt, s->stream)); // incident B at t + dt/2
+        if(int r = launchIncident(s, false, t + 0.5f * s->cfg.dt)) // incident B at t + dt/2
+            return r;
         if(s->expDamp) // exponential absorber on E (FDTDBase.hpp:121-124)
             CUDA_TRY(launchAbsorbExponential(s->E, s->g, s->expDamp, s->pml.nmax, s->stream));
         return PICGB_OK;
@@ -1053,7 +1100,8 @@ extern "C"
             return s->g.open ? launchYeeBHalfOpen(s->E, s->B, s->g, s->pml, true, s->stream)
                              : launchYeeBHalf(s->E, s->B, s->g, s->stream);
         }));
-        CUDA_TRY(launchIncidentB(s->B, s->g, s->inc, float(double(step + 1) * s->cfg.dt), s->stream)); // E at t + dt
+        if(int r = launchIncident(s, true, float(double(step + 1) * s->cfg.dt))) // incident E at t + dt
+            return r;
         if(s->expDamp) // exponential absorber on B (FDTDBase.hpp:178-182)
             CUDA_TRY(launchAbsorbExponential(s->B, s->g, s->expDamp, s->pml.nmax, s->stream));
         return PICGB_OK;
@@ -1102,6 +1150,9 @@ extern "C"
             ax[a].alphaOrder = ma;
             open |= 1 << a;
         }
+        for(int a = 0; a < 3; ++a)
+            for(int side = 0; side < 2; ++side)
+                s->absorberThick[a][side] = b->open[a] ? int(b->thickness[a][side]) : 0;
         CUDA_TRY(cudaSetDevice(s->cfg.device));
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         dfree(s->pml.psiE);
@@ -1140,20 +1191,37 @@ extern "C"
     {
         if(int r = checkSim(s))
             return r;
-        if(!f || !f->enabled)
+        if(!f)
         {
-            s->inc = IncidentParams{};
+            for(auto& face : s->inc)
+                face = IncidentParams{};
             return PICGB_OK;
         }
-        if(f->axis != 1)
-            return fail(PICGB_ERR_UNSUPPORTED, "the incident field enters along +y (axis 1) only");
-        if(f->surface < 1 || f->surface >= s->cfg.ny)
-            return fail(PICGB_ERR_INVALID, "incident-field surface %d outside 1..%d", int(f->surface), int(s->cfg.ny) - 1);
+        int const dir = f->direction == 0 ? 1 : f->direction;
+        if(f->axis < 0 || f->axis > 2 || (dir != 1 && dir != -1))
+            return fail(PICGB_ERR_INVALID, "incident field: axis %d must be 0, 1 or 2 and direction %d +1 or -1",
+                        int(f->axis), int(f->direction));
+        int const face = 2 * f->axis + (dir < 0 ? 1 : 0);
+        if(!f->enabled)
+        {
+            s->inc[face] = IncidentParams{};
+            return PICGB_OK;
+        }
+        int const cells[3] = {s->cfg.nx, s->cfg.ny, s->cfg.nz};
+        int const n = cells[f->axis];
+        int const lo = dir > 0 ? 1 : 0, hi = n - 1; // the scattered-side B plane exists: surface - 1 or surface
+        if(f->surface < lo || f->surface > hi)
+            return fail(PICGB_ERR_INVALID, "incident-field surface %d outside %d..%d on axis %d", int(f->surface), lo, hi,
+                        int(f->axis));
         if(!(f->wavelength > 0.0f && f->waist > 0.0f && f->duration_fwhm > 0.0f) || (f->polarisation != 0 && f->polarisation != 1))
             return fail(PICGB_ERR_INVALID, "incident field needs positive wavelength, waist, duration and polarisation 0 or 1");
+        if(!(f->focus == f->focus))
+            return fail(PICGB_ERR_INVALID, "incident field: focus is not a number");
         IncidentParams p{};
         p.enabled = 1;
-        p.j0 = f->surface;
+        p.axis = f->axis;
+        p.dir = dir;
+        p.plane = f->surface;
         p.pol = f->polarisation;
         double const omega = 2.0 * 3.14159265358979323846 * s->cfg.c / f->wavelength;
         // a0 = q E0 / (m c omega) with the species' units given by the caller through e_over_m = q / m
@@ -1162,15 +1230,15 @@ extern "C"
         p.w0 = f->waist;
         p.sigma = float(f->duration_fwhm / (2.0 * std::sqrt(std::log(2.0)))); // intensity FWHM -> field sigma
         p.tc = f->t_center;
-        p.cx = f->center_x;
-        p.cz = f->center_z;
+        p.c1 = f->center_x;
+        p.c2 = f->center_z;
         p.phase = f->phase;
-        if(!(f->focus == f->focus))
-            return fail(PICGB_ERR_INVALID, "incident field: focus is not a number");
-        p.yf = float(f->surface) + f->focus;
+        p.focus = f->focus;
         p.zR = float(3.14159265358979323846 * double(f->waist) * double(f->waist) / double(f->wavelength));
         p.k = float(omega / s->cfg.c);
-        s->inc = p;
+        if(int r = incidentExtent(s, p))
+            return r;
+        s->inc[face] = p;
         return PICGB_OK;
     }
 

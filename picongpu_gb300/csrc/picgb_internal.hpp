@@ -102,16 +102,24 @@ namespace picgb
     // field at (x, y, z, t) is E0 exp(-r^2 / w0^2) exp(-(tau - tc)^2 / (2 sigma^2))
     // sin(omega (tau - tc) + phase), tau = t - (y - j0 dy) / c, r the distance from the
     // axis (cx, cz), polarised along x (pol 0) or z (pol 1), travelling along +y.
+    // One face of the total-field/scattered-field box.  Transverse axes: the two axes other
+    // than `axis`, in increasing order (first, second).
     struct IncidentParams
     {
         int enabled;
-        int j0; // first E plane of the total-field region
-        int pol;
-        float E0, omega, w0, sigma, tc, cx, cz, phase;
-        float yf; // focus plane (cells)
+        int axis; // propagation axis
+        int dir; // +1: enters through the low face, travels +axis; -1: the high face, travels -axis
+        int plane; // first (dir +1) or last (dir -1) E plane of the total-field region along axis
+        int pol; // E along the first (0) or second (1) transverse axis
+        float E0, omega, w0, sigma, tc;
+        float c1, c2; // beam centre on the first and second transverse axis (cells)
+        float phase;
+        float focus; // distance of the focus beyond the surface along the propagation (cells)
         float zR; // Rayleigh length pi w0^2 / wavelength
         float k; // wave number omega / c
+        int lo[2], hi[2]; // transverse extent of the face in cells, [lo, hi) on each transverse axis
     };
+    constexpr int kIncidentFaces = 6; // face = 2 axis + (dir < 0)
 
     // ---- launchers (kernels_*.cu); all asynchronous on `stream`
     // shape: 1 CIC, 2 TSC, 3 PQS; scId: 0 -> 8x8x4, 1 -> 4x4x4, 2 -> 8x8x8

@@ -136,7 +136,8 @@ struct picgb_sim
     cudaStream_t stream = nullptr;
     bool ownStream = false;
     bool inEnsemble = false; // owned by a picgb_ensemble: not destroyed through picgb_destroy
-    picgb::IncidentParams inc{}; // incident pulse (TF/SF surface), disabled by default
+    picgb::IncidentParams inc[picgb::kIncidentFaces]{}; // incident pulses by TF/SF face, all disabled by default
+    int absorberThick[3][2] = {}; // absorber cells at the low and high face of each open axis (0 when periodic)
     picgb::PmlDev pml{}; // open boundaries: convolution fields and coefficient tables (g.open != 0)
     float* pmlTab = nullptr;
     float* expDamp = nullptr; // exponential absorber: damping factors [3][pml.nmax], or null

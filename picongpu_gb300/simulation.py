@@ -297,17 +297,29 @@ class Simulation:
     # ------------------------------------------------------------ stepping
     def set_incident_field(self, a0: float, wavelength: float, waist: float, duration_fwhm: float, t_center: float,
                            surface: int, polarisation: int = 0, center=None, phase: float = 0.0,
-                           e_over_m: float = 1.0, focus: float = 0.0) -> None:
-        """Focused Gaussian pulse entering along +y through the TF/SF surface y = surface
-        (fields/incidentField/Solver.hpp, profiles/GaussianPulse.hpp), its focus `focus`
-        cells beyond the surface; see picgb_set_incident_field."""
-        cx, cz = center if center is not None else (self.grid.nx / 2.0, self.grid.nz / 2.0)
-        f = L.IncidentField(1, 1, surface, polarisation, a0, e_over_m, wavelength, waist, duration_fwhm, t_center, cx, cz,
-                            phase, focus)
+                           e_over_m: float = 1.0, focus: float = 0.0, axis: int = 1, direction: int = 1) -> None:
+        """Focused Gaussian pulse entering through the TF/SF face normal to `axis` (0, 1, 2):
+        direction +1 from the low face along +axis, -1 from the high face along -axis
+        (fields/incidentField/Solver.hpp, profiles/GaussianPulse.hpp).  `surface` is the first
+        (+1) or last (-1) E plane of the total-field region, the focus lies `focus` cells beyond
+        it, `center` is the beam centre on the two transverse axes in increasing order (default:
+        the middle), `polarisation` 0 or 1 puts E along the first or the second of them.  Each
+        face holds its own pulse; see picgb_set_incident_field."""
+        cells = (self.grid.nx, self.grid.ny, self.grid.nz)
+        t1, t2 = [d for d in range(3) if d != axis] if axis in (0, 1, 2) else (0, 2)
+        c1, c2 = center if center is not None else (cells[t1] / 2.0, cells[t2] / 2.0)
+        f = L.IncidentField(1, axis, surface, polarisation, a0, e_over_m, wavelength, waist, duration_fwhm, t_center,
+                            c1, c2, phase, focus, direction)
         L.call("picgb_set_incident_field", self.handle, ctypes.byref(f))
 
-    def clear_incident_field(self) -> None:
+    def clear_incident_field(self, axis: int | None = None, direction: int = 1) -> None:
+        """Switch off the pulse of one face (axis, direction), or of every face (axis None)."""
+        if axis is None:
+            L.call("picgb_set_incident_field", self.handle, None)
+            return
         f = L.IncidentField()
+        f.axis = axis
+        f.direction = direction
         L.call("picgb_set_incident_field", self.handle, ctypes.byref(f))
 
     def step(self) -> None:
