@@ -253,21 +253,27 @@ extern "C"
      * spans a periodic transverse axis in full and an open one between its absorbers; on an open
      * axis the surface must keep out of the absorber (Solver.hpp:113-168), which every field stage
      * checks (PICGB_ERR_INVALID).  The pulse is the focused Gaussian beam of
-     * profiles/GaussianPulse.hpp:223-290 (fundamental mode, B from E by the slowly varying
-     * envelope approximation, incidentField::detail::ApproximateIncidentB):
-     *   E = E0 (w0/w) exp(-r^2/w^2) exp(-(tau - t_center - r_c/c)^2 / (2 sigma^2))
-     *       sin(omega (tau - t_center) - k r_c + xi + phase),
-     *   zeta = direction (u - surface) the distance travelled beyond the surface (u the
-     *   coordinate along the axis, in cells), tau = t - zeta d/c, r the transverse distance from
-     *   the centre, z_f = (focus - zeta) d the distance to the focus, z_R = pi w0^2 / wavelength,
-     *   w = w0 sqrt(1 + (z_f/z_R)^2), r_c = r^2/2 * (-z_f / (z_R^2 + z_f^2)) (wavefront curvature),
-     *   xi = atan(-z_f / z_R) (Gouy phase), w0 = waist,
-     *   omega = 2 pi c / wavelength, k = omega / c, E0 = a0 omega c / e_over_m,
-     *   sigma = duration_fwhm / (2 sqrt(ln 2)) (duration_fwhm of the intensity).
-     * focus = 0 puts the focus on the surface.  Each of the six faces holds its own pulse:
-     * setting a face replaces that face's pulse, enabled = 0 switches the face (axis, direction)
-     * off, and a NULL field switches every face off.  Propagation oblique to the face (the
-     * reference's DIRECTION_{X,Y,Z} off the axis) is not supported. */
+     * profiles/GaussianPulse.hpp:206-290 (fundamental mode, linear polarisation, B = direction x
+     * E / c: incidentField::detail::ApproximateIncidentB), at a position u along the axis (in
+     * cells) and time t:
+     *   dist = direction (u - origin) d, origin = surface - direction / 4 (the Huygens surface),
+     *   t_loc = t - dist / v_ph with v_ph the Yee grid's phase velocity at omega along the axis
+     *     (calculatePhaseVelocity.hpp; sin(k d/2)/d = sin(omega dt/2)/(c dt)); E = 0 while t_loc < 0,
+     *   time = t_loc - t_center, z_f = focus d - dist (distance to the focus),
+     *   w = w0 sqrt(1 + (z_f/z_R)^2), z_R = pi w0^2 / wavelength, w0 = waist,
+     *   r_c = r^2/2 * (-z_f / (z_R^2 + z_f^2)) with r the transverse distance from the centre,
+     *   E = E0 (w0/w) exp(-r^2/w^2) cos(k z_f - k r_c + xi + omega (time - z_f/c) + phase)
+     *       exp(-((time - r_c/c) / (2 tau))^2),
+     *   xi = atan(-z_f / z_R) (Gouy phase), omega = 2 pi c / wavelength, k = omega / c,
+     *   E0 = a0 omega c / e_over_m, tau = duration_fwhm / (2 sqrt(2 ln 2)) (the rms duration of the
+     *   intensity; duration_fwhm its FWHM).
+     * In the reference's terms: phase = LASER_PHASE, t_center = PULSE_INIT * PULSE_DURATION / 2,
+     * PULSE_DURATION = tau, focus = the distance of FOCUS_POSITION beyond the Huygens surface (0:
+     * on it), center_x/center_z = FOCUS_POSITION on the transverse axes.  Each of the six faces
+     * holds its own pulse: setting a face replaces that face's pulse, enabled = 0 switches the face
+     * (axis, direction) off, and a NULL field switches every face off.  Propagation oblique to the
+     * face (the reference's DIRECTION_{X,Y,Z} off the axis), circular polarisation, Laguerre modes
+     * and TIME_DELAY are not supported. */
     typedef struct picgb_incident_field
     {
         int32_t enabled;
@@ -275,7 +281,7 @@ extern "C"
         int32_t surface;
         int32_t polarisation;
         float a0, e_over_m, wavelength, waist, duration_fwhm, t_center, center_x, center_z, phase;
-        float focus; /* distance of the focus beyond the surface along the propagation, in cells */
+        float focus; /* distance of the focus beyond the Huygens surface along the propagation, in cells */
         int32_t direction; /* +1 (or 0): travels +axis from the low face; -1: travels -axis from the high face */
     } picgb_incident_field;
     int picgb_set_incident_field(picgb_sim* sim, const picgb_incident_field* field);

@@ -58,6 +58,14 @@ class OrcField(ctypes.Structure):
     _fields_ = [("c", ctypes.c_void_p * 3)]
 
 
+class OrcIncidentFace(ctypes.Structure):
+    _fields_ = [("axis", ctypes.c_int), ("dir", ctypes.c_int), ("surface", ctypes.c_int),
+                ("polv", ctypes.c_float * 3), ("focus", ctypes.c_float * 3),
+                ("amplitude", ctypes.c_float), ("wavelength", ctypes.c_float), ("w0", ctypes.c_float),
+                ("pulse_duration", ctypes.c_float), ("time_shift", ctypes.c_float), ("laser_phase", ctypes.c_float),
+                ("phase_velocity", ctypes.c_float)]
+
+
 class OrcParticles64(ctypes.Structure):
     _fields_ = [
         ("n", ctypes.c_uint64),
@@ -108,6 +116,7 @@ def lib() -> ctypes.CDLL:
         L.orc_move_particle.argtypes = [P(OrcGrid), vp, vp, vp]
         L.orc_gather.argtypes = [P(OrcGrid), ctypes.c_int, P(OrcField), ctypes.c_int, vp, vp, vp]
         L.orc_yee_b_half.argtypes = [P(OrcGrid), P(OrcField), P(OrcField)]
+        L.orc_incident_update.argtypes = [P(OrcGrid), P(OrcIncidentFace), P(OrcField), ctypes.c_int, ctypes.c_float]
         L.orc_yee_e.argtypes = [P(OrcGrid), P(OrcField), P(OrcField)]
         L.orc_add_current.argtypes = [P(OrcGrid), P(OrcField), P(OrcField)]
         L.orc_push.argtypes = [P(OrcGrid), P(OrcSpecies), P(OrcParticles), P(OrcField), P(OrcField)]
@@ -208,6 +217,38 @@ def particles(p: dict) -> OrcParticles:
 
 def set_threads(n: int) -> None:
     lib().orc_set_threads(int(n))
+
+
+def incident_face(g, axis, direction, surface, polarisation, a0, wavelength, waist, pulse_duration, time_shift,
+                  laser_phase, focus_position, e_over_m=1.0):
+    """One incident-field face in the reference's parameters (profiles/BaseParam.def,
+    GaussianPulse.def): the E polarisation is the unit vector along the transverse axis
+    `polarisation` (0: the first of the two other axes in increasing order, 1: the second),
+    focus_position is absolute (length units), pulse_duration the rms duration of the
+    intensity (PULSE_DURATION), time_shift = -PULSE_INIT * PULSE_DURATION / 2, and the phase
+    velocity follows from the Yee dispersion relation along the axis (calculatePhaseVelocity.hpp)."""
+    import math
+    f = OrcIncidentFace()
+    f.axis, f.dir, f.surface = int(axis), int(direction), int(surface)
+    t = [d for d in range(3) if d != axis]
+    f.polv[t[polarisation]] = 1.0
+    for d in range(3):
+        f.focus[d] = float(focus_position[d])
+    c, dt = float(g["c"]), float(g["dt"])
+    d_a = float((g["dx"], g["dy"], g["dz"])[axis])
+    omega = 2 * math.pi * c / wavelength
+    k = 2.0 / d_a * math.asin(d_a / (c * dt) * math.sin(omega * dt / 2))
+    f.phase_velocity = omega / k
+    f.amplitude = a0 * omega * c / e_over_m
+    f.wavelength, f.w0, f.pulse_duration = wavelength, waist, pulse_duration
+    f.time_shift, f.laser_phase = time_shift, laser_phase
+    return f
+
+
+def incident_update(g, face: OrcIncidentFace, F, update_b: bool, t: float):
+    """TF/SF correction of one face (incidentField/Solver.kernel) after a B half step
+    (update_b, incident E at t) or the E step (incident B at t), in place on F."""
+    lib().orc_incident_update(grid(g), ctypes.byref(face), field(F), int(bool(update_b)), float(t))
 
 
 def yee_b_half(g, E, B):

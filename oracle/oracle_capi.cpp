@@ -39,6 +39,13 @@ extern "C"
         int32_t* sc;
         uint16_t* lcell;
     };
+    // one face of the incident field (orc::IncidentFace)
+    struct orc_incident_face
+    {
+        int axis, dir, surface;
+        float polv[3], focus[3];
+        float amplitude, wavelength, w0, pulse_duration, time_shift, laser_phase, phase_velocity;
+    };
     // the FP64 instantiation's exchange format (reference gradients of the differentiable run)
     struct orc_field64
     {
@@ -145,6 +152,30 @@ extern "C"
     {
         orc::Grid G = toGrid(g);
         orc::gather(G, shape, toF(F), isB ? orc::kPosB : orc::kPosE, cell, pos, out);
+    }
+
+    // TF/SF correction of one incident-field face after a B half step (update_b = 1, incident E
+    // at time t) or after the E step (update_b = 0, incident B at time t).
+    void orc_incident_update(orc_grid const* g, orc_incident_face const* f, orc_field* F, int update_b, float t)
+    {
+        orc::IncidentFace face;
+        face.axis = f->axis;
+        face.dir = f->dir;
+        face.surface = f->surface;
+        for(int d = 0; d < 3; ++d)
+        {
+            face.polv[d] = f->polv[d];
+            face.focus[d] = f->focus[d];
+        }
+        face.amplitude = f->amplitude;
+        face.wavelength = f->wavelength;
+        face.w0 = f->w0;
+        face.pulseDuration = f->pulse_duration;
+        face.timeShift = f->time_shift;
+        face.laserPhase = f->laser_phase;
+        face.phaseVelocity = f->phase_velocity;
+        auto Ff = toF(F);
+        orc::incidentUpdate(toGrid(g), face, Ff, update_b != 0, t);
     }
 
     void orc_yee_b_half(orc_grid const* g, orc_field const* E, orc_field* B)

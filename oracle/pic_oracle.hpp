@@ -1202,6 +1202,134 @@ namespace orc
         }
     }
 
+    // ---------------------------------------------------------------- incident field (TF/SF)
+    // One face of the Huygens box carrying the focused Gaussian pulse of
+    // profiles/GaussianPulse.hpp:206-290 (linear polarisation, fundamental Laguerre mode), in the
+    // reference's vector form (fields/incidentField/Functors.hpp BaseFunctorE): the origin is the
+    // focus projected along the propagation direction onto the Huygens surface (0.75 cells
+    // inside POSITION, getOrigin), the local time runs from it at the grid's phase velocity
+    // (getCurrentTime), internal coordinates are dot products with the direction (axis0), the
+    // polarisation (axis1) and their cross product (axis2).  POSITION: the first total E plane
+    // of a low face is POSITION + 1, the last of a high face POSITION - 1.
+    struct IncidentFace
+    {
+        int axis = 1, dir = 1; // propagation axis and direction (+1: low face, -1: high face)
+        int surface = 1; // first (dir +1) or last (dir -1) E plane of the total-field region
+        float polv[3] = {1.f, 0.f, 0.f}; // unit E polarisation, orthogonal to the axis
+        float focus[3] = {0.f, 0.f, 0.f}; // focus position (length units)
+        float amplitude = 1.f; // E0
+        float wavelength = 1.f, w0 = 1.f;
+        float pulseDuration = 1.f; // rms duration of the intensity (PULSE_DURATION)
+        float timeShift = 0.f; // GaussianPulseEnvelope::TIME_SHIFT = -PULSE_INIT * PULSE_DURATION / 2
+        float laserPhase = 0.f;
+        float phaseVelocity = 1.f; // calculatePhaseVelocity, times c
+    };
+
+    inline float dotf(float const a[3], float const b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+    // E (or B = direction x E / c: ApproximateIncidentB) of the face at total cell index idx
+    // (fractional, cells) and time t.
+    inline void incidentFieldAt(Grid const& g, IncidentFace const& f, float const idx[3], float t, bool wantB, float out[3])
+    {
+        float const cell[3] = {g.dx, g.dy, g.dz};
+        float dirv[3] = {0.f, 0.f, 0.f};
+        dirv[f.axis] = float(f.dir);
+        // getOrigin: the focus moved along the direction onto the Huygens surface of the face
+        float const minPos = (float(f.surface - 1) + 0.75f) * cell[f.axis];
+        float const maxPos = (float(f.surface + 1) - 0.75f) * cell[f.axis];
+        float origin[3] = {f.focus[0], f.focus[1], f.focus[2]};
+        origin[f.axis] = f.dir > 0 ? minPos : maxPos;
+        float shift[3];
+        for(int d = 0; d < 3; ++d)
+            shift[d] = idx[d] * cell[d] - origin[d];
+        float const pos0 = dotf(shift, dirv);
+        float const currentTime = t - pos0 / f.phaseVelocity;
+        float value = 0.f;
+        if(!(currentTime < 0.f)) // cut off before the pulse reaches this point
+        {
+            float const time = currentTime + f.timeShift;
+            float const axis2[3] = {dirv[1] * f.polv[2] - dirv[2] * f.polv[1], dirv[2] * f.polv[0] - dirv[0] * f.polv[2],
+                                    dirv[0] * f.polv[1] - dirv[1] * f.polv[0]};
+            float const pos1 = dotf(shift, f.polv), pos2 = dotf(shift, axis2);
+            float focusRel[3];
+            for(int d = 0; d < 3; ++d)
+                focusRel[d] = f.focus[d] - origin[d];
+            float const focusPos = dotf(focusRel, dirv) - pos0;
+            float const zR = 3.14159265358979323846f * f.w0 * f.w0 / f.wavelength;
+            float const w = f.w0 * std::sqrt(1.f + (focusPos / zR) * (focusPos / zR));
+            float const omega = 2.f * 3.14159265358979323846f * g.c / f.wavelength;
+            float const phase = omega * (time - focusPos / g.c) + f.laserPhase;
+            float const r2 = pos1 * pos1 + pos2 * pos2;
+            float const rInv = -focusPos / (zR * zR + focusPos * focusPos);
+            float const xi = std::atan(-focusPos / zR);
+            float const r2OverW2 = r2 / w / w;
+            float const r = 0.5f * r2 * rInv;
+            float const k = 2.f * 3.14159265358979323846f / f.wavelength;
+            float etrans = std::exp(-r2OverW2) * std::cos(k * focusPos - k * r + xi + phase);
+            float const shiftedTime = time - r / g.c;
+            float const exponent = shiftedTime / (2.f * f.pulseDuration);
+            etrans *= std::exp(-exponent * exponent);
+            value = f.amplitude * (f.w0 / w) * etrans;
+        }
+        float E[3] = {f.polv[0] * value, f.polv[1] * value, f.polv[2] * value};
+        if(!wantB)
+        {
+            for(int d = 0; d < 3; ++d)
+                out[d] = E[d];
+            return;
+        }
+        out[0] = (dirv[1] * E[2] - dirv[2] * E[1]) / g.c;
+        out[1] = (dirv[2] * E[0] - dirv[0] * E[2]) / g.c;
+        out[2] = (dirv[0] * E[1] - dirv[1] * E[0]) / g.c;
+    }
+
+    // TF/SF correction of one face after a field update (incidentField/Solver.kernel
+    // UpdateFunctor for the Yee curl, margin 1):
+    //   updated[comp2] += base * incident[comp1](shift1), updated[comp1] -= base * incident[comp2](shift2),
+    //   comp1 = (axis + 2) % 3, comp2 = (axis + 1) % 3, base = curlCoefficient / d_axis * dir,
+    // curlCoefficient = -dt/2 for a B half step (incident E) and c^2 dt for the E step (incident B).
+    // The updated plane along the axis is the first total E plane (E) or the scattered B plane
+    // before it (B) for a low face, the last total E plane and the B plane after it for a high
+    // face (Solver.hpp:206-266); the incident field is taken at the updated cell plus its Yee
+    // position, shifted along the axis by -1 (E) or +1 (B) on a low face (Solver.hpp:343-356).
+    inline void incidentUpdate(Grid const& g, IncidentFace const& f, Field3<float>& F, bool updateB, float t)
+    {
+        int const a = f.axis, comp1 = (a + 2) % 3, comp2 = (a + 1) % 3;
+        float const cell[3] = {g.dx, g.dy, g.dz};
+        float const curl = updateB ? -0.5f * g.dt : g.c * g.c * g.dt;
+        float const base = curl / cell[a] * (f.dir > 0 ? 1.f : -1.f);
+        int const plane = (updateB && f.dir > 0) ? f.surface - 1 : f.surface;
+        float baseShift = 0.f;
+        if(f.dir > 0)
+            baseShift = updateB ? 1.f : -1.f;
+        // Yee positions of the incident field's components (B when E is updated, E when B is)
+        auto const& incPos = updateB ? kPosE : kPosB;
+        int const n[3] = {g.nx, g.ny, g.nz};
+        int const u = a == 0 ? 1 : 0, v = a == 2 ? 1 : 2;
+        for(int j = 0; j < n[v]; ++j)
+            for(int i = 0; i < n[u]; ++i)
+            {
+                int c[3];
+                c[a] = plane;
+                c[u] = i;
+                c[v] = j;
+                float s1[3], s2[3];
+                for(int d = 0; d < 3; ++d)
+                {
+                    s1[d] = float(c[d]) + incPos[comp1][d];
+                    s2[d] = float(c[d]) + incPos[comp2][d];
+                }
+                s1[a] += baseShift;
+                s2[a] += baseShift;
+                float inc1[3], inc2[3];
+                incidentFieldAt(g, f, s1, t, !updateB, inc1);
+                incidentFieldAt(g, f, s2, t, !updateB, inc2);
+                size_t const id = g.idx(c[0], c[1], c[2]);
+                F.c[comp2][id] += base * inc1[comp1];
+                F.c[comp1][id] -= base * inc2[comp2];
+            }
+    }
+
     // ---------------------------------------------------------------- full step
     // Simulation::runOneStep (simulation/control/Simulation.hpp:522-542):
     // CurrentReset, ParticlePush (+shift), update_beforeCurrent (B half, E),

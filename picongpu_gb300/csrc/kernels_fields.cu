@@ -104,26 +104,35 @@ namespace picgb
     __device__ __forceinline__ float pick3(float v0, float v1, float v2, int i) { return i == 0 ? v0 : (i == 1 ? v1 : v2); }
 
     // Incident pulse value at (x, y, z) in cell units and time t: the focused Gaussian beam of
-    // profiles/GaussianPulse.hpp:223-290 in its fundamental mode (waist w(z_f), wavefront
-    // curvature, Gouy phase, amplitude w0/w, the envelope shifted by the curvature's delay),
-    // propagating along the face's axis in the face's direction.
+    // profiles/GaussianPulse.hpp:206-290 in its fundamental mode, in the reference's order of
+    // operations.  The local time runs from the Huygens surface at the grid's phase velocity
+    // (Functors.hpp getCurrentTime) and the field is zero before it starts there; the waist
+    // w(z_f), the phase omega (time - z_f / c) + phase, the wavefront curvature, the Gouy phase,
+    // the cosine carrier, the envelope exp(-(t_s / 2 tau)^2) of the curvature-delayed time and
+    // the amplitude w0 / w follow GaussianPulse.hpp:214-290 and GaussianPulseEnvelope.
     __device__ __forceinline__ float incidentValue(IncidentParams const& p, GridParams const& g, float x, float y, float z, float t)
     {
         int const a = p.axis, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
         float const da = pick3(g.dx, g.dy, g.dz, a);
+        float const dist = float(p.dir) * (pick3(x, y, z, a) - p.origin) * da; // beyond the Huygens surface
+        float const tcur = t - dist * p.invVph;
+        if(tcur < 0.0f)
+            return 0.0f;
+        float const time = tcur - p.tc;
         float const r1 = (pick3(x, y, z, t1) - p.c1) * pick3(g.dx, g.dy, g.dz, t1);
         float const r2_ = (pick3(x, y, z, t2) - p.c2) * pick3(g.dx, g.dy, g.dz, t2);
         float const r2 = r1 * r1 + r2_ * r2_;
-        float const zeta = float(p.dir) * (pick3(x, y, z, a) - float(p.plane)); // cells beyond the surface
-        float const tau = t - zeta * da / g.c - p.tc;
-        float const zf = (p.focus - zeta) * da; // distance to the focus along the propagation
-        float const q = zf / p.zR;
-        float const w2 = p.w0 * p.w0 * (1.0f + q * q);
-        float const rc = 0.5f * r2 * (-zf / (p.zR * p.zR + zf * zf)); // r^2/2 times the inverse curvature radius
-        float const xi = atanf(-q); // Gouy phase
-        float const ts = tau - rc / g.c;
-        float const env = sqrtf(p.w0 * p.w0 / w2) * expf(-r2 / w2) * expf(-(ts * ts) / (2.0f * p.sigma * p.sigma));
-        return p.E0 * env * sinf(p.omega * tau - p.k * rc + xi + p.phase);
+        float const fp = p.focusDist - dist; // distance to the focus along the propagation
+        float const w = p.w0 * sqrtf(1.0f + (fp / p.zR) * (fp / p.zR));
+        float const phase = p.omega * (time - fp / g.c) + p.phase;
+        float const rInv = -fp / (p.zR * p.zR + fp * fp); // inverse radius of curvature
+        float const xi = atanf(-fp / p.zR); // Gouy phase
+        float const r2OverW2 = r2 / w / w;
+        float const rc = 0.5f * r2 * rInv;
+        float et = expf(-r2OverW2) * cosf(p.k * fp - p.k * rc + xi + phase);
+        float const e = (time - rc / g.c) / p.tau2;
+        et *= expf(-e * e);
+        return p.E0 * (p.w0 / w) * et;
     }
 
     // Cell (i, j, k) of a face node: `planeIdx` along the axis, (u1, u2) on the transverse axes.

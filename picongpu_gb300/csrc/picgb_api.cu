@@ -1228,12 +1228,24 @@ extern "C"
         p.E0 = float(f->a0 * omega * s->cfg.c / f->e_over_m);
         p.omega = float(omega);
         p.w0 = f->waist;
-        p.sigma = float(f->duration_fwhm / (2.0 * std::sqrt(std::log(2.0)))); // intensity FWHM -> field sigma
+        // intensity FWHM = 2 sqrt(2 ln 2) tau with tau the rms duration of the intensity
+        // (GaussianPulseEnvelope: exp(-(t / (2 tau))^2) on the field)
+        p.tau2 = float(f->duration_fwhm / std::sqrt(2.0 * std::log(2.0)));
         p.tc = f->t_center;
         p.c1 = f->center_x;
         p.c2 = f->center_z;
         p.phase = f->phase;
-        p.focus = f->focus;
+        double const edge[3] = {s->cfg.dx, s->cfg.dy, s->cfg.dz};
+        double const da = edge[f->axis];
+        p.origin = float(double(f->surface) - 0.25 * dir); // 0.75 cells inside POSITION
+        p.focusDist = float(double(f->focus) * da);
+        // phase velocity of the Yee grid at omega along the axis (calculatePhaseVelocity.hpp with the
+        // Yee dispersion relation): sin(k d / 2) / d = sin(omega dt / 2) / (c dt)
+        double const sk = da / (double(s->cfg.c) * double(s->cfg.dt)) * std::sin(0.5 * omega * double(s->cfg.dt));
+        if(!(sk > 0.0 && sk < 1.0))
+            return fail(PICGB_ERR_INVALID, "incident field: wavelength %g is not resolved by the grid", double(f->wavelength));
+        double const kNum = 2.0 / da * std::asin(sk);
+        p.invVph = float(kNum / omega);
         p.zR = float(3.14159265358979323846 * double(f->waist) * double(f->waist) / double(f->wavelength));
         p.k = float(omega / s->cfg.c);
         if(int r = incidentExtent(s, p))

@@ -111,10 +111,13 @@ namespace picgb
         int dir; // +1: enters through the low face, travels +axis; -1: the high face, travels -axis
         int plane; // first (dir +1) or last (dir -1) E plane of the total-field region along axis
         int pol; // E along the first (0) or second (1) transverse axis
-        float E0, omega, w0, sigma, tc;
+        float E0, omega, w0, tc;
+        float tau2; // twice the rms duration of the intensity (the envelope is exp(-(t / tau2)^2))
         float c1, c2; // beam centre on the first and second transverse axis (cells)
         float phase;
-        float focus; // distance of the focus beyond the surface along the propagation (cells)
+        float origin; // Huygens surface along the axis: plane - dir / 4 (cells)
+        float focusDist; // distance of the focus beyond the Huygens surface (length)
+        float invVph; // 1 / the Yee grid's phase velocity at omega along the axis
         float zR; // Rayleigh length pi w0^2 / wavelength
         float k; // wave number omega / c
         int lo[2], hi[2]; // transverse extent of the face in cells, [lo, hi) on each transverse axis

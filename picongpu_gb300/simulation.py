@@ -302,9 +302,11 @@ class Simulation:
         direction +1 from the low face along +axis, -1 from the high face along -axis
         (fields/incidentField/Solver.hpp, profiles/GaussianPulse.hpp).  `surface` is the first
         (+1) or last (-1) E plane of the total-field region, the focus lies `focus` cells beyond
-        it, `center` is the beam centre on the two transverse axes in increasing order (default:
-        the middle), `polarisation` 0 or 1 puts E along the first or the second of them.  Each
-        face holds its own pulse; see picgb_set_incident_field."""
+        the Huygens surface (a quarter cell before that plane), `center` is the beam centre on
+        the two transverse axes in increasing order (default: the middle), `polarisation` 0 or 1
+        puts E along the first or the second of them, `phase` is the reference's LASER_PHASE of
+        the cosine carrier and `t_center` its PULSE_INIT * PULSE_DURATION / 2.  Each face holds
+        its own pulse; see picgb_set_incident_field."""
         cells = (self.grid.nx, self.grid.ny, self.grid.nz)
         t1, t2 = [d for d in range(3) if d != axis] if axis in (0, 1, 2) else (0, 2)
         c1, c2 = center if center is not None else (cells[t1] / 2.0, cells[t2] / 2.0)

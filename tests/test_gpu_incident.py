@@ -4,7 +4,8 @@ Vacuum box 16 x 256 x 16 (periodic), surface at y = 32, a transversely uniform
 pulse (wavelength 16 cells, intensity FWHM 20 dt) travelling +y, polarised along x
 or z.  A transversely uniform wave on the 3D Yee grid obeys the 1D Yee scheme
 exactly, so a float64 numpy restatement of the 1D split update with the same
-TF/SF corrections is the reference.  Contract after 200 steps:
+TF/SF corrections is the reference (the pulse of profiles/GaussianPulse.hpp with its waist
+going to infinity).  Contract after 200 steps:
 * the tangential E and B on every (x, z) line match the 1D reference within 1e-4
   of the amplitude;
 * the scattered-field region holds less than 1e-5 of the amplitude (no backward leak);
@@ -26,11 +27,22 @@ LAM = 16.0
 STEPS = 200
 
 
+def phase_velocity(g, omega):
+    """The Yee grid's phase velocity along y: sin(k dy / 2) / dy = sin(omega dt / 2) / (c dt)."""
+    dt = float(np.float32(g.dt))
+    k = 2.0 / g.dy * math.asin(g.dy / (g.c * dt) * math.sin(omega * dt / 2))
+    return omega / k
+
+
 def incident(y, t, g, fwhm, tc):
+    """The plane pulse (waist -> infinity) of profiles/GaussianPulse.hpp: the local time runs from
+    the Huygens surface J0 - 1/4 at the grid's phase velocity, zero before it starts, cosine
+    carrier, envelope exp(-(time / 2 tau)^2) with tau the rms duration of the intensity."""
     omega = 2 * math.pi * g.c / LAM
-    sigma = fwhm / (2 * math.sqrt(math.log(2)))
-    tau = t - (y - J0) * g.dy / g.c - tc
-    return omega * np.exp(-tau ** 2 / (2 * sigma ** 2)) * np.sin(omega * tau)
+    tau2 = fwhm / math.sqrt(2 * math.log(2))
+    tloc = t - (y - (J0 - 0.25)) * g.dy / phase_velocity(g, omega)
+    time = tloc - tc
+    return np.where(tloc < 0, 0.0, omega * np.exp(-(time / tau2) ** 2) * np.cos(omega * time))
 
 
 def yee_1d(g, fwhm, tc, steps):
@@ -55,10 +67,11 @@ def analytic(t, y, g, fwhm, tc):
     """The pulse with its carrier at the Yee grid's wavenumber k for omega,
     sin(k dy / 2) / dy = sin(omega dt / 2) / (c dt), and its envelope moving at c."""
     omega = 2 * math.pi * g.c / LAM
-    k = 2.0 / g.dy * math.asin(g.dy / (g.c * g.dt) * math.sin(omega * g.dt / 2))
-    sigma = fwhm / (2 * math.sqrt(math.log(2)))
-    tau = t - (y - J0) * g.dy / g.c - tc
-    out = omega * np.exp(-tau ** 2 / (2 * sigma ** 2)) * np.sin(omega * (t - tc) - k * (y - J0) * g.dy)
+    k = omega / phase_velocity(g, omega)
+    tau2 = fwhm / math.sqrt(2 * math.log(2))
+    y0 = J0 - 0.25
+    env = t - (y - y0) * g.dy / g.c - tc
+    out = omega * np.exp(-(env / tau2) ** 2) * np.cos(omega * (t - tc) - k * (y - y0) * g.dy)
     out[y < J0] = 0.0
     return out
 

@@ -4,7 +4,8 @@
 * Every axis, both directions and both polarisations: a transversely uniform pulse
   (wavelength 16 cells, intensity FWHM 20 dt) in a vacuum box 256 cells long along the axis
   and 16 across obeys the 1D Yee scheme exactly, so a float64 restatement of the 1D split
-  update with the TF/SF corrections of either direction is the reference: the tangential
+  update with the TF/SF corrections of either direction, fed with the plane pulse of
+  profiles/GaussianPulse.hpp (waist -> infinity), is the reference: the tangential
   E and B on two lines along the axis match it within 1e-4 of the amplitude, and the
   scattered-field region beyond the surface holds less than 1e-5 of it.
 * A focused beam (waist 6, wavelength 8, focus 5 cells beyond the surface) through the +x
@@ -19,6 +20,7 @@ import numpy as np
 import pytest
 
 import picongpu_gb300 as pg
+from incident_1d import line, yee_1d
 
 pytestmark = pytest.mark.gpu
 
@@ -32,44 +34,6 @@ def dims(axis, long, across):
     d = [across] * 3
     d[axis] = long
     return d
-
-
-def incident(u, t, P, direction, da, c, fwhm, tc):
-    omega = 2 * math.pi * c / LAM
-    sigma = fwhm / (2 * math.sqrt(math.log(2)))
-    tau = t - direction * (u - P) * da / c - tc
-    return omega * np.exp(-tau ** 2 / (2 * sigma ** 2)) * np.sin(omega * tau)
-
-
-def yee_1d(n, P, direction, g, fwhm, tc, steps):
-    """E_p (integer positions) and B' (half-integer positions, B' = eta B_o) of the 1D split
-    Yee update with the TF/SF corrections: dB'/dt = dE/du, dE/dt = c^2 dB'/du; the scattered-
-    side B plane is P - 1 (direction +1) or P (direction -1)."""
-    E = np.zeros(n)
-    Bt = np.zeros(n)
-    dt, da, c = float(np.float32(g.dt)), g.dx, g.c
-    bidx = P - 1 if direction > 0 else P
-    sgn = -1.0 if direction > 0 else 1.0
-    for s in range(steps):
-        t = s * dt
-        Bt += 0.5 * dt * (np.roll(E, -1) - E) / da
-        Bt[bidx] += sgn * 0.5 * dt / da * incident(P, t, P, direction, da, c, fwhm, tc)
-        E += c * c * dt * (Bt - np.roll(Bt, 1)) / da
-        E[P] += c * dt / da * incident(P - 0.5 * direction, t + 0.5 * dt, P, direction, da, c, fwhm, tc)
-        Bt += 0.5 * dt * (np.roll(E, -1) - E) / da
-        Bt[bidx] += sgn * 0.5 * dt / da * incident(P, t + dt, P, direction, da, c, fwhm, tc)
-    return E, Bt
-
-
-def line(F, comp, axis, u1, u2):
-    """Values of component comp along `axis` at transverse cells (u1, u2) (first, second
-    transverse axis in increasing order); F is [3][nz][ny][nx]."""
-    A = F[comp]
-    if axis == 0:
-        return A[u2, u1, :]
-    if axis == 1:
-        return A[u2, :, u1]
-    return A[:, u2, u1]
 
 
 @pytest.mark.parametrize("axis", [0, 1, 2])
@@ -87,7 +51,7 @@ def test_pulse_through_every_face(axis, direction, pol):
         E = sim.get_field("E")
         B = sim.get_field("B")
     E0 = 2 * math.pi / LAM
-    e1, b1 = yee_1d(LONG, P, direction, g, fwhm, tc, STEPS)
+    e1, b1 = yee_1d(LONG, P, direction, g, LAM, fwhm, tc, STEPS)
     t1, t2 = [d for d in range(3) if d != axis]
     p = t1 if pol == 0 else t2
     o = t2 if pol == 0 else t1
