@@ -42,6 +42,9 @@ namespace picgb
 #ifndef PICGB_J_PLANE_PAD
 #    define PICGB_J_PLANE_PAD 1
 #endif
+#ifndef PICGB_POOL_LEFTOVERS
+#    define PICGB_POOL_LEFTOVERS 1 // the warps' leftover deposit jobs drained together after the loop
+#endif
     static_assert(kQueueCap >= 32, "a warp drains 32 jobs at a time");
     constexpr int kJobWords = 9;
 
@@ -253,16 +256,15 @@ namespace picgb
 #else
     __device__ __forceinline__
 #endif
-        void drainQueue(int jOff, int qOff, int njobs, JFixed jf, float dx, float dy, float dz, float dt, float invVdt)
+        void drainQueue(int jOff, int qOff, int idx, bool active, JFixed jf, float dx, float dy, float dz, float dt, float invVdt)
     {
         extern __shared__ __align__(16) float smem[];
-        int const lane = threadIdx.x & 31;
-        if(lane >= njobs)
+        if(!active)
             return;
         WarpQueue const queue{smem + qOff};
         float q0[3], q1[3], qc;
         int qo, qs[3];
-        queue.get(lane, q0, q1, qc, qo, qs);
+        queue.get(idx, q0, q1, qc, qo, qs);
         GridParams g{};
         g.dx = dx;
         g.dy = dy;
@@ -533,7 +535,7 @@ namespace picgb
             if(queued >= 32)
             {
                 drainQueue<SH, TG::JX, TG::JP, TG::JT, EMZ>(
-                    int(Js - smem), qOff, 32, pp.jf, g.dx, g.dy, g.dz, g.dt, pp.invVdt);
+                    int(Js - smem), qOff, lane, true, pp.jf, g.dx, g.dy, g.dz, g.dt, pp.invVdt);
                 __syncwarp();
                 if(lane < queued - 32)
                     queue.move(32 + lane, lane);
@@ -548,10 +550,40 @@ namespace picgb
                 __syncwarp();
             }
         }
-        // the jobs still queued
+        // The jobs still queued (fewer than 32 per warp), pooled over the block: job p of the
+        // pool is job p - (jobs of the warps before) of its warp's queue, and warp w drains pool
+        // jobs 32 w .. 32 w + 31.  A warp draining only its own few leftovers would run the whole
+        // general footprint for a handful of lanes.
+#if !PICGB_POOL_LEFTOVERS
         if(pp.deposit && queued > 0)
             drainQueue<SH, TG::JX, TG::JP, TG::JT, EMZ>(
-                int(Js - smem), qOff, queued, pp.jf, g.dx, g.dy, g.dz, g.dt, pp.invVdt);
+                int(Js - smem), qOff, lane, lane < queued, pp.jf, g.dx, g.dy, g.dz, g.dt, pp.invVdt);
+#else
+        if(pp.deposit)
+        {
+            __shared__ int s_left[THREADS / 32];
+            if(lane == 0)
+                s_left[warp] = queued;
+            __syncthreads(); // every warp's queue is complete
+            int const p = warp * 32 + lane;
+            int total = 0, owner = 0, idx = 0;
+#pragma unroll
+            for(int q = 0; q < THREADS / 32; ++q)
+            {
+                int const c = s_left[q];
+                if(p >= total && p < total + c)
+                {
+                    owner = q;
+                    idx = p - total;
+                }
+                total += c;
+            }
+            if(warp * 32 < total)
+                drainQueue<SH, TG::JX, TG::JP, TG::JT, EMZ>(int(Js - smem),
+                    6 * TG::GT + TG::JWords + owner * kQueueCap * kJobWords, idx, p < total, pp.jf, g.dx, g.dy, g.dz,
+                    g.dt, pp.invVdt);
+        }
+#endif
         __syncthreads(); // every hole is recorded and every deposit done
         if(threadIdx.x == 0)
             sp.nhole[sc] = s_nhole;
