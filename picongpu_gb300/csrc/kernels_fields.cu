@@ -50,6 +50,138 @@ namespace picgb
             yeeBHalfAt(E, B, g, x, blockIdx.y, blockIdx.z);
     }
 
+    // ---- vectorised Yee updates: four cells along x per thread
+    // With nx a multiple of 4 every row and every component plane starts on a 16-byte
+    // boundary, so the four cells' values of a component are one 128-bit load or store; the
+    // neighbour beyond the four cells along x is one scalar load.  The arithmetic per cell is
+    // that of yeeBHalfAt / yeeEAt.  A grid-stride loop over the (nx/4) ny nz quads.
+    constexpr int kYeeVecThreads = 256;
+
+    __device__ __forceinline__ float4 ld4(float const* p) { return __ldg(reinterpret_cast<float4 const*>(p)); }
+    __device__ __forceinline__ float at4(float4 const& v, int m) { return m == 0 ? v.x : (m == 1 ? v.y : (m == 2 ? v.z : v.w)); }
+    __device__ __forceinline__ void set4(float4& v, int m, float a)
+    {
+        if(m == 0)
+            v.x = a;
+        else if(m == 1)
+            v.y = a;
+        else if(m == 2)
+            v.z = a;
+        else
+            v.w = a;
+    }
+
+    __global__ void __launch_bounds__(kYeeVecThreads) kYeeBHalf4(float const* __restrict__ E, float* __restrict__ B, GridParams g)
+    {
+        int const nq = g.nx >> 2;
+        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+        size_t const quads = size_t(nq) * g.ny * g.nz;
+        float const* Ex = E;
+        float const* Ey = E + nc;
+        float const* Ez = E + 2 * nc;
+        for(size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < quads; t += size_t(gridDim.x) * blockDim.x)
+        {
+            size_t const r = t / nq; // row y + ny z
+            int const x = int(t - r * nq) * 4;
+            int const y = int(r % g.ny), z = int(r / g.ny);
+            size_t const i = r * g.nx + x;
+            size_t const iy = (size_t(y + 1 == g.ny ? 0 : y + 1) + size_t(g.ny) * z) * g.nx + x;
+            size_t const iz = (size_t(y) + size_t(g.ny) * (z + 1 == g.nz ? 0 : z + 1)) * g.nx + x;
+            size_t const ix4 = r * g.nx + (x + 4 == g.nx ? 0 : x + 4); // the cell after the four
+            float4 const ex = ld4(Ex + i), ey = ld4(Ey + i), ez = ld4(Ez + i);
+            float const eyN = __ldg(Ey + ix4), ezN = __ldg(Ez + ix4);
+            float4 const exY = ld4(Ex + iy), ezY = ld4(Ez + iy), exZ = ld4(Ex + iz), eyZ = ld4(Ey + iz);
+            float4 b0 = *reinterpret_cast<float4 const*>(B + i);
+            float4 b1 = *reinterpret_cast<float4 const*>(B + nc + i);
+            float4 b2 = *reinterpret_cast<float4 const*>(B + 2 * nc + i);
+#pragma unroll
+            for(int m = 0; m < 4; ++m)
+            {
+                float const cx = at4(ex, m), cy = at4(ey, m), cz = at4(ez, m);
+                float const dFdx_y = divCell(fs(m < 3 ? at4(ey, m + 1) : eyN, cy), 0, g);
+                float const dFdx_z = divCell(fs(m < 3 ? at4(ez, m + 1) : ezN, cz), 0, g);
+                float const dFdy_x = divCell(fs(at4(exY, m), cx), 1, g);
+                float const dFdy_z = divCell(fs(at4(ezY, m), cz), 1, g);
+                float const dFdz_x = divCell(fs(at4(exZ, m), cx), 2, g);
+                float const dFdz_y = divCell(fs(at4(eyZ, m), cy), 2, g);
+                float const c0 = fs(dFdy_z, dFdz_y), c1 = fs(dFdz_x, dFdx_z), c2 = fs(dFdx_y, dFdy_x);
+                set4(b0, m, fs(at4(b0, m), fm(fm(c0, 0.5f), g.dt)));
+                set4(b1, m, fs(at4(b1, m), fm(fm(c1, 0.5f), g.dt)));
+                set4(b2, m, fs(at4(b2, m), fm(fm(c2, 0.5f), g.dt)));
+            }
+            *reinterpret_cast<float4*>(B + i) = b0;
+            *reinterpret_cast<float4*>(B + nc + i) = b1;
+            *reinterpret_cast<float4*>(B + 2 * nc + i) = b2;
+        }
+    }
+
+    __global__ void __launch_bounds__(kYeeVecThreads)
+        kYeeE4(float const* __restrict__ B, float* __restrict__ E, float const* __restrict__ J, float coeff, GridParams g)
+    {
+        int const nq = g.nx >> 2;
+        size_t const nc = size_t(g.nx) * g.ny * g.nz;
+        size_t const quads = size_t(nq) * g.ny * g.nz;
+        float const* Bx = B;
+        float const* By = B + nc;
+        float const* Bz = B + 2 * nc;
+        float const c2 = fm(g.c, g.c);
+        for(size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < quads; t += size_t(gridDim.x) * blockDim.x)
+        {
+            size_t const r = t / nq;
+            int const x = int(t - r * nq) * 4;
+            int const y = int(r % g.ny), z = int(r / g.ny);
+            size_t const i = r * g.nx + x;
+            size_t const iy = (size_t(y == 0 ? g.ny - 1 : y - 1) + size_t(g.ny) * z) * g.nx + x;
+            size_t const iz = (size_t(y) + size_t(g.ny) * (z == 0 ? g.nz - 1 : z - 1)) * g.nx + x;
+            size_t const ixP = r * g.nx + (x == 0 ? g.nx - 1 : x - 1); // the cell before the four
+            float4 const bx = ld4(Bx + i), by = ld4(By + i), bz = ld4(Bz + i);
+            float const byP = __ldg(By + ixP), bzP = __ldg(Bz + ixP);
+            float4 const bxY = ld4(Bx + iy), bzY = ld4(Bz + iy), bxZ = ld4(Bx + iz), byZ = ld4(By + iz);
+            float4 e[3] = {*reinterpret_cast<float4 const*>(E + i), *reinterpret_cast<float4 const*>(E + nc + i),
+                           *reinterpret_cast<float4 const*>(E + 2 * nc + i)};
+            float4 j[3];
+            if(J)
+            {
+                j[0] = ld4(J + i);
+                j[1] = ld4(J + nc + i);
+                j[2] = ld4(J + 2 * nc + i);
+            }
+#pragma unroll
+            for(int m = 0; m < 4; ++m)
+            {
+                float const cx = at4(bx, m), cy = at4(by, m), cz = at4(bz, m);
+                float const dFdx_y = divCell(fs(cy, m > 0 ? at4(by, m - 1) : byP), 0, g);
+                float const dFdx_z = divCell(fs(cz, m > 0 ? at4(bz, m - 1) : bzP), 0, g);
+                float const dFdy_x = divCell(fs(cx, at4(bxY, m)), 1, g);
+                float const dFdy_z = divCell(fs(cz, at4(bzY, m)), 1, g);
+                float const dFdz_x = divCell(fs(cx, at4(bxZ, m)), 2, g);
+                float const dFdz_y = divCell(fs(cy, at4(byZ, m)), 2, g);
+                float const cu[3] = {fs(dFdy_z, dFdz_y), fs(dFdz_x, dFdx_z), fs(dFdx_y, dFdy_x)};
+#pragma unroll
+                for(int d = 0; d < 3; ++d)
+                {
+                    float v = fa(at4(e[d], m), fm(fm(cu[d], c2), g.dt));
+                    if(J)
+                        v = fa(v, fm(coeff, at4(j[d], m)));
+                    set4(e[d], m, v);
+                }
+            }
+#pragma unroll
+            for(int d = 0; d < 3; ++d)
+                *reinterpret_cast<float4*>(E + d * nc + i) = e[d];
+        }
+    }
+
+    int yeeVecBlocks(GridParams const& g)
+    {
+        size_t const quads = size_t(g.nx >> 2) * g.ny * g.nz;
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        size_t const cap = size_t(sms > 0 ? sms : 152) * 8; // 8 blocks of 256 threads per SM
+        return int(std::min<size_t>((quads + kYeeVecThreads - 1) / kYeeVecThreads, cap));
+    }
+
     // E += curl(B) * c^2 * dt with backward differences at cell (x, y, z) (FDTDBase.kernel:51-81
     // UpdateEFunctor, BackwardDerivative.hpp:45-63); optionally followed by E += coeff * J
     // (currentInterpolation/None.hpp:60-65) as a separate rounding step.
@@ -296,6 +428,11 @@ namespace picgb
 
     cudaError_t launchYeeBHalf(float const* E, float* B, GridParams const& g, cudaStream_t stream)
     {
+        if(g.nx % 4 == 0)
+        {
+            kYeeBHalf4<<<yeeVecBlocks(g), kYeeVecThreads, 0, stream>>>(E, B, g);
+            return cudaGetLastError();
+        }
         dim3 grid((g.nx + kFieldBX - 1) / kFieldBX, g.ny, g.nz);
         kYeeBHalf<<<grid, kFieldBX, 0, stream>>>(E, B, g);
         return cudaGetLastError();
@@ -303,6 +440,11 @@ namespace picgb
 
     cudaError_t launchYeeE(float const* B, float* E, float const* J, float coeff, GridParams const& g, cudaStream_t stream)
     {
+        if(g.nx % 4 == 0)
+        {
+            kYeeE4<<<yeeVecBlocks(g), kYeeVecThreads, 0, stream>>>(B, E, J, coeff, g);
+            return cudaGetLastError();
+        }
         dim3 grid((g.nx + kFieldBX - 1) / kFieldBX, g.ny, g.nz);
         kYeeE<<<grid, kFieldBX, 0, stream>>>(B, E, J, coeff, g);
         return cudaGetLastError();
