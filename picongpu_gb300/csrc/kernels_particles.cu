@@ -180,58 +180,6 @@ namespace picgb
         return cudaErrorInvalidValue;
     }
 
-    // ------------------------------------------------------------ block scan
-    // In-place exclusive scan of n <= 32 * 32 * items entries in shared memory by
-    // one block of blockDim.x (multiple of 32, <= 1024) threads; returns the total.
-    __device__ uint32_t blockExclusiveScan(uint32_t* a, int n, uint32_t* warpSums)
-    {
-        int const T = blockDim.x;
-        int const per = (n + T - 1) / T;
-        int const b = threadIdx.x * per;
-        int const e = min(n, b + per);
-        uint32_t local = 0;
-        for(int i = b; i < e; ++i)
-            local += a[i];
-        // inclusive warp scan of the per-thread totals
-        uint32_t v = local;
-        int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-        for(int o = 1; o < 32; o <<= 1)
-        {
-            uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
-            if(lane >= o)
-                v += t;
-        }
-        if(lane == 31)
-            warpSums[warp] = v;
-        __syncthreads();
-        if(warp == 0)
-        {
-            int const nw = T >> 5;
-            uint32_t s = lane < nw ? warpSums[lane] : 0u;
-#pragma unroll
-            for(int o = 1; o < 32; o <<= 1)
-            {
-                uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
-                if(lane >= o)
-                    s += t;
-            }
-            if(lane < nw)
-                warpSums[lane] = s;
-        }
-        __syncthreads();
-        uint32_t offset = (v - local) + (warp > 0 ? warpSums[warp - 1] : 0u);
-        uint32_t const total = warpSums[(T >> 5) - 1];
-        for(int i = b; i < e; ++i)
-        {
-            uint32_t const x = a[i];
-            a[i] = offset;
-            offset += x;
-        }
-        __syncthreads();
-        return total;
-    }
-
     __device__ __forceinline__ uint32_t maskBelow(int w, uint32_t limit)
     {
         // bits j of word w with 32 * w + j < limit
@@ -257,17 +205,23 @@ namespace picgb
             sp.id[dst] = sp.id[src];
     }
 
-    // Fill the slots vacated by leaving particles with the last valid particles
-    // of supercell `sc` so that slots [0, count) are dense again.  One block;
-    // `csm` holds 3 * ceil(cap / 32) words.
-    __device__ __forceinline__ void compactSupercell(SpeciesDev const& sp, int const sc, uint32_t* csm, uint32_t* warpSums)
+    // Fill the slots vacated by leaving particles with the last valid particles of supercell
+    // `sc` so that slots [0, count) are dense again.  One warp per supercell (a supercell loses a
+    // few percent of its particles per step, so a block per supercell spent its time in barriers):
+    // a bitmap of the holes, per 32-slot word the number of holes below the new count
+    // (destinations) and of particles at or above it (sources), their exclusive prefix sums by
+    // warp scans, and the r-th destination takes the r-th source.  Destinations and sources are
+    // disjoint slots, so the lanes' copies never conflict.  `csm` holds 3 * ceil(cap / 32) words
+    // for this warp.
+    __device__ __forceinline__ void compactSupercell(SpeciesDev const& sp, int const sc, uint32_t* csm)
     {
+        int const lane = threadIdx.x & 31;
         uint32_t const tail = sp.tail[sc];
         uint32_t const n = tail < sp.cap ? tail : sp.cap;
         uint32_t const h = sp.nhole[sc];
         if(h == 0)
         {
-            if(threadIdx.x == 0)
+            if(lane == 0)
             {
                 sp.count[sc] = n;
                 sp.tail[sc] = n;
@@ -279,27 +233,50 @@ namespace picgb
         uint32_t* bm = csm;
         uint32_t* dpre = csm + W;
         uint32_t* spre = csm + 2 * W;
-        for(int i = threadIdx.x; i < W; i += blockDim.x)
+        for(int i = lane; i < W; i += 32)
             bm[i] = 0u;
-        __syncthreads();
+        __syncwarp();
         size_t const base = size_t(sc) * sp.cap;
-        for(uint32_t i = threadIdx.x; i < h; i += blockDim.x)
+        for(uint32_t i = lane; i < h; i += 32)
         {
             uint32_t const s = sp.holes[base + i];
             atomicOr(bm + (s >> 5), 1u << (s & 31));
         }
-        __syncthreads();
-        for(int w = threadIdx.x; w < W; w += blockDim.x)
+        __syncwarp();
+        uint32_t carryD = 0, carryS = 0;
+        for(int w0 = 0; w0 < W; w0 += 32)
         {
-            uint32_t const lo = maskBelow(w, newc);
-            uint32_t const hi = maskBelow(w, n) & ~lo;
-            dpre[w] = __popc(bm[w] & lo);
-            spre[w] = __popc(~bm[w] & hi);
+            int const w = w0 + lane;
+            uint32_t d = 0, c = 0;
+            if(w < W)
+            {
+                uint32_t const lo = maskBelow(w, newc);
+                uint32_t const hi = maskBelow(w, n) & ~lo;
+                d = __popc(bm[w] & lo);
+                c = __popc(~bm[w] & hi);
+            }
+            uint32_t id = d, ic = c; // inclusive warp scans
+#pragma unroll
+            for(int o = 1; o < 32; o <<= 1)
+            {
+                uint32_t const vd = __shfl_up_sync(0xffffffffu, id, o);
+                uint32_t const vc = __shfl_up_sync(0xffffffffu, ic, o);
+                if(lane >= o)
+                {
+                    id += vd;
+                    ic += vc;
+                }
+            }
+            if(w < W)
+            {
+                dpre[w] = carryD + id - d;
+                spre[w] = carryS + ic - c;
+            }
+            carryD += __shfl_sync(0xffffffffu, id, 31);
+            carryS += __shfl_sync(0xffffffffu, ic, 31);
         }
-        __syncthreads();
-        blockExclusiveScan(dpre, W, warpSums);
-        blockExclusiveScan(spre, W, warpSums);
-        for(int w = threadIdx.x; w < W; w += blockDim.x)
+        __syncwarp();
+        for(int w = lane; w < W; w += 32)
         {
             uint32_t m = bm[w] & maskBelow(w, newc);
             uint32_t r = dpre[w];
@@ -328,8 +305,8 @@ namespace picgb
                 ++r;
             }
         }
-        __syncthreads();
-        if(threadIdx.x == 0)
+        __syncwarp();
+        if(lane == 0)
         {
             sp.count[sc] = newc;
             sp.tail[sc] = newc;
@@ -337,22 +314,36 @@ namespace picgb
         }
     }
 
-    __global__ void __launch_bounds__(256) kCompact(SpeciesDev sp)
+    // Warps per block of the compaction: eight, fewer when a warp's 3 ceil(cap / 32) words of
+    // shared memory would take more than 48 KB for the block.
+    int compactWarps(uint32_t cap)
     {
-        extern __shared__ uint32_t csm[];
-        __shared__ uint32_t warpSums[32];
-        compactSupercell(sp, blockIdx.x, csm, warpSums);
+        size_t const perWarp = sizeof(uint32_t) * 3 * ((cap + 31) / 32);
+        size_t const w = (48 * 1024) / (perWarp ? perWarp : 1);
+        return int(w < 1 ? 1 : (w > 8 ? 8 : w));
     }
 
-    // Compaction over the supercells of every box of an ensemble: block b
-    // handles work item b (box, supercell).
-    __global__ void __launch_bounds__(256)
-        kCompactBatch(BatchSpecies const* __restrict__ boxes, uint32_t const* __restrict__ items)
+    __global__ void __launch_bounds__(256) kCompact(SpeciesDev sp, int nsc, int words)
     {
         extern __shared__ uint32_t csm[];
-        __shared__ uint32_t warpSums[32];
-        uint32_t const it = items[blockIdx.x];
-        compactSupercell(boxes[batchBox(it)].sp, int(batchSc(it)), csm, warpSums);
+        int const warp = threadIdx.x >> 5;
+        int const sc = blockIdx.x * (blockDim.x >> 5) + warp;
+        if(sc < nsc)
+            compactSupercell(sp, sc, csm + warp * 3 * words);
+    }
+
+    // Compaction over the supercells of every box of an ensemble: warp k of block b handles
+    // work item b * (warps per block) + k (box, supercell).
+    __global__ void __launch_bounds__(256)
+        kCompactBatch(BatchSpecies const* __restrict__ boxes, uint32_t const* __restrict__ items, uint32_t nitems, int words)
+    {
+        extern __shared__ uint32_t csm[];
+        int const warp = threadIdx.x >> 5;
+        uint32_t const k = blockIdx.x * (blockDim.x >> 5) + warp;
+        if(k >= nitems)
+            return;
+        uint32_t const it = items[k];
+        compactSupercell(boxes[batchBox(it)].sp, int(batchSc(it)), csm + warp * 3 * words);
     }
 
     cudaError_t launchCompactBatch(
@@ -364,14 +355,16 @@ namespace picgb
     {
         if(nitems == 0)
             return cudaSuccess;
-        size_t const smem = sizeof(uint32_t) * 3 * ((maxCap + 31) / 32);
+        int const warps = compactWarps(maxCap);
+        int const words = int((maxCap + 31) / 32);
+        size_t const smem = sizeof(uint32_t) * 3 * size_t(words) * warps;
         if(smem > 48 * 1024)
         {
             cudaError_t e = cudaFuncSetAttribute(kCompactBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if(e != cudaSuccess)
                 return e;
         }
-        kCompactBatch<<<nitems, 256, smem, stream>>>(boxes, items);
+        kCompactBatch<<<(nitems + warps - 1) / warps, 32 * warps, smem, stream>>>(boxes, items, nitems, words);
         return cudaGetLastError();
     }
 
@@ -593,14 +586,16 @@ namespace picgb
 
     cudaError_t launchCompact(SpeciesDev const& sp, int nsc, cudaStream_t stream)
     {
-        size_t const smem = sizeof(uint32_t) * 3 * ((sp.cap + 31) / 32);
+        int const warps = compactWarps(sp.cap);
+        int const words = int((sp.cap + 31) / 32);
+        size_t const smem = sizeof(uint32_t) * 3 * size_t(words) * warps;
         if(smem > 48 * 1024)
         {
             cudaError_t e = cudaFuncSetAttribute(kCompact, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if(e != cudaSuccess)
                 return e;
         }
-        kCompact<<<nsc, 256, smem, stream>>>(sp);
+        kCompact<<<(nsc + warps - 1) / warps, 32 * warps, smem, stream>>>(sp, nsc, words);
         return cudaGetLastError();
     }
 
