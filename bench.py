@@ -301,8 +301,13 @@ def run_e2e(args, wl, sim, pg, torch, local_rank, world):
         p = sim.get_particles(name)
         host[name], ts = pinned_like(torch, p)
         keep += ts
-    E0 = sim.get_field("E")
-    B0 = sim.get_field("B")
+    # the fields from page-locked host memory too
+    E0t = torch.empty(sim._field_shape("E"), dtype=torch.float32, pin_memory=True)
+    B0t = torch.empty(sim._field_shape("B"), dtype=torch.float32, pin_memory=True)
+    E0, B0 = E0t.numpy(), B0t.numpy()
+    E0[...] = sim.get_field("E")
+    B0[...] = sim.get_field("B")
+    keep += [E0t, B0t]
     sim2 = build_sim(pg, wl, local_rank)
     npart = sum(host[n]["w"].size for n in host)
     h2d = sum(a.nbytes for n in host for a in host[n].values()) + E0.nbytes + B0.nbytes

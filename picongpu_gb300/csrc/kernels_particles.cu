@@ -777,22 +777,36 @@ namespace picgb
         float* a[7];
     };
 
+    // Output-major gather of a species into the host exchange format: output d belongs to the
+    // last supercell whose offset is at most d (empty supercells share the offset of the next),
+    // and is its slot d - offset.  Consecutive threads write consecutive outputs, so a warp's
+    // stores to each array are whole aligned 128-byte lines even when the supercells' counts put
+    // their ranges at arbitrary offsets (a supercell-major loop straddled lines, which costs
+    // about a third of the host link's bandwidth when the arrays are host memory written over
+    // the link); the reads stay contiguous within a supercell.
     __global__ void kGatherOut(
         SpeciesDev sp,
         uint64_t const* __restrict__ offsets,
+        int nsc,
+        uint64_t total,
         OutAttr out,
         int32_t* __restrict__ osc,
         uint16_t* __restrict__ olc,
         uint32_t* __restrict__ oid)
     {
-        int const sc = blockIdx.x;
-        uint32_t const n = sp.count[sc];
-        size_t const base = size_t(sc) * sp.cap;
-        uint64_t const o = offsets[sc];
-        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        for(uint64_t d = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; d < total; d += uint64_t(gridDim.x) * blockDim.x)
         {
-            size_t const s = base + k;
-            uint64_t const d = o + k;
+            int lo = 0, hi = nsc - 1;
+            while(lo < hi)
+            {
+                int const mid = (lo + hi + 1) >> 1;
+                if(__ldg(offsets + mid) <= d)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            int const sc = lo;
+            size_t const s = size_t(sc) * sp.cap + size_t(d - __ldg(offsets + sc));
             out.a[0][d] = sp.px[s];
             out.a[1][d] = sp.py[s];
             out.a[2][d] = sp.pz[s];
@@ -811,16 +825,23 @@ namespace picgb
         SpeciesDev const& sp,
         int nsc,
         uint64_t const* offsets,
+        uint64_t total,
         float* const* attr,
         int32_t* sc,
         uint16_t* lcell,
         uint32_t* id,
         cudaStream_t stream)
     {
+        if(total == 0)
+            return cudaSuccess;
         OutAttr o;
         for(int i = 0; i < 7; ++i)
             o.a[i] = attr[i];
-        kGatherOut<<<nsc, 256, 0, stream>>>(sp, offsets, o, sc, lcell, id);
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        uint64_t const blocks = std::min<uint64_t>((total + 255) / 256, uint64_t(sms > 0 ? sms : 152) * 16);
+        kGatherOut<<<unsigned(blocks), 256, 0, stream>>>(sp, offsets, nsc, total, o, sc, lcell, id);
         return cudaGetLastError();
     }
 

@@ -369,7 +369,7 @@ namespace picgb::host
         uint64_t* doff = nullptr;
         CUDA_TRY(dalloc(doff, size_t(s->nsc)));
         CUDA_TRY(cudaMemcpyAsync(doff, off.data(), sizeof(uint64_t) * s->nsc, cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, st.a, st.sc, st.lcell, st.id, s->stream));
+        CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, total, st.a, st.sc, st.lcell, st.id, s->stream));
         ++s->launches;
         size_t const C = sp.dev.spill_cap;
         for(int k = 0; k < 7; ++k)
@@ -863,14 +863,14 @@ extern "C"
         zeroCopy = zeroCopy && dsc && dlc && (!h->id || did);
         if(zeroCopy)
         {
-            CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, direct, dsc, dlc, did, s->stream));
+            CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, total, direct, dsc, dlc, did, s->stream));
             ++s->launches;
         }
         else
         {
             Staging st;
             CUDA_TRY(st.alloc(s, total, h->id != nullptr));
-            CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, st.a, st.sc, st.lcell, st.id, s->stream));
+            CUDA_TRY(launchGatherOut(sp.dev, s->nsc, doff, total, st.a, st.sc, st.lcell, st.id, s->stream));
             ++s->launches;
             for(int k = 0; k < 7; ++k)
                 CUDA_TRY(cudaMemcpyAsync(dst[k], st.a[k], sizeof(float) * total, cudaMemcpyDeviceToHost, s->stream));

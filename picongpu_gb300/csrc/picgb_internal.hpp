@@ -171,10 +171,12 @@ namespace picgb
         SpeciesDev const& sp,
         unsigned* status,
         cudaStream_t stream);
+    // offsets[sc]: first output of supercell sc (a prefix of its counts); total: the sum
     cudaError_t launchGatherOut(
         SpeciesDev const& sp,
         int nsc,
         uint64_t const* offsets,
+        uint64_t total,
         float* const* attr,
         int32_t* sc,
         uint16_t* lcell,
