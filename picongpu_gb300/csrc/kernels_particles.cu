@@ -880,28 +880,46 @@ namespace picgb
         // the rounding error of every addition is collected in `comp`), as the reference sums
         // per thread in float_X; FP64 from the thread sums on.  An FP64 add per particle runs
         // on this GPU's narrow FP64 pipe.
+        // The loads of kBatch particles are issued before their arithmetic, so a thread waits
+        // for memory once per batch; the particles are summed in the same order as one at a time.
+        constexpr int kBatch = 8;
         float sum = 0.0f, comp = 0.0f;
-        for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        for(uint32_t k0 = threadIdx.x; k0 < n; k0 += kBatch * blockDim.x)
         {
-            size_t const s = base + k;
-            float const m = fm(mass0, sp.w[s]);
-            float const ux = sp.ux[s], uy = sp.uy[s], uz = sp.uz[s];
-            float const mom2 = l2n2(ux, uy, uz);
-            float e;
-            if(m == 0.0f)
-                e = fm(c, fsq(mom2));
-            else
+            float wv[kBatch], uxv[kBatch], uyv[kBatch], uzv[kBatch];
+#pragma unroll
+            for(int b = 0; b < kBatch; ++b)
             {
-                float const r = fdv(1.0f, fm(fm(m, m), c2));
-                float const gamma = fsq(fa(1.0f, fm(mom2, r)));
-                if(gamma < 1.005f)
-                    e = fdv(mom2, fm(2.0f, m));
-                else
-                    e = fm(fm(fs(gamma, 1.0f), m), c2);
+                uint32_t const k = k0 + b * blockDim.x;
+                size_t const s = base + (k < n ? k : 0u);
+                wv[b] = sp.w[s];
+                uxv[b] = sp.ux[s];
+                uyv[b] = sp.uy[s];
+                uzv[b] = sp.uz[s];
             }
-            float const t = fa(sum, e);
-            comp = fa(comp, fabsf(sum) >= fabsf(e) ? fa(fs(sum, t), e) : fa(fs(e, t), sum));
-            sum = t;
+#pragma unroll
+            for(int b = 0; b < kBatch; ++b)
+            {
+                if(k0 + b * blockDim.x >= n)
+                    break;
+                float const m = fm(mass0, wv[b]);
+                float const mom2 = l2n2(uxv[b], uyv[b], uzv[b]);
+                float e;
+                if(m == 0.0f)
+                    e = fm(c, fsq(mom2));
+                else
+                {
+                    float const r = fdv(1.0f, fm(fm(m, m), c2));
+                    float const gamma = fsq(fa(1.0f, fm(mom2, r)));
+                    if(gamma < 1.005f)
+                        e = fdv(mom2, fm(2.0f, m));
+                    else
+                        e = fm(fm(fs(gamma, 1.0f), m), c2);
+                }
+                float const t = fa(sum, e);
+                comp = fa(comp, fabsf(sum) >= fabsf(e) ? fa(fs(sum, t), e) : fa(fs(e, t), sum));
+                sum = t;
+            }
         }
         double const s = blockSumD(double(sum) + double(comp));
         if(threadIdx.x == 0 && s != 0.0)
