@@ -320,8 +320,12 @@ def run_e2e(args, wl, sim, pg, torch, local_rank, world):
     t0 = time.perf_counter()
     sim2.set_field("E", E0)
     sim2.set_field("B", B0)
+    t_fields = time.perf_counter()
+    t_sp = {}
     for name in ("e", "i"):
+        ts0 = time.perf_counter()
         sim2.set_particles(name, host[name])
+        t_sp[name] = round(time.perf_counter() - ts0, 4)
     t_up = time.perf_counter()
     for _ in range(args.steps):
         sim2.step()
@@ -344,7 +348,8 @@ def run_e2e(args, wl, sim, pg, torch, local_rank, world):
             "timed": "uploads of both species and E, B from pinned memory, the steps with an FP64 energy read-back "
                      "after each, downloads of both species into pinned memory; the particle storage was allocated "
                      "by one untimed upload before",
-            "phases_s": {"upload": round(t_up - t0, 4), "steps_with_energies": round(t_steps - t_up, 4),
+            "phases_s": {"upload": round(t_up - t0, 4), "upload_fields": round(t_fields - t0, 4),
+                         "upload_species": t_sp, "steps_with_energies": round(t_steps - t_up, 4),
                          "download": round(t1 - t_steps, 4)}}
 
 

@@ -777,6 +777,45 @@ namespace picgb
         float* a[7];
     };
 
+    // Host-to-device copy by the SMs: segment blockIdx.y, four 16-byte loads per thread and round
+    // in flight when both ends are 16-byte aligned (the rest byte by byte).
+    __global__ void __launch_bounds__(256) kCopyIn(CopyJobs jobs)
+    {
+        CopySeg const sg = jobs.s[blockIdx.y];
+        char* const d = static_cast<char*>(sg.dst);
+        char const* const src = static_cast<char const*>(sg.src);
+        bool const aligned = ((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0;
+        size_t const n16 = aligned ? sg.bytes / 16 : 0;
+        uint4* const d16 = reinterpret_cast<uint4*>(d);
+        uint4 const* const s16 = reinterpret_cast<uint4 const*>(src);
+        size_t const stride = size_t(gridDim.x) * blockDim.x;
+        size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        for(; i + 3 * stride < n16; i += 4 * stride)
+        {
+            uint4 const a = s16[i], b = s16[i + stride], c = s16[i + 2 * stride], e = s16[i + 3 * stride];
+            d16[i] = a;
+            d16[i + stride] = b;
+            d16[i + 2 * stride] = c;
+            d16[i + 3 * stride] = e;
+        }
+        for(; i < n16; i += stride)
+            d16[i] = s16[i];
+        for(size_t j = n16 * 16 + size_t(blockIdx.x) * blockDim.x + threadIdx.x; j < sg.bytes; j += stride)
+            d[j] = src[j];
+    }
+
+    cudaError_t launchCopyIn(CopyJobs const& jobs, cudaStream_t stream)
+    {
+        if(jobs.n <= 0)
+            return cudaSuccess;
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        dim3 const grid(unsigned((sms > 0 ? sms : 152) * 2), unsigned(jobs.n));
+        kCopyIn<<<grid, 256, 0, stream>>>(jobs);
+        return cudaGetLastError();
+    }
+
     // Output-major gather of a species into the host exchange format: output d belongs to the
     // last supercell whose offset is at most d (empty supercells share the offset of the next),
     // and is its slot d - offset.  Consecutive threads write consecutive outputs, so a warp's

@@ -689,12 +689,36 @@ extern "C"
         Staging st;
         CUDA_TRY(st.alloc(s, n, sp.cfg.with_ids != 0 && h->id));
         float const* src[7] = {h->pos[0], h->pos[1], h->pos[2], h->mom[0], h->mom[1], h->mom[2], h->w};
+        // page-locked host arrays are read by a copy kernel over the host link (SM loads, as the
+        // download writes); other host memory goes through cudaMemcpyAsync
+        CopyJobs jobs{};
+        bool zeroCopy = n > 0;
+        auto add = [&](void* dst, void const* hostSrc, size_t bytes)
+        {
+            void* const dv = deviceView(const_cast<void*>(hostSrc));
+            zeroCopy = zeroCopy && dv != nullptr;
+            jobs.s[jobs.n++] = CopySeg{dst, dv, bytes};
+        };
         for(int k = 0; k < 7; ++k)
-            CUDA_TRY(cudaMemcpyAsync(st.a[k], src[k], sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(cudaMemcpyAsync(st.sc, h->sc, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(cudaMemcpyAsync(st.lcell, h->lcell, sizeof(uint16_t) * n, cudaMemcpyHostToDevice, s->stream));
+            add(st.a[k], src[k], sizeof(float) * n);
+        add(st.sc, h->sc, sizeof(int32_t) * n);
+        add(st.lcell, h->lcell, sizeof(uint16_t) * n);
         if(st.id)
-            CUDA_TRY(cudaMemcpyAsync(st.id, h->id, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s->stream));
+            add(st.id, h->id, sizeof(uint32_t) * n);
+        if(zeroCopy)
+        {
+            CUDA_TRY(launchCopyIn(jobs, s->stream));
+            ++s->launches;
+        }
+        else
+        {
+            for(int k = 0; k < 7; ++k)
+                CUDA_TRY(cudaMemcpyAsync(st.a[k], src[k], sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(st.sc, h->sc, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(st.lcell, h->lcell, sizeof(uint16_t) * n, cudaMemcpyHostToDevice, s->stream));
+            if(st.id)
+                CUDA_TRY(cudaMemcpyAsync(st.id, h->id, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s->stream));
+        }
         // per-supercell counts, and in the last word the bits of the largest |w|
         uint32_t* hcount = nullptr;
         CUDA_TRY(dalloc(hcount, size_t(s->nsc) + 1));
@@ -749,6 +773,14 @@ extern "C"
         CUDA_TRY(launchScatter(n, attr, st.sc, st.lcell, st.id, sp.dev, s->status, s->stream));
         ++s->launches;
         CUDA_TRY(cudaMemcpyAsync(sp.dev.tail, sp.dev.count, sizeof(uint32_t) * s->nsc, cudaMemcpyDeviceToDevice, s->stream));
+        // the scatter's slots follow the arrival of its atomics: give the particles the interleaved
+        // cell order the push's tiles are laid out for, as the periodic reorder does
+        int const vol = s->sc[0] * s->sc[1] * s->sc[2];
+        if(s->sortInterval && sp.cfg.pusher != PICGB_PUSHER_NONE && reorderSmemBytes(vol, sp.dev.cap) <= 200 * 1024)
+        {
+            CUDA_TRY(launchReorder(sp.dev, s->nsc, vol, s->stream));
+            ++s->launches;
+        }
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         return PICGB_OK;
     }

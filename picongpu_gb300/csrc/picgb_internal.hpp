@@ -171,6 +171,21 @@ namespace picgb
         SpeciesDev const& sp,
         unsigned* status,
         cudaStream_t stream);
+    // Copy of up to kCopySegs host-mapped (page-locked) arrays into device memory by a kernel:
+    // the SMs read the host memory over the link, as the download's gather writes it.
+    constexpr int kCopySegs = 10;
+    struct CopySeg
+    {
+        void* dst;
+        void const* src;
+        size_t bytes;
+    };
+    struct CopyJobs
+    {
+        CopySeg s[kCopySegs];
+        int n;
+    };
+    cudaError_t launchCopyIn(CopyJobs const& jobs, cudaStream_t stream);
     // offsets[sc]: first output of supercell sc (a prefix of its counts); total: the sum
     cudaError_t launchGatherOut(
         SpeciesDev const& sp,
