@@ -271,9 +271,19 @@ extern "C"
      * PULSE_DURATION = tau, focus = the distance of FOCUS_POSITION beyond the Huygens surface (0:
      * on it), center_x/center_z = FOCUS_POSITION on the transverse axes.  Each of the six faces
      * holds its own pulse: setting a face replaces that face's pulse, enabled = 0 switches the face
-     * (axis, direction) off, and a NULL field switches every face off.  Propagation oblique to the
-     * face (the reference's DIRECTION_{X,Y,Z} off the axis), circular polarisation, Laguerre modes
-     * and TIME_DELAY are not supported. */
+     * (axis, direction) off, and a NULL field switches every face off.
+     * Oblique incidence: `propagation` (DIRECTION_{X,Y,Z}, unit, entering through the face) and
+     * `polarisation_vector` (POLARISATION_DIRECTION_{X,Y,Z}, unit, orthogonal to it) replace the
+     * face normal and the axis `polarisation`; the pulse is then evaluated in the reference's
+     * vector form: internal coordinates are the dot products of the offset from the origin with
+     * the direction, the polarisation and their cross product (Functors.hpp
+     * getInternalCoordinates); the origin is where the beam axis crosses the face's Huygens plane
+     * at the transverse centre (center_x, center_z), the focus lies `focus` face-axis cells along
+     * the direction from it, and v_ph solves the Yee dispersion relation along the direction,
+     * sum_a (sin(k d_a h_a / 2) / h_a)^2 = (sin(omega dt / 2) / (c dt))^2.  circular = 1 gives
+     * E = (p/sqrt 2) value(phase + pi/2) + (d x p / sqrt 2) value(phase)
+     * (GaussianPulseFunctorIncidentE::operator()).  Laguerre modes, pulse-front tilt and
+     * TIME_DELAY are not supported. */
     typedef struct picgb_incident_field
     {
         int32_t enabled;
@@ -283,6 +293,10 @@ extern "C"
         float a0, e_over_m, wavelength, waist, duration_fwhm, t_center, center_x, center_z, phase;
         float focus; /* distance of the focus beyond the Huygens surface along the propagation, in cells */
         int32_t direction; /* +1 (or 0): travels +axis from the low face; -1: travels -axis from the high face */
+        float propagation[3]; /* unit DIRECTION_{X,Y,Z}; all zero: the face normal (direction * e_axis) */
+        float polarisation_vector[3]; /* unit POLARISATION_DIRECTION_{X,Y,Z}, orthogonal to the propagation;
+                                          all zero: the transverse axis `polarisation` */
+        int32_t circular; /* 0: linear polarisation; 1: circular (PolarisationType::Circular) */
     } picgb_incident_field;
     int picgb_set_incident_field(picgb_sim* sim, const picgb_incident_field* field);
 

@@ -60,7 +60,8 @@ class OrcField(ctypes.Structure):
 
 class OrcIncidentFace(ctypes.Structure):
     _fields_ = [("axis", ctypes.c_int), ("dir", ctypes.c_int), ("surface", ctypes.c_int),
-                ("polv", ctypes.c_float * 3), ("focus", ctypes.c_float * 3),
+                ("dirv", ctypes.c_float * 3), ("polv", ctypes.c_float * 3), ("focus", ctypes.c_float * 3),
+                ("circular", ctypes.c_int),
                 ("amplitude", ctypes.c_float), ("wavelength", ctypes.c_float), ("w0", ctypes.c_float),
                 ("pulse_duration", ctypes.c_float), ("time_shift", ctypes.c_float), ("laser_phase", ctypes.c_float),
                 ("phase_velocity", ctypes.c_float)]
@@ -220,25 +221,36 @@ def set_threads(n: int) -> None:
 
 
 def incident_face(g, axis, direction, surface, polarisation, a0, wavelength, waist, pulse_duration, time_shift,
-                  laser_phase, focus_position, e_over_m=1.0):
+                  laser_phase, focus_position, e_over_m=1.0, propagation=None, polarisation_vector=None,
+                  circular=False):
     """One incident-field face in the reference's parameters (profiles/BaseParam.def,
-    GaussianPulse.def): the E polarisation is the unit vector along the transverse axis
-    `polarisation` (0: the first of the two other axes in increasing order, 1: the second),
-    focus_position is absolute (length units), pulse_duration the rms duration of the
-    intensity (PULSE_DURATION), time_shift = -PULSE_INIT * PULSE_DURATION / 2, and the phase
-    velocity follows from the Yee dispersion relation along the axis (calculatePhaseVelocity.hpp)."""
+    GaussianPulse.def): the propagation direction is `propagation` (DIRECTION_*) or the face
+    normal, the E polarisation `polarisation_vector` (POLARISATION_DIRECTION_*) or the unit vector
+    along the transverse axis `polarisation` (0: the first of the two other axes in increasing
+    order, 1: the second), focus_position is absolute (length units), pulse_duration the rms
+    duration of the intensity (PULSE_DURATION), time_shift = -PULSE_INIT * PULSE_DURATION / 2, and
+    the phase velocity solves the Yee dispersion relation along the direction
+    (calculatePhaseVelocity.hpp) by bisection."""
     import math
     f = OrcIncidentFace()
     f.axis, f.dir, f.surface = int(axis), int(direction), int(surface)
     t = [d for d in range(3) if d != axis]
-    f.polv[t[polarisation]] = 1.0
+    dv = list(propagation) if propagation is not None else [float(direction) if d == axis else 0.0 for d in range(3)]
+    pv = list(polarisation_vector) if polarisation_vector is not None else [1.0 if d == t[polarisation] else 0.0
+                                                                             for d in range(3)]
     for d in range(3):
-        f.focus[d] = float(focus_position[d])
+        f.dirv[d], f.polv[d], f.focus[d] = float(dv[d]), float(pv[d]), float(focus_position[d])
+    f.circular = int(bool(circular))
     c, dt = float(g["c"]), float(g["dt"])
-    d_a = float((g["dx"], g["dy"], g["dz"])[axis])
+    h = [float(g["dx"]), float(g["dy"]), float(g["dz"])]
     omega = 2 * math.pi * c / wavelength
-    k = 2.0 / d_a * math.asin(d_a / (c * dt) * math.sin(omega * dt / 2))
-    f.phase_velocity = omega / k
+    rhs = (math.sin(omega * dt / 2) / (c * dt)) ** 2
+    lhs = lambda k: sum((math.sin(k * dv[a] * h[a] / 2) / h[a]) ** 2 for a in range(3))
+    lo, hi = 0.0, math.pi / max(abs(dv[a]) * h[a] for a in range(3))
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        lo, hi = (mid, hi) if lhs(mid) < rhs else (lo, mid)
+    f.phase_velocity = omega / (0.5 * (lo + hi))
     f.amplitude = a0 * omega * c / e_over_m
     f.wavelength, f.w0, f.pulse_duration = wavelength, waist, pulse_duration
     f.time_shift, f.laser_phase = time_shift, laser_phase

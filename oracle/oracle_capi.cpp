@@ -43,7 +43,8 @@ extern "C"
     struct orc_incident_face
     {
         int axis, dir, surface;
-        float polv[3], focus[3];
+        float dirv[3], polv[3], focus[3];
+        int circular;
         float amplitude, wavelength, w0, pulse_duration, time_shift, laser_phase, phase_velocity;
     };
     // the FP64 instantiation's exchange format (reference gradients of the differentiable run)
@@ -164,9 +165,11 @@ extern "C"
         face.surface = f->surface;
         for(int d = 0; d < 3; ++d)
         {
+            face.dirv[d] = f->dirv[d];
             face.polv[d] = f->polv[d];
             face.focus[d] = f->focus[d];
         }
+        face.circular = f->circular;
         face.amplitude = f->amplitude;
         face.wavelength = f->wavelength;
         face.w0 = f->w0;

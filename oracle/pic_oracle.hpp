@@ -1213,9 +1213,11 @@ namespace orc
     // of a low face is POSITION + 1, the last of a high face POSITION - 1.
     struct IncidentFace
     {
-        int axis = 1, dir = 1; // propagation axis and direction (+1: low face, -1: high face)
+        int axis = 1, dir = 1; // face normal and side (+1: low face, -1: high face)
         int surface = 1; // first (dir +1) or last (dir -1) E plane of the total-field region
-        float polv[3] = {1.f, 0.f, 0.f}; // unit E polarisation, orthogonal to the axis
+        float dirv[3] = {0.f, 1.f, 0.f}; // unit propagation direction (DIRECTION_*), entering through the face
+        float polv[3] = {1.f, 0.f, 0.f}; // unit E polarisation, orthogonal to dirv
+        int circular = 0; // PolarisationType::Circular
         float focus[3] = {0.f, 0.f, 0.f}; // focus position (length units)
         float amplitude = 1.f; // E0
         float wavelength = 1.f, w0 = 1.f;
@@ -1232,19 +1234,22 @@ namespace orc
     inline void incidentFieldAt(Grid const& g, IncidentFace const& f, float const idx[3], float t, bool wantB, float out[3])
     {
         float const cell[3] = {g.dx, g.dy, g.dz};
-        float dirv[3] = {0.f, 0.f, 0.f};
-        dirv[f.axis] = float(f.dir);
-        // getOrigin: the focus moved along the direction onto the Huygens surface of the face
+        float const* dirv = f.dirv;
+        // getOrigin: the focus moved back along the direction onto the Huygens surface of the face
+        // (the reference takes the latest crossing of the box's planes; the face's own plane here)
         float const minPos = (float(f.surface - 1) + 0.75f) * cell[f.axis];
         float const maxPos = (float(f.surface + 1) - 0.75f) * cell[f.axis];
-        float origin[3] = {f.focus[0], f.focus[1], f.focus[2]};
+        float const originP = ((f.dir > 0 ? minPos : maxPos) - f.focus[f.axis]) / dirv[f.axis];
+        float origin[3];
+        for(int d = 0; d < 3; ++d)
+            origin[d] = f.focus[d] + originP * dirv[d];
         origin[f.axis] = f.dir > 0 ? minPos : maxPos;
         float shift[3];
         for(int d = 0; d < 3; ++d)
             shift[d] = idx[d] * cell[d] - origin[d];
         float const pos0 = dotf(shift, dirv);
         float const currentTime = t - pos0 / f.phaseVelocity;
-        float value = 0.f;
+        float value = 0.f, value1 = 0.f; // value1: with the phase shifted by pi/2 (circular)
         if(!(currentTime < 0.f)) // cut off before the pulse reaches this point
         {
             float const time = currentTime + f.timeShift;
@@ -1265,13 +1270,35 @@ namespace orc
             float const r2OverW2 = r2 / w / w;
             float const r = 0.5f * r2 * rInv;
             float const k = 2.f * 3.14159265358979323846f / f.wavelength;
-            float etrans = std::exp(-r2OverW2) * std::cos(k * focusPos - k * r + xi + phase);
             float const shiftedTime = time - r / g.c;
             float const exponent = shiftedTime / (2.f * f.pulseDuration);
+            float etrans = std::exp(-r2OverW2) * std::cos(k * focusPos - k * r + xi + phase);
             etrans *= std::exp(-exponent * exponent);
             value = f.amplitude * (f.w0 / w) * etrans;
+            if(f.circular)
+            {
+                float const phase1 = omega * (time - focusPos / g.c) + f.laserPhase + 1.57079633f;
+                float et1 = std::exp(-r2OverW2) * std::cos(k * focusPos - k * r + xi + phase1);
+                et1 *= std::exp(-exponent * exponent);
+                value1 = f.amplitude * (f.w0 / w) * et1;
+            }
         }
-        float E[3] = {f.polv[0] * value, f.polv[1] * value, f.polv[2] * value};
+        float E[3];
+        if(!f.circular)
+            for(int d = 0; d < 3; ++d)
+                E[d] = f.polv[d] * value;
+        else
+        {
+            // getCircularPolarizationVector1 = polarisation / sqrt(2), vector2 = direction x vector1
+            float v1[3], v2[3];
+            for(int d = 0; d < 3; ++d)
+                v1[d] = f.polv[d] / std::sqrt(2.f);
+            v2[0] = dirv[1] * v1[2] - dirv[2] * v1[1];
+            v2[1] = dirv[2] * v1[0] - dirv[0] * v1[2];
+            v2[2] = dirv[0] * v1[1] - dirv[1] * v1[0];
+            for(int d = 0; d < 3; ++d)
+                E[d] = v1[d] * value1 + v2[d] * value;
+        }
         if(!wantB)
         {
             for(int d = 0; d < 3; ++d)

@@ -72,7 +72,8 @@ class IncidentField(ctypes.Structure):
     _fields_ = [("enabled", c_int), ("axis", c_int), ("surface", c_int), ("polarisation", c_int), ("a0", c_float),
                 ("e_over_m", c_float), ("wavelength", c_float), ("waist", c_float), ("duration_fwhm", c_float),
                 ("t_center", c_float), ("center_x", c_float), ("center_z", c_float), ("phase", c_float),
-                ("focus", c_float), ("direction", c_int)]
+                ("focus", c_float), ("direction", c_int), ("propagation", c_float * 3),
+                ("polarisation_vector", c_float * 3), ("circular", c_int)]
 
 
 class EnsembleConfig(ctypes.Structure):

@@ -235,36 +235,51 @@ namespace picgb
     // ------------------------------------------------------------ incident field (TF/SF)
     __device__ __forceinline__ float pick3(float v0, float v1, float v2, int i) { return i == 0 ? v0 : (i == 1 ? v1 : v2); }
 
-    // Incident pulse value at (x, y, z) in cell units and time t: the focused Gaussian beam of
+    // Incident E at (x, y, z) in cell units and time t: the focused Gaussian beam of
     // profiles/GaussianPulse.hpp:206-290 in its fundamental mode, in the reference's order of
-    // operations.  The local time runs from the Huygens surface at the grid's phase velocity
-    // (Functors.hpp getCurrentTime) and the field is zero before it starts there; the waist
-    // w(z_f), the phase omega (time - z_f / c) + phase, the wavefront curvature, the Gouy phase,
-    // the cosine carrier, the envelope exp(-(t_s / 2 tau)^2) of the curvature-delayed time and
-    // the amplitude w0 / w follow GaussianPulse.hpp:214-290 and GaussianPulseEnvelope.
-    __device__ __forceinline__ float incidentValue(IncidentParams const& p, GridParams const& g, float x, float y, float z, float t)
+    // operations.  Internal coordinates are dot products of the offset from the origin with the
+    // propagation direction and the two polarisation axes (Functors.hpp getInternalCoordinates);
+    // the local time runs from the origin at the grid's phase velocity along the direction
+    // (getCurrentTime) and the field is zero before it starts there; the waist w(z_f), the phase
+    // omega (time - z_f / c) + phase, the wavefront curvature, the Gouy phase, the cosine carrier,
+    // the envelope exp(-(t_s / 2 tau)^2) of the curvature-delayed time and the amplitude w0 / w
+    // follow GaussianPulse.hpp:214-290; circular polarisation adds the carrier shifted by pi/2
+    // along the first vector (GaussianPulseFunctorIncidentE::operator()).
+    __device__ __forceinline__ void incidentE(IncidentParams const& p, GridParams const& g, float x, float y, float z, float t, float E[3])
     {
-        int const a = p.axis, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
-        float const da = pick3(g.dx, g.dy, g.dz, a);
-        float const dist = float(p.dir) * (pick3(x, y, z, a) - p.origin) * da; // beyond the Huygens surface
-        float const tcur = t - dist * p.invVph;
+        E[0] = E[1] = E[2] = 0.0f;
+        float const s0 = x * g.dx - p.o[0], s1 = y * g.dy - p.o[1], s2 = z * g.dz - p.o[2];
+        float const pos0 = s0 * p.d[0] + s1 * p.d[1] + s2 * p.d[2];
+        float const tcur = t - pos0 * p.invVph;
         if(tcur < 0.0f)
-            return 0.0f;
+            return;
         float const time = tcur - p.tc;
-        float const r1 = (pick3(x, y, z, t1) - p.c1) * pick3(g.dx, g.dy, g.dz, t1);
-        float const r2_ = (pick3(x, y, z, t2) - p.c2) * pick3(g.dx, g.dy, g.dz, t2);
-        float const r2 = r1 * r1 + r2_ * r2_;
-        float const fp = p.focusDist - dist; // distance to the focus along the propagation
+        float const a1 = s0 * p.pol[0] + s1 * p.pol[1] + s2 * p.pol[2];
+        float const a2 = s0 * p.pol2[0] + s1 * p.pol2[1] + s2 * p.pol2[2];
+        float const r2 = a1 * a1 + a2 * a2;
+        float const fp = p.focusDist - pos0; // distance to the focus along the propagation
         float const w = p.w0 * sqrtf(1.0f + (fp / p.zR) * (fp / p.zR));
         float const phase = p.omega * (time - fp / g.c) + p.phase;
         float const rInv = -fp / (p.zR * p.zR + fp * fp); // inverse radius of curvature
         float const xi = atanf(-fp / p.zR); // Gouy phase
         float const r2OverW2 = r2 / w / w;
         float const rc = 0.5f * r2 * rInv;
-        float et = expf(-r2OverW2) * cosf(p.k * fp - p.k * rc + xi + phase);
         float const e = (time - rc / g.c) / p.tau2;
-        et *= expf(-e * e);
-        return p.E0 * (p.w0 / w) * et;
+        float const gt = expf(-r2OverW2), ge = expf(-e * e), amp = p.E0 * (p.w0 / w);
+        // E0 (w0 / w) ((exp(-r^2/w^2) cos(...)) exp(-e^2)), the association of the reference
+        float const v2 = amp * ((gt * cosf(p.k * fp - p.k * rc + xi + phase)) * ge);
+        if(!p.circular)
+        {
+#pragma unroll
+            for(int c = 0; c < 3; ++c)
+                E[c] = p.pv1[c] * v2;
+            return;
+        }
+        float const phase1 = p.omega * (time - fp / g.c) + p.phase + 1.57079633f; // + pi/2
+        float const v1 = amp * ((gt * cosf(p.k * fp - p.k * rc + xi + phase1)) * ge);
+#pragma unroll
+        for(int c = 0; c < 3; ++c)
+            E[c] = p.pv1[c] * v1 + p.pv2[c] * v2;
     }
 
     // Cell (i, j, k) of a face node: `planeIdx` along the axis, (u1, u2) on the transverse axes.
@@ -275,55 +290,72 @@ namespace picgb
         k = a == 2 ? planeIdx : u2;
     }
 
-    // The incident E is polarised along axis p (first or second transverse axis); o is the other
-    // transverse axis; with (a, b, c) cyclic, dB_o/dt contains +dE_p/da when p = c and -dE_p/da
-    // when p = b.  After B -= dt/2 curl E the B plane on the scattered side of the surface
-    // (a-index plane - 1 for dir +1, plane for dir -1) used the total E_p of the E plane `plane`;
-    // removing its incident part adds sigma dt/2 E_p,inc / da to B_o, sigma = -dir (p = c) or
-    // +dir (p = b).  For a wave along +y: B_z -= dt/2 E_x,inc / dy, B_x += dt/2 E_z,inc / dy.
+    __constant__ float kYeePosE[3][3] = {{0.5f, 0.f, 0.f}, {0.f, 0.5f, 0.f}, {0.f, 0.f, 0.5f}};
+    __constant__ float kYeePosB[3][3] = {{0.f, 0.5f, 0.5f}, {0.5f, 0.f, 0.5f}, {0.5f, 0.5f, 0.f}};
+
+    // The incident field of component c at the Yee position of that component in cell (i, j, k)
+    // shifted by `shift` cells along the face axis: E (wantB false) or B = d x E / c.
+    __device__ __forceinline__ float incidentComponent(
+        IncidentParams const& p, GridParams const& g, int c, bool wantB, int i, int j, int k, float shift, float t)
+    {
+        float const(*pos)[3] = wantB ? kYeePosB : kYeePosE;
+        float x = float(i) + pos[c][0], y = float(j) + pos[c][1], z = float(k) + pos[c][2];
+        if(p.axis == 0)
+            x += shift;
+        else if(p.axis == 1)
+            y += shift;
+        else
+            z += shift;
+        float E[3];
+        incidentE(p, g, x, y, z, t, E);
+        if(!wantB)
+            return E[c];
+        int const c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+        return (p.d[c1] * E[c2] - p.d[c2] * E[c1]) / g.c;
+    }
+
+    // TF/SF correction of a face after a field update (incidentField/Solver.kernel UpdateFunctor
+    // with the Yee curl): updated[comp2] += base * incident[comp1], updated[comp1] -= base *
+    // incident[comp2], comp1 = (axis + 2) % 3, comp2 = (axis + 1) % 3, base = curl coefficient /
+    // d_axis * face direction.  After a B half step (curl coefficient -dt/2) the B plane on the
+    // scattered side of the surface (plane - 1 for a low face, plane for a high face) takes the
+    // incident E one plane further in on a low face (Solver.hpp:343-356); after the E step
+    // (c^2 dt) the E plane `plane` takes the incident B half a plane out.  For a wave along +y
+    // polarised along x: B_z -= dt/2 E_x,inc / dy and E_x += c^2 dt E_x,inc(at B_z) / (c dy).
     __global__ void kIncidentB(float* __restrict__ B, GridParams g, IncidentParams p, float t)
     {
         int const u1 = p.lo[0] + int(blockIdx.x * blockDim.x + threadIdx.x), u2 = p.lo[1] + int(blockIdx.y);
         if(u1 >= p.hi[0])
             return;
-        int const a = p.axis, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
-        int const pa = p.pol == 0 ? t1 : t2, oa = p.pol == 0 ? t2 : t1;
-        float const sigma = (pa == (a + 2) % 3) ? -float(p.dir) : float(p.dir);
+        int const a = p.axis, comp1 = (a + 2) % 3, comp2 = (a + 1) % 3;
+        float const da = pick3(g.dx, g.dy, g.dz, a);
+        float const base = -0.5f * g.dt / da * float(p.dir);
+        float const shift = p.dir > 0 ? 1.0f : 0.0f;
         int i, j, k;
         faceCell(a, p.dir > 0 ? p.plane - 1 : p.plane, u1, u2, i, j, k);
         size_t const nc = size_t(g.nx) * g.ny * g.nz;
         size_t const idx = size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * size_t(k));
-        float const h = 0.5f * g.dt / pick3(g.dx, g.dy, g.dz, a);
-        // E_p at the E plane, staggered by 1/2 along p
-        float const x = a == 0 ? float(p.plane) : float(i) + (pa == 0 ? 0.5f : 0.0f);
-        float const y = a == 1 ? float(p.plane) : float(j) + (pa == 1 ? 0.5f : 0.0f);
-        float const z = a == 2 ? float(p.plane) : float(k) + (pa == 2 ? 0.5f : 0.0f);
-        B[size_t(oa) * nc + idx] += sigma * h * incidentValue(p, g, x, y, z, t);
+        if(p.pv1[comp1] != 0.0f || p.pv2[comp1] != 0.0f)
+            B[size_t(comp2) * nc + idx] += base * incidentComponent(p, g, comp1, false, i, j, k, shift, t);
+        if(p.pv1[comp2] != 0.0f || p.pv2[comp2] != 0.0f)
+            B[size_t(comp1) * nc + idx] -= base * incidentComponent(p, g, comp2, false, i, j, k, shift, t);
     }
 
-    // After E += c^2 dt curl B: the E plane `plane` (total side) used the scattered B_o of the
-    // plane beyond it; adding the incident B_o = (dir e_a x E_inc)_o / c gives, for either
-    // direction and polarisation, E_p += c^2 dt / da * E_inc(at B_o) / c.  For a wave along +y:
-    // E_x -= c^2 dt B_z,inc / dy with B_z,inc = -E_x,inc / c, E_z += c^2 dt B_x,inc / dy with
-    // B_x,inc = E_z,inc / c.
     __global__ void kIncidentE(float* __restrict__ E, GridParams g, IncidentParams p, float t)
     {
         int const u1 = p.lo[0] + int(blockIdx.x * blockDim.x + threadIdx.x), u2 = p.lo[1] + int(blockIdx.y);
         if(u1 >= p.hi[0])
             return;
-        int const a = p.axis, t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
-        int const pa = p.pol == 0 ? t1 : t2;
+        int const a = p.axis, comp1 = (a + 2) % 3, comp2 = (a + 1) % 3;
+        float const da = pick3(g.dx, g.dy, g.dz, a);
+        float const base = g.c * g.c * g.dt / da * float(p.dir);
+        float const shift = p.dir > 0 ? -1.0f : 0.0f;
         int i, j, k;
         faceCell(a, p.plane, u1, u2, i, j, k);
         size_t const nc = size_t(g.nx) * g.ny * g.nz;
         size_t const idx = size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * size_t(k));
-        float const h = g.c * g.c * g.dt / pick3(g.dx, g.dy, g.dz, a);
-        // B_o half a cell beyond the surface, staggered by 1/2 along a and along p
-        float const ab = float(p.plane) - 0.5f * float(p.dir);
-        float const x = a == 0 ? ab : float(i) + (pa == 0 ? 0.5f : 0.0f);
-        float const y = a == 1 ? ab : float(j) + (pa == 1 ? 0.5f : 0.0f);
-        float const z = a == 2 ? ab : float(k) + (pa == 2 ? 0.5f : 0.0f);
-        E[size_t(pa) * nc + idx] += h * (incidentValue(p, g, x, y, z, t) / g.c);
+        E[size_t(comp2) * nc + idx] += base * incidentComponent(p, g, comp1, true, i, j, k, shift, t);
+        E[size_t(comp1) * nc + idx] -= base * incidentComponent(p, g, comp2, true, i, j, k, shift, t);
     }
 
     cudaError_t launchIncidentB(float* B, GridParams const& g, IncidentParams const& inc, float t, cudaStream_t stream)

@@ -1254,7 +1254,45 @@ extern "C"
         p.axis = f->axis;
         p.dir = dir;
         p.plane = f->surface;
-        p.pol = f->polarisation;
+        double const edge[3] = {s->cfg.dx, s->cfg.dy, s->cfg.dz};
+        double const da = edge[f->axis];
+        int const t1 = f->axis == 0 ? 1 : 0, t2 = f->axis == 2 ? 1 : 2;
+        // propagation direction and polarisation (BaseParam.def DIRECTION_*, POLARISATION_DIRECTION_*)
+        double dv[3] = {0.0, 0.0, 0.0}, pv[3] = {0.0, 0.0, 0.0};
+        bool const oblique = f->propagation[0] != 0.0f || f->propagation[1] != 0.0f || f->propagation[2] != 0.0f;
+        bool const polGiven = f->polarisation_vector[0] != 0.0f || f->polarisation_vector[1] != 0.0f
+            || f->polarisation_vector[2] != 0.0f;
+        for(int a = 0; a < 3; ++a)
+        {
+            dv[a] = oblique ? double(f->propagation[a]) : (a == f->axis ? double(dir) : 0.0);
+            pv[a] = polGiven ? double(f->polarisation_vector[a]) : (a == (f->polarisation == 0 ? t1 : t2) ? 1.0 : 0.0);
+        }
+        double const dn = dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2];
+        double const pn = pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2];
+        double const dp = dv[0] * pv[0] + dv[1] * pv[1] + dv[2] * pv[2];
+        if(!(std::fabs(dn - 1.0) < 1e-4) || !(std::fabs(pn - 1.0) < 1e-4))
+            return fail(PICGB_ERR_INVALID, "incident field: propagation and polarisation vectors must be unit vectors");
+        if(!(std::fabs(dp) < 1e-4))
+            return fail(PICGB_ERR_INVALID, "incident field: the polarisation must be orthogonal to the propagation");
+        if(!(dv[f->axis] * dir > 1e-3))
+            return fail(PICGB_ERR_INVALID, "incident field: the propagation must enter the box through the face");
+        if(f->circular != 0 && f->circular != 1)
+            return fail(PICGB_ERR_INVALID, "incident field: circular must be 0 or 1");
+        double const qv[3] = {dv[1] * pv[2] - dv[2] * pv[1], dv[2] * pv[0] - dv[0] * pv[2], dv[0] * pv[1] - dv[1] * pv[0]};
+        p.circular = f->circular;
+        for(int a = 0; a < 3; ++a)
+        {
+            p.d[a] = float(dv[a]);
+            p.pol[a] = float(pv[a]);
+            p.pol2[a] = float(qv[a]);
+        }
+        for(int a = 0; a < 3; ++a)
+            p.pv1[a] = f->circular ? p.pol[a] / std::sqrt(2.0f) : p.pol[a];
+        for(int a = 0; a < 3; ++a) // d x pv1 (getCircularPolarizationVector2)
+        {
+            int const b = (a + 1) % 3, c = (a + 2) % 3;
+            p.pv2[a] = f->circular ? p.d[b] * p.pv1[c] - p.d[c] * p.pv1[b] : 0.0f;
+        }
         double const omega = 2.0 * 3.14159265358979323846 * s->cfg.c / f->wavelength;
         // a0 = q E0 / (m c omega) with the species' units given by the caller through e_over_m = q / m
         p.E0 = float(f->a0 * omega * s->cfg.c / f->e_over_m);
@@ -1264,20 +1302,36 @@ extern "C"
         // (GaussianPulseEnvelope: exp(-(t / (2 tau))^2) on the field)
         p.tau2 = float(f->duration_fwhm / std::sqrt(2.0 * std::log(2.0)));
         p.tc = f->t_center;
-        p.c1 = f->center_x;
-        p.c2 = f->center_z;
         p.phase = f->phase;
-        double const edge[3] = {s->cfg.dx, s->cfg.dy, s->cfg.dz};
-        double const da = edge[f->axis];
-        p.origin = float(double(f->surface) - 0.25 * dir); // 0.75 cells inside POSITION
+        // origin: the beam axis on the Huygens plane, 0.75 cells inside POSITION
+        p.o[f->axis] = float((double(f->surface) - 0.25 * dir) * da);
+        p.o[t1] = float(double(f->center_x) * edge[t1]);
+        p.o[t2] = float(double(f->center_z) * edge[t2]);
         p.focusDist = float(double(f->focus) * da);
-        // phase velocity of the Yee grid at omega along the axis (calculatePhaseVelocity.hpp with the
-        // Yee dispersion relation): sin(k d / 2) / d = sin(omega dt / 2) / (c dt)
-        double const sk = da / (double(s->cfg.c) * double(s->cfg.dt)) * std::sin(0.5 * omega * double(s->cfg.dt));
-        if(!(sk > 0.0 && sk < 1.0))
+        // phase velocity of the Yee grid at omega along d (calculatePhaseVelocity.hpp with the Yee
+        // dispersion relation): sum_a (sin(k d_a h_a / 2) / h_a)^2 = (sin(omega dt / 2) / (c dt))^2,
+        // by bisection on the monotonic branch k max_a |d_a| h_a <= pi
+        double const rhs = std::pow(std::sin(0.5 * omega * double(s->cfg.dt)) / (double(s->cfg.c) * double(s->cfg.dt)), 2);
+        auto lhs = [&](double k)
+        {
+            double v = 0.0;
+            for(int a = 0; a < 3; ++a)
+                v += std::pow(std::sin(0.5 * k * dv[a] * edge[a]) / edge[a], 2);
+            return v;
+        };
+        double kmax = 0.0;
+        for(int a = 0; a < 3; ++a)
+            kmax = std::max(kmax, std::fabs(dv[a]) * edge[a]);
+        kmax = 3.14159265358979323846 / kmax;
+        if(!(rhs > 0.0 && rhs < lhs(kmax)))
             return fail(PICGB_ERR_INVALID, "incident field: wavelength %g is not resolved by the grid", double(f->wavelength));
-        double const kNum = 2.0 / da * std::asin(sk);
-        p.invVph = float(kNum / omega);
+        double klo = 0.0, khi = kmax;
+        for(int it = 0; it < 200; ++it)
+        {
+            double const km = 0.5 * (klo + khi);
+            (lhs(km) < rhs ? klo : khi) = km;
+        }
+        p.invVph = float(0.5 * (klo + khi) / omega);
         p.zR = float(3.14159265358979323846 * double(f->waist) * double(f->waist) / double(f->wavelength));
         p.k = float(omega / s->cfg.c);
         if(int r = incidentExtent(s, p))

@@ -102,22 +102,27 @@ namespace picgb
     // field at (x, y, z, t) is E0 exp(-r^2 / w0^2) exp(-(tau - tc)^2 / (2 sigma^2))
     // sin(omega (tau - tc) + phase), tau = t - (y - j0 dy) / c, r the distance from the
     // axis (cx, cz), polarised along x (pol 0) or z (pol 1), travelling along +y.
-    // One face of the total-field/scattered-field box.  Transverse axes: the two axes other
-    // than `axis`, in increasing order (first, second).
+    // One face of the total-field/scattered-field box and its pulse, in the vector form of
+    // fields/incidentField/Functors.hpp (BaseFunctorE): propagation direction d, polarisation
+    // vectors, origin on the face's Huygens plane.
     struct IncidentParams
     {
         int enabled;
-        int axis; // propagation axis
-        int dir; // +1: enters through the low face, travels +axis; -1: the high face, travels -axis
+        int axis; // face normal
+        int dir; // +1: the low face (the pulse enters towards +axis); -1: the high face
         int plane; // first (dir +1) or last (dir -1) E plane of the total-field region along axis
-        int pol; // E along the first (0) or second (1) transverse axis
+        int circular; // 0: E = pv1 value; 1: E = pv1 value(phase + pi/2) + pv2 value(phase)
         float E0, omega, w0, tc;
         float tau2; // twice the rms duration of the intensity (the envelope is exp(-(t / tau2)^2))
-        float c1, c2; // beam centre on the first and second transverse axis (cells)
         float phase;
-        float origin; // Huygens surface along the axis: plane - dir / 4 (cells)
-        float focusDist; // distance of the focus beyond the Huygens surface (length)
-        float invVph; // 1 / the Yee grid's phase velocity at omega along the axis
+        float d[3]; // unit propagation direction
+        float pv1[3]; // linear: the unit polarisation; circular: polarisation / sqrt(2)
+        float pv2[3]; // circular: d x pv1 (zero for linear)
+        float pol[3]; // the unit polarisation (internal coordinate axis 1)
+        float pol2[3]; // d x pol (internal coordinate axis 2)
+        float o[3]; // origin: the beam axis on the face's Huygens plane (length)
+        float focusDist; // distance of the focus from the origin along d (length)
+        float invVph; // 1 / the Yee grid's phase velocity at omega along d
         float zR; // Rayleigh length pi w0^2 / wavelength
         float k; // wave number omega / c
         int lo[2], hi[2]; // transverse extent of the face in cells, [lo, hi) on each transverse axis

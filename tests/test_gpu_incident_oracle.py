@@ -37,17 +37,24 @@ def dims(axis):
     return d
 
 
-def oracle_face(gd, axis, direction, surface, pol, center):
+def oracle_face(gd, axis, direction, surface, pol, center, prop=None, polvec=None, circular=False):
+    """The face in the reference's parameters: the origin is the beam axis on the Huygens plane (a
+    quarter cell before the first or last total E plane) at the transverse centre, the focus lies
+    `focus` face-axis cells from it along the propagation."""
     cell = (gd["dx"], gd["dy"], gd["dz"])
     t1, t2 = [d for d in range(3) if d != axis]
-    focus = [0.0, 0.0, 0.0]
-    focus[t1] = center[0] * cell[t1]
-    focus[t2] = center[1] * cell[t2]
-    # the Huygens surface lies a quarter cell before the first (last) total E plane
-    focus[axis] = (surface - 0.25 * direction) * cell[axis] + direction * BEAM["focus"] * cell[axis]
+    d = [float(np.float32(v)) for v in prop] if prop is not None else [float(direction) if a == axis else 0.0
+                                                                        for a in range(3)]
+    origin = [0.0, 0.0, 0.0]
+    origin[t1] = center[0] * cell[t1]
+    origin[t2] = center[1] * cell[t2]
+    origin[axis] = (surface - 0.25 * direction) * cell[axis]
+    focus = [origin[a] + BEAM["focus"] * cell[axis] * d[a] for a in range(3)]
     tau = BEAM["duration_fwhm"] / (2 * math.sqrt(2 * math.log(2)))  # rms duration of the intensity
+    pv = [float(np.float32(v)) for v in polvec] if polvec is not None else None
     return orc.incident_face(gd, axis, direction, surface, pol, BEAM["a0"], BEAM["wavelength"], BEAM["waist"], tau,
-                             -BEAM["t_center"], BEAM["phase"], focus)
+                             -BEAM["t_center"], BEAM["phase"], focus, propagation=d if prop is not None else None,
+                             polarisation_vector=pv, circular=circular)
 
 
 def run_both(axis, faces):
@@ -56,12 +63,14 @@ def run_both(axis, faces):
     with pg.Simulation(g) as sim:
         for f in faces:
             sim.set_incident_field(surface=f["surface"], polarisation=f["pol"], center=f["center"], axis=f["axis"],
-                                   direction=f["dir"], **BEAM)
+                                   direction=f["dir"], propagation=f.get("prop"), polarisation_vector=f.get("polvec"),
+                                   circular=f.get("circular", False), **BEAM)
         sim.run(STEPS)
         Eg, Bg = sim.get_field("E"), sim.get_field("B")
     E = np.zeros_like(Eg)
     B = np.zeros_like(Bg)
-    of = [oracle_face(gd, f["axis"], f["dir"], f["surface"], f["pol"], f["center"]) for f in faces]
+    of = [oracle_face(gd, f["axis"], f["dir"], f["surface"], f["pol"], f["center"], f.get("prop"), f.get("polvec"),
+                      f.get("circular", False)) for f in faces]
     dt = np.float32(g.dt)
     for s in range(STEPS):
         # the times of the field stages: step dt, step dt + dt/2, (step + 1) dt, in float
@@ -96,3 +105,59 @@ def test_two_faces_match_the_oracle():
     Eg, Bg, E, B = run_both(1, faces)
     assert np.abs(Eg - E).max() <= TOL * E0, np.abs(Eg - E).max() / E0
     assert np.abs(Bg - B).max() <= TOL * E0, np.abs(Bg - B).max() / E0
+
+
+def unit(v):
+    v = np.asarray(v, np.float64)
+    return tuple(v / np.linalg.norm(v))
+
+
+TH = math.radians(25.0)
+OBLIQUE = [
+    # s-polarised through the low y face, 25 degrees off the normal in the x-y plane
+    dict(axis=1, dir=1, surface=16, pol=0, center=(13.0, 18.5), prop=(math.sin(TH), math.cos(TH), 0.0),
+         polvec=(0.0, 0.0, 1.0)),
+    # p-polarised (E in the plane of incidence)
+    dict(axis=1, dir=1, surface=16, pol=0, center=(13.0, 18.5), prop=(math.sin(TH), math.cos(TH), 0.0),
+         polvec=(math.cos(TH), -math.sin(TH), 0.0)),
+    # through the high x face, 30 degrees towards +z
+    dict(axis=0, dir=-1, surface=LONG - 1 - 16, pol=0, center=(13.0, 18.5),
+         prop=(-math.cos(math.radians(30)), 0.0, math.sin(math.radians(30))), polvec=(0.0, 1.0, 0.0)),
+    # circular, normal incidence through the low z face
+    dict(axis=2, dir=1, surface=16, pol=0, center=(13.0, 18.5), circular=True),
+    # circular and oblique through the high y face
+    dict(axis=1, dir=-1, surface=LONG - 1 - 16, pol=0, center=(15.0, 14.0), prop=unit((0.3, -0.85, 0.4)),
+         polvec=unit(np.cross(unit((0.3, -0.85, 0.4)), (1.0, 0.0, 0.0))), circular=True),
+]
+
+
+@pytest.mark.parametrize("face", OBLIQUE, ids=["s-pol", "p-pol", "x-high", "circular", "oblique-circular"])
+def test_oblique_and_circular_faces_match_the_oracle(face):
+    Eg, Bg, E, B = run_both(face["axis"], [face])
+    scale = max(np.abs(E).max(), np.abs(B).max())
+    assert scale > 0.05
+    assert np.abs(Eg - E).max() <= TOL * E0, np.abs(Eg - E).max() / E0
+    assert np.abs(Bg - B).max() <= TOL * E0, np.abs(Bg - B).max() / E0
+
+
+def test_oblique_pulse_travels_along_its_direction():
+    """The E-field energy centroid of a 30-degree pulse through the low y face moves along the
+    propagation direction: the angle of its displacement between two times is within 3 degrees."""
+    th = math.radians(30.0)
+    g = pg.Grid(128, 96, 32)
+    with pg.Simulation(g) as sim:
+        sim.set_incident_field(a0=1.0, wavelength=8.0, waist=8.0, duration_fwhm=12.0, t_center=30.0, surface=8,
+                               center=(32.0, 16.0), focus=20.0, propagation=(math.sin(th), math.cos(th), 0.0),
+                               polarisation_vector=(0.0, 0.0, 1.0))
+        cents = []
+        for steps in (110, 50):
+            sim.run(steps)
+            Ez = sim.get_field("E")[2].astype(np.float64)
+            w = (Ez ** 2).sum(axis=0)  # over z: [y][x]
+            w[:12, :] = 0.0  # the region next to the surface
+            y, x = np.mgrid[0:96, 0:128]
+            cents.append(((w * x).sum() / w.sum(), (w * y).sum() / w.sum()))
+    dx, dy = cents[1][0] - cents[0][0], cents[1][1] - cents[0][1]
+    ang = math.degrees(math.atan2(dx, dy))
+    assert abs(ang - 30.0) < 3.0, ang
+    assert math.hypot(dx, dy) > 15.0
