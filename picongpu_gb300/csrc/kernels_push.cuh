@@ -42,6 +42,9 @@ namespace picgb
 #ifndef PICGB_J_PLANE_PAD
 #    define PICGB_J_PLANE_PAD 1
 #endif
+#ifndef PICGB_GATHER_PAIRS
+#    define PICGB_GATHER_PAIRS 1 // the six field components gathered in three f32x2 pairs
+#endif
 #ifndef PICGB_POOL_LEFTOVERS
 #    define PICGB_POOL_LEFTOVERS 1 // the warps' leftover deposit jobs drained together after the loop
 #endif
@@ -367,12 +370,25 @@ namespace picgb
                     GatherWeights<SH> gw;
                     gw.compute(pos);
                     // Yee positions (fields/YeeCell.hpp:70-131): E_x (1/2,0,0) ... B_x (0,1/2,1/2) ...
+#if PICGB_GATHER_PAIRS
+                    // pairs sharing the staggering along two axes, with packed f32x2 FMAs
+                    float2 const bxEy = gw.template gather2<TG::PX, TG::PY, 0, 1, 1, 0, 1, 0>(Bs, Es + TG::GT, lx, ly, lz);
+                    float2 const byEz = gw.template gather2<TG::PX, TG::PY, 1, 0, 1, 0, 0, 1>(Bs + TG::GT, Es + 2 * TG::GT, lx, ly, lz);
+                    float2 const bzEx = gw.template gather2<TG::PX, TG::PY, 1, 1, 0, 1, 0, 0>(Bs + 2 * TG::GT, Es, lx, ly, lz);
+                    Bv[0] = bxEy.x;
+                    Ev[1] = bxEy.y;
+                    Bv[1] = byEz.x;
+                    Ev[2] = byEz.y;
+                    Bv[2] = bzEx.x;
+                    Ev[0] = bzEx.y;
+#else
                     Bv[0] = gw.template gather<TG::PX, TG::PY, 0, 1, 1>(Bs, lx, ly, lz);
                     Bv[1] = gw.template gather<TG::PX, TG::PY, 1, 0, 1>(Bs + TG::GT, lx, ly, lz);
                     Bv[2] = gw.template gather<TG::PX, TG::PY, 1, 1, 0>(Bs + 2 * TG::GT, lx, ly, lz);
                     Ev[0] = gw.template gather<TG::PX, TG::PY, 1, 0, 0>(Es, lx, ly, lz);
                     Ev[1] = gw.template gather<TG::PX, TG::PY, 0, 1, 0>(Es + TG::GT, lx, ly, lz);
                     Ev[2] = gw.template gather<TG::PX, TG::PY, 0, 0, 1>(Es + 2 * TG::GT, lx, ly, lz);
+#endif
                     if constexpr(!ALT)
                         boris(charge, mass, Ev, Bv, pp.dt, pp.c2, pp.rc2, mom, vel);
                     else

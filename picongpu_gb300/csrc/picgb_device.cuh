@@ -244,6 +244,52 @@ namespace picgb
         return rz;
     }
 
+    // Two components gathered together with packed f32x2 fused multiply-adds (each half is the
+    // scalar chain of `interpolate`, so both results are bit-identical to two scalar gathers).
+    template<typename SH, int TX, int TY>
+    __device__ __forceinline__ float2 interpolate2(
+        float const* __restrict__ tileA,
+        float const* __restrict__ tileB,
+        int lx,
+        int ly,
+        int lz,
+        int const shA[3],
+        int const shB[3],
+        float const* axA,
+        float const* ayA,
+        float const* azA,
+        float const* axB,
+        float const* ayB,
+        float const* azB)
+    {
+        constexpr int S = SH::supp;
+        float const* baseA = tileA
+            + ((lx + SH::gLo + shA[0] + SH::osBegin)
+               + TX * ((ly + SH::gLo + shA[1] + SH::osBegin) + TY * (lz + SH::gLo + shA[2] + SH::osBegin)));
+        float const* baseB = tileB
+            + ((lx + SH::gLo + shB[0] + SH::osBegin)
+               + TX * ((ly + SH::gLo + shB[1] + SH::osBegin) + TY * (lz + SH::gLo + shB[2] + SH::osBegin)));
+        float2 rz = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for(int z = 0; z < S; ++z)
+        {
+            float2 ry = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for(int y = 0; y < S; ++y)
+            {
+                float2 rx = make_float2(0.0f, 0.0f);
+                float const* rowA = baseA + TX * (y + TY * z);
+                float const* rowB = baseB + TX * (y + TY * z);
+#pragma unroll
+                for(int x = 0; x < S; ++x)
+                    rx = __ffma2_rn(make_float2(rowA[x], rowB[x]), make_float2(axA[x], axB[x]), rx);
+                ry = __ffma2_rn(rx, make_float2(ayA[y], ayB[y]), ry);
+            }
+            rz = __ffma2_rn(ry, make_float2(azA[z], azB[z]), rz);
+        }
+        return rz;
+    }
+
     // ShiftCoordinateSystem (algorithms/ShiftCoordinateSystem.hpp:54-79) and the
     // on-support shape array for the two staggering offsets a Yee component can
     // have along an axis (0 and 1/2, fields/YeeCell.hpp:70-131).  The six
@@ -270,6 +316,16 @@ namespace picgb
                     sh[a][d] = s;
                     SH::base(fa(fs(v, float(s)), 0.5f), w[a][d]);
                 }
+        }
+
+        // components A (staggering ax, ay, az) and B (bx, by, bz) together
+        template<int TX, int TY, int ax, int ay, int az, int bx, int by, int bz>
+        __device__ __forceinline__ float2 gather2(float const* __restrict__ tileA, float const* __restrict__ tileB, int lx, int ly, int lz) const
+        {
+            int const shA[3] = {sh[ax][0], sh[ay][1], sh[az][2]};
+            int const shB[3] = {sh[bx][0], sh[by][1], sh[bz][2]};
+            return interpolate2<SH, TX, TY>(
+                tileA, tileB, lx, ly, lz, shA, shB, w[ax][0], w[ay][1], w[az][2], w[bx][0], w[by][1], w[bz][2]);
         }
 
         // ax, ay, az: staggering (0 or 1) of the component along x, y, z
