@@ -282,8 +282,12 @@ extern "C"
      * the direction from it, and v_ph solves the Yee dispersion relation along the direction,
      * sum_a (sin(k d_a h_a / 2) / h_a)^2 = (sin(omega dt / 2) / (c dt))^2.  circular = 1 gives
      * E = (p/sqrt 2) value(phase + pi/2) + (d x p / sqrt 2) value(phase)
-     * (GaussianPulseFunctorIncidentE::operator()).  Laguerre modes, pulse-front tilt and
-     * TIME_DELAY are not supported. */
+     * (GaussianPulseFunctorIncidentE::operator()).  With laguerre_count > 0 the transverse profile
+     * is the reference's sum of Laguerre-Gauss modes (GaussianPulse.hpp:260-289):
+     *   E = E0 (w0/w) [sum_m a_m L_m(2 r^2/w^2) exp(-r^2/w^2) cos(... + (2m+1) xi + phase + phi_m)]
+     *       exp(-((time - r_c/c) / (2 tau))^2) / sum_m a_m,
+     * L_m the Laguerre polynomials; time_delay is TIME_DELAY (t_loc = t - dist / v_ph - time_delay).
+     * Pulse-front tilt is not supported. */
     typedef struct picgb_incident_field
     {
         int32_t enabled;
@@ -297,6 +301,10 @@ extern "C"
         float polarisation_vector[3]; /* unit POLARISATION_DIRECTION_{X,Y,Z}, orthogonal to the propagation;
                                           all zero: the transverse axis `polarisation` */
         int32_t circular; /* 0: linear polarisation; 1: circular (PolarisationType::Circular) */
+        float time_delay; /* TIME_DELAY: the local time starts this much later (>= 0) */
+        int32_t laguerre_count; /* Laguerre-Gauss modes 0 .. count-1 (at most 8); 0: the fundamental mode */
+        float laguerre_modes[8]; /* laguerreModes: mode amplitudes (their sum must not be 0) */
+        float laguerre_phases[8]; /* laguerrePhases: mode phases */
     } picgb_incident_field;
     int picgb_set_incident_field(picgb_sim* sim, const picgb_incident_field* field);
 

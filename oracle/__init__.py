@@ -64,7 +64,8 @@ class OrcIncidentFace(ctypes.Structure):
                 ("circular", ctypes.c_int),
                 ("amplitude", ctypes.c_float), ("wavelength", ctypes.c_float), ("w0", ctypes.c_float),
                 ("pulse_duration", ctypes.c_float), ("time_shift", ctypes.c_float), ("laser_phase", ctypes.c_float),
-                ("phase_velocity", ctypes.c_float)]
+                ("phase_velocity", ctypes.c_float), ("time_delay", ctypes.c_float), ("nmodes", ctypes.c_int),
+                ("modes", ctypes.c_float * 8), ("mode_phases", ctypes.c_float * 8)]
 
 
 class OrcParticles64(ctypes.Structure):
@@ -222,7 +223,7 @@ def set_threads(n: int) -> None:
 
 def incident_face(g, axis, direction, surface, polarisation, a0, wavelength, waist, pulse_duration, time_shift,
                   laser_phase, focus_position, e_over_m=1.0, propagation=None, polarisation_vector=None,
-                  circular=False):
+                  circular=False, time_delay=0.0, laguerre_modes=None, laguerre_phases=None):
     """One incident-field face in the reference's parameters (profiles/BaseParam.def,
     GaussianPulse.def): the propagation direction is `propagation` (DIRECTION_*) or the face
     normal, the E polarisation `polarisation_vector` (POLARISATION_DIRECTION_*) or the unit vector
@@ -254,6 +255,12 @@ def incident_face(g, axis, direction, surface, polarisation, a0, wavelength, wai
     f.amplitude = a0 * omega * c / e_over_m
     f.wavelength, f.w0, f.pulse_duration = wavelength, waist, pulse_duration
     f.time_shift, f.laser_phase = time_shift, laser_phase
+    f.time_delay = time_delay  # TIME_DELAY
+    modes = list(laguerre_modes) if laguerre_modes else [1.0]  # laguerreModes, laguerrePhases
+    phases = list(laguerre_phases) if laguerre_phases else [0.0] * len(modes)
+    f.nmodes = len(modes)
+    for m in range(len(modes)):
+        f.modes[m], f.mode_phases[m] = modes[m], phases[m]
     return f
 
 

@@ -46,6 +46,9 @@ extern "C"
         float dirv[3], polv[3], focus[3];
         int circular;
         float amplitude, wavelength, w0, pulse_duration, time_shift, laser_phase, phase_velocity;
+        float time_delay;
+        int nmodes;
+        float modes[8], mode_phases[8];
     };
     // the FP64 instantiation's exchange format (reference gradients of the differentiable run)
     struct orc_field64
@@ -177,6 +180,13 @@ extern "C"
         face.timeShift = f->time_shift;
         face.laserPhase = f->laser_phase;
         face.phaseVelocity = f->phase_velocity;
+        face.timeDelay = f->time_delay;
+        face.nmodes = f->nmodes;
+        for(int m = 0; m < 8; ++m)
+        {
+            face.modes[m] = f->modes[m];
+            face.modePhases[m] = f->mode_phases[m];
+        }
         auto Ff = toF(F);
         orc::incidentUpdate(toGrid(g), face, Ff, update_b != 0, t);
     }

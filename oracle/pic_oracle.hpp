@@ -1225,7 +1225,27 @@ namespace orc
         float timeShift = 0.f; // GaussianPulseEnvelope::TIME_SHIFT = -PULSE_INIT * PULSE_DURATION / 2
         float laserPhase = 0.f;
         float phaseVelocity = 1.f; // calculatePhaseVelocity, times c
+        float timeDelay = 0.f; // TIME_DELAY
+        int nmodes = 1; // laguerreModes / laguerrePhases
+        float modes[8] = {1.f}, modePhases[8] = {0.f};
     };
+
+    // simpleLaguerre (GaussianPulse.hpp:298-323): the Laguerre polynomial L_n(x) by its recursion
+    inline float simpleLaguerre(int n, float x)
+    {
+        if(n == 0)
+            return 1.f;
+        int cur = 1;
+        float lm1 = 1.f, l = 1.f - x, lp = 0.f;
+        while(cur < n)
+        {
+            lp = ((2.f * float(cur) + 1.f - x) * l - float(cur) * lm1) / float(cur + 1);
+            lm1 = l;
+            l = lp;
+            ++cur;
+        }
+        return l;
+    }
 
     inline float dotf(float const a[3], float const b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
@@ -1248,7 +1268,7 @@ namespace orc
         for(int d = 0; d < 3; ++d)
             shift[d] = idx[d] * cell[d] - origin[d];
         float const pos0 = dotf(shift, dirv);
-        float const currentTime = t - pos0 / f.phaseVelocity;
+        float const currentTime = t - (pos0 / f.phaseVelocity + f.timeDelay);
         float value = 0.f, value1 = 0.f; // value1: with the phase shifted by pi/2 (circular)
         if(!(currentTime < 0.f)) // cut off before the pulse reaches this point
         {
@@ -1272,16 +1292,21 @@ namespace orc
             float const k = 2.f * 3.14159265358979323846f / f.wavelength;
             float const shiftedTime = time - r / g.c;
             float const exponent = shiftedTime / (2.f * f.pulseDuration);
-            float etrans = std::exp(-r2OverW2) * std::cos(k * focusPos - k * r + xi + phase);
-            etrans *= std::exp(-exponent * exponent);
-            value = f.amplitude * (f.w0 / w) * etrans;
-            if(f.circular)
+            float norm = 0.f;
+            for(int m = 0; m < f.nmodes; ++m)
+                norm += f.modes[m];
+            auto modesSum = [&](float ph)
             {
-                float const phase1 = omega * (time - focusPos / g.c) + f.laserPhase + 1.57079633f;
-                float et1 = std::exp(-r2OverW2) * std::cos(k * focusPos - k * r + xi + phase1);
-                et1 *= std::exp(-exponent * exponent);
-                value1 = f.amplitude * (f.w0 / w) * et1;
-            }
+                float etrans = 0.f;
+                for(int m = 0; m < f.nmodes; ++m)
+                    etrans += f.modes[m] * simpleLaguerre(m, 2.f * r2OverW2) * std::exp(-r2OverW2)
+                        * std::cos(k * focusPos - k * r + (2.f * float(m) + 1.f) * xi + ph + f.modePhases[m]);
+                etrans *= std::exp(-exponent * exponent);
+                return f.amplitude * (f.w0 / w) * etrans / norm;
+            };
+            value = modesSum(phase);
+            if(f.circular)
+                value1 = modesSum(omega * (time - focusPos / g.c) + f.laserPhase + 1.57079633f);
         }
         float E[3];
         if(!f.circular)

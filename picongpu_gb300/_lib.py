@@ -73,7 +73,8 @@ class IncidentField(ctypes.Structure):
                 ("e_over_m", c_float), ("wavelength", c_float), ("waist", c_float), ("duration_fwhm", c_float),
                 ("t_center", c_float), ("center_x", c_float), ("center_z", c_float), ("phase", c_float),
                 ("focus", c_float), ("direction", c_int), ("propagation", c_float * 3),
-                ("polarisation_vector", c_float * 3), ("circular", c_int)]
+                ("polarisation_vector", c_float * 3), ("circular", c_int), ("time_delay", c_float),
+                ("laguerre_count", c_int), ("laguerre_modes", c_float * 8), ("laguerre_phases", c_float * 8)]
 
 
 class EnsembleConfig(ctypes.Structure):

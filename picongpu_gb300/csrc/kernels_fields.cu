@@ -250,7 +250,7 @@ namespace picgb
         E[0] = E[1] = E[2] = 0.0f;
         float const s0 = x * g.dx - p.o[0], s1 = y * g.dy - p.o[1], s2 = z * g.dz - p.o[2];
         float const pos0 = s0 * p.d[0] + s1 * p.d[1] + s2 * p.d[2];
-        float const tcur = t - pos0 * p.invVph;
+        float const tcur = t - (pos0 * p.invVph + p.timeDelay);
         if(tcur < 0.0f)
             return;
         float const time = tcur - p.tc;
@@ -266,8 +266,30 @@ namespace picgb
         float const rc = 0.5f * r2 * rInv;
         float const e = (time - rc / g.c) / p.tau2;
         float const gt = expf(-r2OverW2), ge = expf(-e * e), amp = p.E0 * (p.w0 / w);
-        // E0 (w0 / w) ((exp(-r^2/w^2) cos(...)) exp(-e^2)), the association of the reference
-        float const v2 = amp * ((gt * cosf(p.k * fp - p.k * rc + xi + phase)) * ge);
+        // E0 (w0 / w) ((sum_m a_m L_m(2 r^2/w^2) exp(-r^2/w^2) cos(... + (2m+1) xi + phi_m)) exp(-e^2))
+        // / sum_m a_m, the loop and association of the reference (GaussianPulse.hpp:260-289)
+        auto value = [&](float ph)
+        {
+            float et = 0.0f;
+            float const x = 2.0f * r2OverW2;
+            float lm1 = 1.0f, lm = 1.0f; // L_{m-1}, L_m (simpleLaguerre's recursion)
+            for(int m = 0; m < p.nmodes; ++m)
+            {
+                if(m == 1)
+                    lm = 1.0f - x;
+                else if(m > 1)
+                {
+                    float const next = ((2.0f * float(m - 1) + 1.0f - x) * lm - float(m - 1) * lm1) / float(m);
+                    lm1 = lm;
+                    lm = next;
+                }
+                et += p.modes[m] * lm * gt
+                    * cosf(p.k * fp - p.k * rc + (2.0f * float(m) + 1.0f) * xi + ph + p.modePhases[m]);
+            }
+            et *= ge;
+            return amp * et / p.modeNorm;
+        };
+        float const v2 = value(phase);
         if(!p.circular)
         {
 #pragma unroll
@@ -275,8 +297,7 @@ namespace picgb
                 E[c] = p.pv1[c] * v2;
             return;
         }
-        float const phase1 = p.omega * (time - fp / g.c) + p.phase + 1.57079633f; // + pi/2
-        float const v1 = amp * ((gt * cosf(p.k * fp - p.k * rc + xi + phase1)) * ge);
+        float const v1 = value(p.omega * (time - fp / g.c) + p.phase + 1.57079633f); // + pi/2
 #pragma unroll
         for(int c = 0; c < 3; ++c)
             E[c] = p.pv1[c] * v1 + p.pv2[c] * v2;

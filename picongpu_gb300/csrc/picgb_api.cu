@@ -1334,6 +1334,21 @@ extern "C"
         p.invVph = float(0.5 * (klo + khi) / omega);
         p.zR = float(3.14159265358979323846 * double(f->waist) * double(f->waist) / double(f->wavelength));
         p.k = float(omega / s->cfg.c);
+        if(!(f->time_delay >= 0.0f))
+            return fail(PICGB_ERR_INVALID, "incident field: time_delay must be >= 0 (TIME_DELAY)");
+        p.timeDelay = f->time_delay;
+        if(f->laguerre_count < 0 || f->laguerre_count > 8)
+            return fail(PICGB_ERR_INVALID, "incident field: laguerre_count %d outside 0..8", int(f->laguerre_count));
+        p.nmodes = f->laguerre_count ? f->laguerre_count : 1;
+        p.modeNorm = 0.0f;
+        for(int m = 0; m < p.nmodes; ++m)
+        {
+            p.modes[m] = f->laguerre_count ? f->laguerre_modes[m] : 1.0f;
+            p.modePhases[m] = f->laguerre_count ? f->laguerre_phases[m] : 0.0f;
+            p.modeNorm += p.modes[m];
+        }
+        if(!(std::fabs(p.modeNorm) > 1.1920929e-7f)) // GaussianPulse: "Sum of laguerreModes can not be 0."
+            return fail(PICGB_ERR_INVALID, "incident field: the sum of the Laguerre mode amplitudes is 0");
         if(int r = incidentExtent(s, p))
             return r;
         s->inc[face] = p;

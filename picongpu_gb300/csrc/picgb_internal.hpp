@@ -125,6 +125,10 @@ namespace picgb
         float invVph; // 1 / the Yee grid's phase velocity at omega along d
         float zR; // Rayleigh length pi w0^2 / wavelength
         float k; // wave number omega / c
+        float timeDelay; // TIME_DELAY
+        int nmodes; // Laguerre-Gauss modes 0 .. nmodes-1 (1: the fundamental mode)
+        float modes[8], modePhases[8];
+        float modeNorm; // the sum of the mode amplitudes
         int lo[2], hi[2]; // transverse extent of the face in cells, [lo, hi) on each transverse axis
     };
     constexpr int kIncidentFaces = 6; // face = 2 axis + (dir < 0)

@@ -298,7 +298,8 @@ class Simulation:
     def set_incident_field(self, a0: float, wavelength: float, waist: float, duration_fwhm: float, t_center: float,
                            surface: int, polarisation: int = 0, center=None, phase: float = 0.0,
                            e_over_m: float = 1.0, focus: float = 0.0, axis: int = 1, direction: int = 1,
-                           propagation=None, polarisation_vector=None, circular: bool = False) -> None:
+                           propagation=None, polarisation_vector=None, circular: bool = False,
+                           time_delay: float = 0.0, laguerre_modes=None, laguerre_phases=None) -> None:
         """Focused Gaussian pulse entering through the TF/SF face normal to `axis` (0, 1, 2):
         direction +1 from the low face along +axis, -1 from the high face along -axis
         (fields/incidentField/Solver.hpp, profiles/GaussianPulse.hpp).  `surface` is the first
@@ -308,14 +309,18 @@ class Simulation:
         puts E along the first or the second of them, `phase` is the reference's LASER_PHASE of
         the cosine carrier and `t_center` its PULSE_INIT * PULSE_DURATION / 2.  `propagation`
         and `polarisation_vector` (unit 3-vectors, DIRECTION_* and POLARISATION_DIRECTION_*) give
-        oblique incidence through the face, `circular` circular polarisation.  Each face holds
-        its own pulse; see picgb_set_incident_field."""
+        oblique incidence through the face, `circular` circular polarisation; `time_delay` is
+        TIME_DELAY and `laguerre_modes` / `laguerre_phases` (up to 8) the Laguerre-Gauss mode sum
+        of GaussianPulse.  Each face holds its own pulse; see picgb_set_incident_field."""
         cells = (self.grid.nx, self.grid.ny, self.grid.nz)
         t1, t2 = [d for d in range(3) if d != axis] if axis in (0, 1, 2) else (0, 2)
         c1, c2 = center if center is not None else (cells[t1] / 2.0, cells[t2] / 2.0)
         f = L.IncidentField(1, axis, surface, polarisation, a0, e_over_m, wavelength, waist, duration_fwhm, t_center,
                             c1, c2, phase, focus, direction, (ctypes.c_float * 3)(*(propagation or (0, 0, 0))),
-                            (ctypes.c_float * 3)(*(polarisation_vector or (0, 0, 0))), int(bool(circular)))
+                            (ctypes.c_float * 3)(*(polarisation_vector or (0, 0, 0))), int(bool(circular)),
+                            float(time_delay), len(laguerre_modes or ()),
+                            (ctypes.c_float * 8)(*(laguerre_modes or ())),
+                            (ctypes.c_float * 8)(*(laguerre_phases or ())))
         L.call("picgb_set_incident_field", self.handle, ctypes.byref(f))
 
     def clear_incident_field(self, axis: int | None = None, direction: int = 1) -> None:

@@ -9,8 +9,9 @@ intensity FWHM 12, t_center 40), 140 steps.  The oracle runs the same split Yee 
 the reference's vector formulation (origin on the Huygens surface, internal coordinates by
 dot products, updated[comp2] += base * inc[comp1], updated[comp1] -= base * inc[comp2]).
 Contract: E and B agree within 2e-6 of the amplitude E0 = a0 omega (measured on GB300: 2e-7
-to 3e-7), for faces on all three axes, both directions and both polarisations, and for two
-faces at once; the rest is float rounding of the carrier's argument (up to about 40 rad) and
+to 3e-7), for faces on all three axes, both directions and both polarisations, for two faces
+at once, at oblique incidence (s and p polarised), with circular polarisation, and with a sum
+of Laguerre-Gauss modes and TIME_DELAY; the rest is float rounding of the carrier's argument (up to about 40 rad) and
 the GPU's fused multiply-adds.  A structural difference (a quarter cell in the origin, a sign,
 a staggering) shows at 1e-2 E0 or more.
 """
@@ -37,7 +38,8 @@ def dims(axis):
     return d
 
 
-def oracle_face(gd, axis, direction, surface, pol, center, prop=None, polvec=None, circular=False):
+def oracle_face(gd, axis, direction, surface, pol, center, prop=None, polvec=None, circular=False, delay=0.0,
+                modes=None, phases=None):
     """The face in the reference's parameters: the origin is the beam axis on the Huygens plane (a
     quarter cell before the first or last total E plane) at the transverse centre, the focus lies
     `focus` face-axis cells from it along the propagation."""
@@ -54,7 +56,8 @@ def oracle_face(gd, axis, direction, surface, pol, center, prop=None, polvec=Non
     pv = [float(np.float32(v)) for v in polvec] if polvec is not None else None
     return orc.incident_face(gd, axis, direction, surface, pol, BEAM["a0"], BEAM["wavelength"], BEAM["waist"], tau,
                              -BEAM["t_center"], BEAM["phase"], focus, propagation=d if prop is not None else None,
-                             polarisation_vector=pv, circular=circular)
+                             polarisation_vector=pv, circular=circular, time_delay=delay, laguerre_modes=modes,
+                             laguerre_phases=phases)
 
 
 def run_both(axis, faces):
@@ -64,13 +67,14 @@ def run_both(axis, faces):
         for f in faces:
             sim.set_incident_field(surface=f["surface"], polarisation=f["pol"], center=f["center"], axis=f["axis"],
                                    direction=f["dir"], propagation=f.get("prop"), polarisation_vector=f.get("polvec"),
-                                   circular=f.get("circular", False), **BEAM)
+                                   circular=f.get("circular", False), time_delay=f.get("delay", 0.0),
+                                   laguerre_modes=f.get("modes"), laguerre_phases=f.get("phases"), **BEAM)
         sim.run(STEPS)
         Eg, Bg = sim.get_field("E"), sim.get_field("B")
     E = np.zeros_like(Eg)
     B = np.zeros_like(Bg)
     of = [oracle_face(gd, f["axis"], f["dir"], f["surface"], f["pol"], f["center"], f.get("prop"), f.get("polvec"),
-                      f.get("circular", False)) for f in faces]
+                      f.get("circular", False), f.get("delay", 0.0), f.get("modes"), f.get("phases")) for f in faces]
     dt = np.float32(g.dt)
     for s in range(STEPS):
         # the times of the field stages: step dt, step dt + dt/2, (step + 1) dt, in float
@@ -128,10 +132,19 @@ OBLIQUE = [
     # circular and oblique through the high y face
     dict(axis=1, dir=-1, surface=LONG - 1 - 16, pol=0, center=(15.0, 14.0), prop=unit((0.3, -0.85, 0.4)),
          polvec=unit(np.cross(unit((0.3, -0.85, 0.4)), (1.0, 0.0, 0.0))), circular=True),
+
+
+    # a sum of three Laguerre-Gauss modes with phases, and TIME_DELAY
+    dict(axis=1, dir=1, surface=16, pol=1, center=(13.0, 18.5), delay=7.5, modes=(1.0, 0.5, -0.25),
+         phases=(0.0, 0.3, -0.2)),
+    # the same, circular and oblique
+    dict(axis=1, dir=1, surface=16, pol=0, center=(13.0, 18.5), prop=(math.sin(TH), math.cos(TH), 0.0),
+         polvec=(0.0, 0.0, 1.0), circular=True, delay=3.0, modes=(0.8, 0.4, 0.2, 0.1), phases=(0.1, 0.0, 0.5, 1.0)),
 ]
 
 
-@pytest.mark.parametrize("face", OBLIQUE, ids=["s-pol", "p-pol", "x-high", "circular", "oblique-circular"])
+@pytest.mark.parametrize("face", OBLIQUE, ids=["s-pol", "p-pol", "x-high", "circular", "oblique-circular",
+                                               "laguerre-delay", "laguerre-circular-oblique"])
 def test_oblique_and_circular_faces_match_the_oracle(face):
     Eg, Bg, E, B = run_both(face["axis"], [face])
     scale = max(np.abs(E).max(), np.abs(B).max())
