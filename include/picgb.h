@@ -287,7 +287,13 @@ extern "C"
      *   E = E0 (w0/w) [sum_m a_m L_m(2 r^2/w^2) exp(-r^2/w^2) cos(... + (2m+1) xi + phase + phi_m)]
      *       exp(-((time - r_c/c) / (2 tau))^2) / sum_m a_m,
      * L_m the Laguerre polynomials; time_delay is TIME_DELAY (t_loc = t - dist / v_ph - time_delay).
-     * Pulse-front tilt is not supported. */
+     * Pulse-front tilt is not supported.
+     * profile = PICGB_PROFILE_PLANE_WAVE is profiles/PlaneWave.hpp (a separable functor, transversal
+     * factor 1, the waist, focus and Laguerre fields unused): with mu = ramp_init tau / 2 and
+     * T = tau sqrt(2), E = E0 (sin(ph) + cos(ph) f) env, ph = omega (t_loc - mu) + phase, env =
+     * exp(-(t_loc - mu)^2 / (2 T^2)) and f = (t_loc - mu) / (omega T^2) on the rising ramp (t_loc < mu),
+     * the same with mu + plateau on the falling ramp (t_loc > mu + plateau), env = 1 and f = 0 on the
+     * plateau. */
     typedef struct picgb_incident_field
     {
         int32_t enabled;
@@ -305,7 +311,15 @@ extern "C"
         int32_t laguerre_count; /* Laguerre-Gauss modes 0 .. count-1 (at most 8); 0: the fundamental mode */
         float laguerre_modes[8]; /* laguerreModes: mode amplitudes (their sum must not be 0) */
         float laguerre_phases[8]; /* laguerrePhases: mode phases */
+        int32_t profile; /* PICGB_PROFILE_GAUSSIAN_PULSE (0) or PICGB_PROFILE_PLANE_WAVE */
+        float ramp_init; /* PlaneWave RAMP_INIT: PULSE_DURATIONs of the rising ramp before the plateau */
+        float plateau; /* PlaneWave LASER_NOFOCUS_CONSTANT: duration of the plateau */
     } picgb_incident_field;
+    enum picgb_incident_profile
+    {
+        PICGB_PROFILE_GAUSSIAN_PULSE = 0, /* profiles/GaussianPulse.hpp */
+        PICGB_PROFILE_PLANE_WAVE = 1 /* profiles/PlaneWave.hpp */
+    };
     int picgb_set_incident_field(picgb_sim* sim, const picgb_incident_field* field);
 
     /* ------------------------------------------------------------ diagnostics */

@@ -65,7 +65,8 @@ class OrcIncidentFace(ctypes.Structure):
                 ("amplitude", ctypes.c_float), ("wavelength", ctypes.c_float), ("w0", ctypes.c_float),
                 ("pulse_duration", ctypes.c_float), ("time_shift", ctypes.c_float), ("laser_phase", ctypes.c_float),
                 ("phase_velocity", ctypes.c_float), ("time_delay", ctypes.c_float), ("nmodes", ctypes.c_int),
-                ("modes", ctypes.c_float * 8), ("mode_phases", ctypes.c_float * 8)]
+                ("modes", ctypes.c_float * 8), ("mode_phases", ctypes.c_float * 8), ("profile", ctypes.c_int),
+                ("ramp_init", ctypes.c_float), ("nofocus", ctypes.c_float)]
 
 
 class OrcParticles64(ctypes.Structure):
@@ -223,7 +224,8 @@ def set_threads(n: int) -> None:
 
 def incident_face(g, axis, direction, surface, polarisation, a0, wavelength, waist, pulse_duration, time_shift,
                   laser_phase, focus_position, e_over_m=1.0, propagation=None, polarisation_vector=None,
-                  circular=False, time_delay=0.0, laguerre_modes=None, laguerre_phases=None):
+                  circular=False, time_delay=0.0, laguerre_modes=None, laguerre_phases=None, profile=0,
+                  ramp_init=0.0, plateau=0.0):
     """One incident-field face in the reference's parameters (profiles/BaseParam.def,
     GaussianPulse.def): the propagation direction is `propagation` (DIRECTION_*) or the face
     normal, the E polarisation `polarisation_vector` (POLARISATION_DIRECTION_*) or the unit vector
@@ -261,6 +263,7 @@ def incident_face(g, axis, direction, surface, polarisation, a0, wavelength, wai
     f.nmodes = len(modes)
     for m in range(len(modes)):
         f.modes[m], f.mode_phases[m] = modes[m], phases[m]
+    f.profile, f.ramp_init, f.nofocus = int(profile), ramp_init, plateau  # PlaneWave: RAMP_INIT, LASER_NOFOCUS_CONSTANT
     return f
 
 

@@ -49,6 +49,8 @@ extern "C"
         float time_delay;
         int nmodes;
         float modes[8], mode_phases[8];
+        int profile;
+        float ramp_init, nofocus;
     };
     // the FP64 instantiation's exchange format (reference gradients of the differentiable run)
     struct orc_field64
@@ -182,6 +184,9 @@ extern "C"
         face.phaseVelocity = f->phase_velocity;
         face.timeDelay = f->time_delay;
         face.nmodes = f->nmodes;
+        face.profile = f->profile;
+        face.rampInit = f->ramp_init;
+        face.nofocus = f->nofocus;
         for(int m = 0; m < 8; ++m)
         {
             face.modes[m] = f->modes[m];

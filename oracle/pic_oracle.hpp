@@ -1228,7 +1228,35 @@ namespace orc
         float timeDelay = 0.f; // TIME_DELAY
         int nmodes = 1; // laguerreModes / laguerrePhases
         float modes[8] = {1.f}, modePhases[8] = {0.f};
+        int profile = 0; // 0 GaussianPulse, 1 PlaneWave
+        float rampInit = 0.f, nofocus = 0.f; // PlaneWave RAMP_INIT, LASER_NOFOCUS_CONSTANT
     };
+
+    // PlaneWaveFunctorIncidentE::getLongitudinal (profiles/PlaneWave.hpp:79-106)
+    inline float planeWaveLongitudinal(IncidentFace const& f, float omega, float time, float phaseShift)
+    {
+        float envelope = f.amplitude;
+        float const mue = 0.5f * f.rampInit * f.pulseDuration;
+        float const tau = f.pulseDuration * std::sqrt(2.0f);
+        float const endUpramp = mue;
+        float const startDownramp = mue + f.nofocus;
+        float integrationCorrectionFactor = 0.f;
+        if(time > startDownramp)
+        {
+            float const exponent = (time - startDownramp) / tau;
+            envelope *= std::exp(-0.5f * exponent * exponent);
+            integrationCorrectionFactor = (time - startDownramp) / (omega * tau * tau);
+        }
+        else if(time < endUpramp)
+        {
+            float const exponent = (time - endUpramp) / tau;
+            envelope *= std::exp(-0.5f * exponent * exponent);
+            integrationCorrectionFactor = (time - endUpramp) / (omega * tau * tau);
+        }
+        float const timeOszi = time - endUpramp;
+        float const phase = omega * timeOszi + f.laserPhase + phaseShift;
+        return (std::sin(phase) + std::cos(phase) * integrationCorrectionFactor) * envelope;
+    }
 
     // simpleLaguerre (GaussianPulse.hpp:298-323): the Laguerre polynomial L_n(x) by its recursion
     inline float simpleLaguerre(int n, float x)
@@ -1270,7 +1298,14 @@ namespace orc
         float const pos0 = dotf(shift, dirv);
         float const currentTime = t - (pos0 / f.phaseVelocity + f.timeDelay);
         float value = 0.f, value1 = 0.f; // value1: with the phase shifted by pi/2 (circular)
-        if(!(currentTime < 0.f)) // cut off before the pulse reaches this point
+        if(f.profile == 1 && !(currentTime < 0.f))
+        {
+            // BaseSeparableFunctorE with the transversal factor 1 of PlaneWave
+            float const omega = 2.f * 3.14159265358979323846f * g.c / f.wavelength;
+            value = planeWaveLongitudinal(f, omega, currentTime, 0.f) * 1.f;
+            value1 = planeWaveLongitudinal(f, omega, currentTime, 1.57079633f) * 1.f;
+        }
+        else if(!(currentTime < 0.f)) // cut off before the pulse reaches this point
         {
             float const time = currentTime + f.timeShift;
             float const axis2[3] = {dirv[1] * f.polv[2] - dirv[2] * f.polv[1], dirv[2] * f.polv[0] - dirv[0] * f.polv[2],

@@ -74,7 +74,8 @@ class IncidentField(ctypes.Structure):
                 ("t_center", c_float), ("center_x", c_float), ("center_z", c_float), ("phase", c_float),
                 ("focus", c_float), ("direction", c_int), ("propagation", c_float * 3),
                 ("polarisation_vector", c_float * 3), ("circular", c_int), ("time_delay", c_float),
-                ("laguerre_count", c_int), ("laguerre_modes", c_float * 8), ("laguerre_phases", c_float * 8)]
+                ("laguerre_count", c_int), ("laguerre_modes", c_float * 8), ("laguerre_phases", c_float * 8),
+                ("profile", c_int), ("ramp_init", c_float), ("plateau", c_float)]
 
 
 class EnsembleConfig(ctypes.Structure):

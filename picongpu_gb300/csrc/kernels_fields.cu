@@ -253,6 +253,44 @@ namespace picgb
         float const tcur = t - (pos0 * p.invVph + p.timeDelay);
         if(tcur < 0.0f)
             return;
+        if(p.profile == 1)
+        {
+            // PlaneWave (profiles/PlaneWave.hpp getLongitudinal, a separable functor with
+            // transversal factor 1): Gaussian ramps of width tau sqrt(2) around a plateau, and the
+            // integration correction of the sine carrier on the ramps
+            auto longitudinal = [&](float ph)
+            {
+                float envelope = p.E0, corr = 0.0f;
+                float const startDown = p.pwMu + p.pwPlateau;
+                if(tcur > startDown)
+                {
+                    float const ex = (tcur - startDown) / p.pwTau;
+                    envelope *= expf(-0.5f * ex * ex);
+                    corr = (tcur - startDown) / (p.omega * p.pwTau * p.pwTau);
+                }
+                else if(tcur < p.pwMu)
+                {
+                    float const ex = (tcur - p.pwMu) / p.pwTau;
+                    envelope *= expf(-0.5f * ex * ex);
+                    corr = (tcur - p.pwMu) / (p.omega * p.pwTau * p.pwTau);
+                }
+                float const phase = p.omega * (tcur - p.pwMu) + p.phase + ph;
+                return (sinf(phase) + cosf(phase) * corr) * envelope;
+            };
+            if(!p.circular)
+            {
+                float const v = longitudinal(0.0f) * 1.0f;
+#pragma unroll
+                for(int c = 0; c < 3; ++c)
+                    E[c] = p.pv1[c] * v;
+                return;
+            }
+            float const v1 = longitudinal(1.57079633f) * 1.0f, v2 = longitudinal(0.0f) * 1.0f;
+#pragma unroll
+            for(int c = 0; c < 3; ++c)
+                E[c] = p.pv1[c] * v1 + p.pv2[c] * v2;
+            return;
+        }
         float const time = tcur - p.tc;
         float const a1 = s0 * p.pol[0] + s1 * p.pol[1] + s2 * p.pol[2];
         float const a2 = s0 * p.pol2[0] + s1 * p.pol2[1] + s2 * p.pol2[2];

@@ -1349,6 +1349,18 @@ extern "C"
         }
         if(!(std::fabs(p.modeNorm) > 1.1920929e-7f)) // GaussianPulse: "Sum of laguerreModes can not be 0."
             return fail(PICGB_ERR_INVALID, "incident field: the sum of the Laguerre mode amplitudes is 0");
+        if(f->profile != PICGB_PROFILE_GAUSSIAN_PULSE && f->profile != PICGB_PROFILE_PLANE_WAVE)
+            return fail(PICGB_ERR_INVALID, "incident field: unknown profile %d", int(f->profile));
+        p.profile = f->profile;
+        if(p.profile == PICGB_PROFILE_PLANE_WAVE)
+        {
+            if(!(f->ramp_init >= 0.0f) || !(f->plateau >= 0.0f))
+                return fail(PICGB_ERR_INVALID, "incident field: PlaneWave needs ramp_init >= 0 and plateau >= 0");
+            float const tau = float(f->duration_fwhm / (2.0 * std::sqrt(2.0 * std::log(2.0)))); // PULSE_DURATION
+            p.pwMu = 0.5f * f->ramp_init * tau;
+            p.pwTau = tau * std::sqrt(2.0f);
+            p.pwPlateau = f->plateau;
+        }
         if(int r = incidentExtent(s, p))
             return r;
         s->inc[face] = p;

@@ -299,7 +299,8 @@ class Simulation:
                            surface: int, polarisation: int = 0, center=None, phase: float = 0.0,
                            e_over_m: float = 1.0, focus: float = 0.0, axis: int = 1, direction: int = 1,
                            propagation=None, polarisation_vector=None, circular: bool = False,
-                           time_delay: float = 0.0, laguerre_modes=None, laguerre_phases=None) -> None:
+                           time_delay: float = 0.0, laguerre_modes=None, laguerre_phases=None,
+                           profile: str = "GaussianPulse", ramp_init: float = 0.0, plateau: float = 0.0) -> None:
         """Focused Gaussian pulse entering through the TF/SF face normal to `axis` (0, 1, 2):
         direction +1 from the low face along +axis, -1 from the high face along -axis
         (fields/incidentField/Solver.hpp, profiles/GaussianPulse.hpp).  `surface` is the first
@@ -311,7 +312,12 @@ class Simulation:
         and `polarisation_vector` (unit 3-vectors, DIRECTION_* and POLARISATION_DIRECTION_*) give
         oblique incidence through the face, `circular` circular polarisation; `time_delay` is
         TIME_DELAY and `laguerre_modes` / `laguerre_phases` (up to 8) the Laguerre-Gauss mode sum
-        of GaussianPulse.  Each face holds its own pulse; see picgb_set_incident_field."""
+        of GaussianPulse.  profile "PlaneWave" is profiles/PlaneWave.hpp with `ramp_init` (RAMP_INIT)
+        and `plateau` (LASER_NOFOCUS_CONSTANT).  Each face holds its own pulse; see
+        picgb_set_incident_field."""
+        profiles = {"GaussianPulse": 0, "PlaneWave": 1}
+        if profile not in profiles:
+            raise ValueError(f"unknown incident profile {profile!r}: 'GaussianPulse' or 'PlaneWave'")
         cells = (self.grid.nx, self.grid.ny, self.grid.nz)
         t1, t2 = [d for d in range(3) if d != axis] if axis in (0, 1, 2) else (0, 2)
         c1, c2 = center if center is not None else (cells[t1] / 2.0, cells[t2] / 2.0)
@@ -320,7 +326,8 @@ class Simulation:
                             (ctypes.c_float * 3)(*(polarisation_vector or (0, 0, 0))), int(bool(circular)),
                             float(time_delay), len(laguerre_modes or ()),
                             (ctypes.c_float * 8)(*(laguerre_modes or ())),
-                            (ctypes.c_float * 8)(*(laguerre_phases or ())))
+                            (ctypes.c_float * 8)(*(laguerre_phases or ())), profiles[profile], float(ramp_init),
+                            float(plateau))
         L.call("picgb_set_incident_field", self.handle, ctypes.byref(f))
 
     def clear_incident_field(self, axis: int | None = None, direction: int = 1) -> None:
