@@ -293,7 +293,13 @@ extern "C"
      * T = tau sqrt(2), E = E0 (sin(ph) + cos(ph) f) env, ph = omega (t_loc - mu) + phase, env =
      * exp(-(t_loc - mu)^2 / (2 T^2)) and f = (t_loc - mu) / (omega T^2) on the rising ramp (t_loc < mu),
      * the same with mu + plateau on the falling ramp (t_loc > mu + plateau), env = 1 and f = 0 on the
-     * plateau. */
+     * plateau.  PICGB_PROFILE_WAVEPACKET (profiles/Wavepacket.hpp) and PICGB_PROFILE_POLYNOM
+     * (profiles/Polynom.hpp) are separable functors with the transversal factor
+     * exp(-((x_1 / W0_1)^2 + (x_2 / W0_2)^2)), x_1 along the polarisation and x_2 along d x p: the
+     * Wavepacket's carrier and ramp correction as PlaneWave's around a plateau centred at
+     * (pulse_init tau + plateau) / 2; the Polynom's sin(omega (t_loc - tau/2) + phase) times E0
+     * s(2 t_loc / tau), s(u) = u^3 (10 - 15 u + 6 u^2) on [0, 1] and (2 - u)^3 (4 - 9 u + 6 u^2) on
+     * (1, 2].  tau is pulse_duration when > 0, else duration_fwhm / (2 sqrt(2 ln 2)). */
     typedef struct picgb_incident_field
     {
         int32_t enabled;
@@ -313,12 +319,17 @@ extern "C"
         float laguerre_phases[8]; /* laguerrePhases: mode phases */
         int32_t profile; /* PICGB_PROFILE_GAUSSIAN_PULSE (0) or PICGB_PROFILE_PLANE_WAVE */
         float ramp_init; /* PlaneWave RAMP_INIT: PULSE_DURATIONs of the rising ramp before the plateau */
-        float plateau; /* PlaneWave LASER_NOFOCUS_CONSTANT: duration of the plateau */
+        float plateau; /* PlaneWave, Wavepacket LASER_NOFOCUS_CONSTANT: duration of the plateau */
+        float pulse_duration; /* PULSE_DURATION; > 0 replaces the one derived from duration_fwhm */
+        float waist_axis[2]; /* Wavepacket, Polynom W0_AXIS_1, W0_AXIS_2; 0: waist */
+        float pulse_init; /* Wavepacket PULSE_INIT */
     } picgb_incident_field;
     enum picgb_incident_profile
     {
         PICGB_PROFILE_GAUSSIAN_PULSE = 0, /* profiles/GaussianPulse.hpp */
-        PICGB_PROFILE_PLANE_WAVE = 1 /* profiles/PlaneWave.hpp */
+        PICGB_PROFILE_PLANE_WAVE = 1, /* profiles/PlaneWave.hpp */
+        PICGB_PROFILE_WAVEPACKET = 2, /* profiles/Wavepacket.hpp */
+        PICGB_PROFILE_POLYNOM = 3 /* profiles/Polynom.hpp */
     };
     int picgb_set_incident_field(picgb_sim* sim, const picgb_incident_field* field);
 

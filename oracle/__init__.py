@@ -66,7 +66,8 @@ class OrcIncidentFace(ctypes.Structure):
                 ("pulse_duration", ctypes.c_float), ("time_shift", ctypes.c_float), ("laser_phase", ctypes.c_float),
                 ("phase_velocity", ctypes.c_float), ("time_delay", ctypes.c_float), ("nmodes", ctypes.c_int),
                 ("modes", ctypes.c_float * 8), ("mode_phases", ctypes.c_float * 8), ("profile", ctypes.c_int),
-                ("ramp_init", ctypes.c_float), ("nofocus", ctypes.c_float)]
+                ("ramp_init", ctypes.c_float), ("nofocus", ctypes.c_float), ("pulse_init", ctypes.c_float),
+                ("w0_axis1", ctypes.c_float), ("w0_axis2", ctypes.c_float)]
 
 
 class OrcParticles64(ctypes.Structure):
@@ -225,7 +226,7 @@ def set_threads(n: int) -> None:
 def incident_face(g, axis, direction, surface, polarisation, a0, wavelength, waist, pulse_duration, time_shift,
                   laser_phase, focus_position, e_over_m=1.0, propagation=None, polarisation_vector=None,
                   circular=False, time_delay=0.0, laguerre_modes=None, laguerre_phases=None, profile=0,
-                  ramp_init=0.0, plateau=0.0):
+                  ramp_init=0.0, plateau=0.0, pulse_init=0.0, waist_axis=None):
     """One incident-field face in the reference's parameters (profiles/BaseParam.def,
     GaussianPulse.def): the propagation direction is `propagation` (DIRECTION_*) or the face
     normal, the E polarisation `polarisation_vector` (POLARISATION_DIRECTION_*) or the unit vector
@@ -264,6 +265,8 @@ def incident_face(g, axis, direction, surface, polarisation, a0, wavelength, wai
     for m in range(len(modes)):
         f.modes[m], f.mode_phases[m] = modes[m], phases[m]
     f.profile, f.ramp_init, f.nofocus = int(profile), ramp_init, plateau  # PlaneWave: RAMP_INIT, LASER_NOFOCUS_CONSTANT
+    f.pulse_init = pulse_init  # Wavepacket PULSE_INIT
+    f.w0_axis1, f.w0_axis2 = waist_axis if waist_axis else (waist, waist)  # W0_AXIS_1, W0_AXIS_2
     return f
 
 

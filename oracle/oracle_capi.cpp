@@ -50,7 +50,7 @@ extern "C"
         int nmodes;
         float modes[8], mode_phases[8];
         int profile;
-        float ramp_init, nofocus;
+        float ramp_init, nofocus, pulse_init, w0_axis1, w0_axis2;
     };
     // the FP64 instantiation's exchange format (reference gradients of the differentiable run)
     struct orc_field64
@@ -187,6 +187,9 @@ extern "C"
         face.profile = f->profile;
         face.rampInit = f->ramp_init;
         face.nofocus = f->nofocus;
+        face.pulseInit = f->pulse_init;
+        face.w0Axis1 = f->w0_axis1;
+        face.w0Axis2 = f->w0_axis2;
         for(int m = 0; m < 8; ++m)
         {
             face.modes[m] = f->modes[m];

@@ -1228,9 +1228,51 @@ namespace orc
         float timeDelay = 0.f; // TIME_DELAY
         int nmodes = 1; // laguerreModes / laguerrePhases
         float modes[8] = {1.f}, modePhases[8] = {0.f};
-        int profile = 0; // 0 GaussianPulse, 1 PlaneWave
+        int profile = 0; // 0 GaussianPulse, 1 PlaneWave, 2 Wavepacket, 3 Polynom
         float rampInit = 0.f, nofocus = 0.f; // PlaneWave RAMP_INIT, LASER_NOFOCUS_CONSTANT
+        float pulseInit = 0.f; // Wavepacket PULSE_INIT
+        float w0Axis1 = 1.f, w0Axis2 = 1.f; // W0_AXIS_1, W0_AXIS_2
     };
+
+    // WavepacketFunctorIncidentE::getLongitudinal (profiles/Wavepacket.hpp:118-151)
+    inline float wavepacketLongitudinal(IncidentFace const& f, float omega, float time, float phaseShift)
+    {
+        float const initTime = f.pulseInit * f.pulseDuration + f.nofocus;
+        float const endUpramp = -0.5f * f.nofocus, startDownramp = 0.5f * f.nofocus;
+        float const mue = 0.5f * initTime;
+        float const runTime = time - mue;
+        float const tau = f.pulseDuration * std::sqrt(2.f);
+        float envelope = f.amplitude, correctionFactor = 0.f;
+        if(runTime > startDownramp)
+        {
+            float const exponent = ((runTime - startDownramp) / f.pulseDuration / std::sqrt(2.f));
+            envelope *= std::exp(-0.5f * exponent * exponent);
+            correctionFactor = (runTime - startDownramp) / (tau * tau * omega);
+        }
+        else if(runTime < endUpramp)
+        {
+            float const exponent = ((runTime - endUpramp) / f.pulseDuration / std::sqrt(2.f));
+            envelope *= std::exp(-0.5f * exponent * exponent);
+            correctionFactor = (runTime - endUpramp) / (tau * tau * omega);
+        }
+        float const phase = omega * runTime + f.laserPhase + phaseShift;
+        return (std::sin(phase) + correctionFactor * std::cos(phase)) * envelope;
+    }
+
+    // PolynomFunctorIncidentE::getLongitudinal and polynomial (profiles/Polynom.hpp:113-136)
+    inline float polynomLongitudinal(IncidentFace const& f, float omega, float time, float phaseShift)
+    {
+        float const riseTime = 0.5f * f.pulseDuration;
+        float const tau = time / riseTime;
+        float const phase = omega * (time - riseTime) + f.laserPhase + phaseShift;
+        float result = 0.f;
+        if(tau >= 0.f && tau <= 1.f)
+            result = tau * tau * tau * (10.f - 15.f * tau + 6.f * tau * tau);
+        else if(tau > 1.f && tau <= 2.f)
+            result = (2.f - tau) * (2.f - tau) * (2.f - tau) * (4.f - 9.f * tau + 6.f * tau * tau);
+        float const amplitude = f.amplitude * result;
+        return std::sin(phase) * amplitude;
+    }
 
     // PlaneWaveFunctorIncidentE::getLongitudinal (profiles/PlaneWave.hpp:79-106)
     inline float planeWaveLongitudinal(IncidentFace const& f, float omega, float time, float phaseShift)
@@ -1298,12 +1340,31 @@ namespace orc
         float const pos0 = dotf(shift, dirv);
         float const currentTime = t - (pos0 / f.phaseVelocity + f.timeDelay);
         float value = 0.f, value1 = 0.f; // value1: with the phase shifted by pi/2 (circular)
-        if(f.profile == 1 && !(currentTime < 0.f))
+        if(f.profile != 0 && !(currentTime < 0.f))
         {
-            // BaseSeparableFunctorE with the transversal factor 1 of PlaneWave
+            // BaseSeparableFunctorE: longitudinal(time) times the transversal factor, 1 for PlaneWave,
+            // exp(-|internal position / (1, W0_AXIS_1, W0_AXIS_2)|^2) with the propagation coordinate set
+            // to 0 for Wavepacket and Polynom (BaseSeparableTransversalGaussianFunctorE)
             float const omega = 2.f * 3.14159265358979323846f * g.c / f.wavelength;
-            value = planeWaveLongitudinal(f, omega, currentTime, 0.f) * 1.f;
-            value1 = planeWaveLongitudinal(f, omega, currentTime, 1.57079633f) * 1.f;
+            float transversal = 1.f;
+            if(f.profile >= 2)
+            {
+                float const axis2[3] = {dirv[1] * f.polv[2] - dirv[2] * f.polv[1],
+                                        dirv[2] * f.polv[0] - dirv[0] * f.polv[2],
+                                        dirv[0] * f.polv[1] - dirv[1] * f.polv[0]};
+                float const q[3] = {0.f / 1.f, dotf(shift, f.polv) / f.w0Axis1, dotf(shift, axis2) / f.w0Axis2};
+                transversal = std::exp(-(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]));
+            }
+            auto lon = [&](float ph)
+            {
+                if(f.profile == 2)
+                    return wavepacketLongitudinal(f, omega, currentTime, ph);
+                if(f.profile == 3)
+                    return polynomLongitudinal(f, omega, currentTime, ph);
+                return planeWaveLongitudinal(f, omega, currentTime, ph);
+            };
+            value = lon(0.f) * transversal;
+            value1 = lon(1.57079633f) * transversal;
         }
         else if(!(currentTime < 0.f)) // cut off before the pulse reaches this point
         {

@@ -75,7 +75,8 @@ class IncidentField(ctypes.Structure):
                 ("focus", c_float), ("direction", c_int), ("propagation", c_float * 3),
                 ("polarisation_vector", c_float * 3), ("circular", c_int), ("time_delay", c_float),
                 ("laguerre_count", c_int), ("laguerre_modes", c_float * 8), ("laguerre_phases", c_float * 8),
-                ("profile", c_int), ("ramp_init", c_float), ("plateau", c_float)]
+                ("profile", c_int), ("ramp_init", c_float), ("plateau", c_float), ("pulse_duration", c_float),
+                ("waist_axis", c_float * 2), ("pulse_init", c_float)]
 
 
 class EnsembleConfig(ctypes.Structure):

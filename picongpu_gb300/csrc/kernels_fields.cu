@@ -253,13 +253,57 @@ namespace picgb
         float const tcur = t - (pos0 * p.invVph + p.timeDelay);
         if(tcur < 0.0f)
             return;
-        if(p.profile == 1)
+        if(p.profile != 0)
         {
-            // PlaneWave (profiles/PlaneWave.hpp getLongitudinal, a separable functor with
-            // transversal factor 1): Gaussian ramps of width tau sqrt(2) around a plateau, and the
-            // integration correction of the sine carrier on the ramps
+            // separable functors (BaseSeparableFunctorE): E = polarisation (longitudinal(t_loc) transversal)
+            float transversal = 1.0f;
+            if(p.profile >= 2)
+            {
+                // BaseSeparableTransversalGaussianFunctorE::getTransversal: exp(-|x / W0|^2) in the
+                // internal coordinates, the propagation coordinate set to 0
+                float const a1 = (s0 * p.pol[0] + s1 * p.pol[1] + s2 * p.pol[2]) / p.w01;
+                float const a2 = (s0 * p.pol2[0] + s1 * p.pol2[1] + s2 * p.pol2[2]) / p.w02;
+                transversal = expf(-(0.0f + a1 * a1 + a2 * a2));
+            }
             auto longitudinal = [&](float ph)
             {
+                if(p.profile == 2)
+                {
+                    // Wavepacket (profiles/Wavepacket.hpp getLongitudinal)
+                    float const runTime = tcur - p.wpMu;
+                    float const tau = p.pulseDuration * sqrtf(2.0f);
+                    float envelope = p.E0, corr = 0.0f;
+                    float const startDown = 0.5f * p.pwPlateau, endUp = -0.5f * p.pwPlateau;
+                    if(runTime > startDown)
+                    {
+                        float const ex = (runTime - startDown) / p.pulseDuration / sqrtf(2.0f);
+                        envelope *= expf(-0.5f * ex * ex);
+                        corr = (runTime - startDown) / (tau * tau * p.omega);
+                    }
+                    else if(runTime < endUp)
+                    {
+                        float const ex = (runTime - endUp) / p.pulseDuration / sqrtf(2.0f);
+                        envelope *= expf(-0.5f * ex * ex);
+                        corr = (runTime - endUp) / (tau * tau * p.omega);
+                    }
+                    float const phase = p.omega * runTime + p.phase + ph;
+                    return (sinf(phase) + corr * cosf(phase)) * envelope;
+                }
+                if(p.profile == 3)
+                {
+                    // Polynom (profiles/Polynom.hpp getLongitudinal, polynomial)
+                    float const riseTime = 0.5f * p.pulseDuration;
+                    float const u = tcur / riseTime;
+                    float const phase = p.omega * (tcur - riseTime) + p.phase + ph;
+                    float poly = 0.0f;
+                    if(u >= 0.0f && u <= 1.0f)
+                        poly = u * u * u * (10.0f - 15.0f * u + 6.0f * u * u);
+                    else if(u > 1.0f && u <= 2.0f)
+                        poly = (2.0f - u) * (2.0f - u) * (2.0f - u) * (4.0f - 9.0f * u + 6.0f * u * u);
+                    return sinf(phase) * (p.E0 * poly);
+                }
+                // PlaneWave (profiles/PlaneWave.hpp getLongitudinal): Gaussian ramps of width
+                // tau sqrt(2) around a plateau, and the integration correction of the sine carrier
                 float envelope = p.E0, corr = 0.0f;
                 float const startDown = p.pwMu + p.pwPlateau;
                 if(tcur > startDown)
@@ -279,13 +323,13 @@ namespace picgb
             };
             if(!p.circular)
             {
-                float const v = longitudinal(0.0f) * 1.0f;
+                float const v = longitudinal(0.0f) * transversal;
 #pragma unroll
                 for(int c = 0; c < 3; ++c)
                     E[c] = p.pv1[c] * v;
                 return;
             }
-            float const v1 = longitudinal(1.57079633f) * 1.0f, v2 = longitudinal(0.0f) * 1.0f;
+            float const v1 = longitudinal(1.57079633f) * transversal, v2 = longitudinal(0.0f) * transversal;
 #pragma unroll
             for(int c = 0; c < 3; ++c)
                 E[c] = p.pv1[c] * v1 + p.pv2[c] * v2;

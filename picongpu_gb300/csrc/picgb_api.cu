@@ -1298,9 +1298,15 @@ extern "C"
         p.E0 = float(f->a0 * omega * s->cfg.c / f->e_over_m);
         p.omega = float(omega);
         p.w0 = f->waist;
-        // intensity FWHM = 2 sqrt(2 ln 2) tau with tau the rms duration of the intensity
-        // (GaussianPulseEnvelope: exp(-(t / (2 tau))^2) on the field)
-        p.tau2 = float(f->duration_fwhm / std::sqrt(2.0 * std::log(2.0)));
+        // PULSE_DURATION: given, or from the intensity FWHM = 2 sqrt(2 ln 2) tau with tau the rms
+        // duration of the intensity (GaussianPulseEnvelope: exp(-(t / (2 tau))^2) on the field)
+        if(!(f->pulse_duration >= 0.0f))
+            return fail(PICGB_ERR_INVALID, "incident field: pulse_duration must be >= 0");
+        float const pulseTau = f->pulse_duration > 0.0f
+            ? f->pulse_duration
+            : float(f->duration_fwhm / (2.0 * std::sqrt(2.0 * std::log(2.0))));
+        p.pulseDuration = pulseTau;
+        p.tau2 = 2.0f * pulseTau;
         p.tc = f->t_center;
         p.phase = f->phase;
         // origin: the beam axis on the Huygens plane, 0.75 cells inside POSITION
@@ -1349,18 +1355,22 @@ extern "C"
         }
         if(!(std::fabs(p.modeNorm) > 1.1920929e-7f)) // GaussianPulse: "Sum of laguerreModes can not be 0."
             return fail(PICGB_ERR_INVALID, "incident field: the sum of the Laguerre mode amplitudes is 0");
-        if(f->profile != PICGB_PROFILE_GAUSSIAN_PULSE && f->profile != PICGB_PROFILE_PLANE_WAVE)
+        if(f->profile < PICGB_PROFILE_GAUSSIAN_PULSE || f->profile > PICGB_PROFILE_POLYNOM)
             return fail(PICGB_ERR_INVALID, "incident field: unknown profile %d", int(f->profile));
         p.profile = f->profile;
+        if(!(f->ramp_init >= 0.0f) || !(f->plateau >= 0.0f) || !(f->pulse_init >= 0.0f))
+            return fail(PICGB_ERR_INVALID, "incident field: ramp_init, plateau and pulse_init must be >= 0");
+        p.pwPlateau = f->plateau;
         if(p.profile == PICGB_PROFILE_PLANE_WAVE)
         {
-            if(!(f->ramp_init >= 0.0f) || !(f->plateau >= 0.0f))
-                return fail(PICGB_ERR_INVALID, "incident field: PlaneWave needs ramp_init >= 0 and plateau >= 0");
-            float const tau = float(f->duration_fwhm / (2.0 * std::sqrt(2.0 * std::log(2.0)))); // PULSE_DURATION
-            p.pwMu = 0.5f * f->ramp_init * tau;
-            p.pwTau = tau * std::sqrt(2.0f);
-            p.pwPlateau = f->plateau;
+            p.pwMu = 0.5f * f->ramp_init * pulseTau;
+            p.pwTau = pulseTau * std::sqrt(2.0f);
         }
+        p.wpMu = 0.5f * (f->pulse_init * pulseTau + f->plateau); // Wavepacket INIT_TIME / 2
+        p.w01 = f->waist_axis[0] > 0.0f ? f->waist_axis[0] : f->waist;
+        p.w02 = f->waist_axis[1] > 0.0f ? f->waist_axis[1] : f->waist;
+        if(!(p.w01 > 0.0f && p.w02 > 0.0f))
+            return fail(PICGB_ERR_INVALID, "incident field: the transverse waists must be > 0");
         if(int r = incidentExtent(s, p))
             return r;
         s->inc[face] = p;

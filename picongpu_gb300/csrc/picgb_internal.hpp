@@ -129,8 +129,11 @@ namespace picgb
         int nmodes; // Laguerre-Gauss modes 0 .. nmodes-1 (1: the fundamental mode)
         float modes[8], modePhases[8];
         float modeNorm; // the sum of the mode amplitudes
-        int profile; // 0: GaussianPulse, 1: PlaneWave
+        int profile; // 0: GaussianPulse, 1: PlaneWave, 2: Wavepacket, 3: Polynom
         float pwMu, pwTau, pwPlateau; // PlaneWave: end of the rising ramp, ramp width tau sqrt(2), plateau
+        float pulseDuration; // PULSE_DURATION (Wavepacket, Polynom)
+        float wpMu; // Wavepacket: centre of the plateau, INIT_TIME / 2
+        float w01, w02; // W0_AXIS_1, W0_AXIS_2 of the transversal Gaussian
         int lo[2], hi[2]; // transverse extent of the face in cells, [lo, hi) on each transverse axis
     };
     constexpr int kIncidentFaces = 6; // face = 2 axis + (dir < 0)

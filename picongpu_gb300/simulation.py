@@ -300,7 +300,8 @@ class Simulation:
                            e_over_m: float = 1.0, focus: float = 0.0, axis: int = 1, direction: int = 1,
                            propagation=None, polarisation_vector=None, circular: bool = False,
                            time_delay: float = 0.0, laguerre_modes=None, laguerre_phases=None,
-                           profile: str = "GaussianPulse", ramp_init: float = 0.0, plateau: float = 0.0) -> None:
+                           profile: str = "GaussianPulse", ramp_init: float = 0.0, plateau: float = 0.0,
+                           pulse_duration: float = 0.0, waist_axis=None, pulse_init: float = 0.0) -> None:
         """Focused Gaussian pulse entering through the TF/SF face normal to `axis` (0, 1, 2):
         direction +1 from the low face along +axis, -1 from the high face along -axis
         (fields/incidentField/Solver.hpp, profiles/GaussianPulse.hpp).  `surface` is the first
@@ -313,11 +314,13 @@ class Simulation:
         oblique incidence through the face, `circular` circular polarisation; `time_delay` is
         TIME_DELAY and `laguerre_modes` / `laguerre_phases` (up to 8) the Laguerre-Gauss mode sum
         of GaussianPulse.  profile "PlaneWave" is profiles/PlaneWave.hpp with `ramp_init` (RAMP_INIT)
-        and `plateau` (LASER_NOFOCUS_CONSTANT).  Each face holds its own pulse; see
-        picgb_set_incident_field."""
-        profiles = {"GaussianPulse": 0, "PlaneWave": 1}
+        and `plateau` (LASER_NOFOCUS_CONSTANT), "Wavepacket" and "Polynom" their profiles with
+        `waist_axis` (W0_AXIS_1, W0_AXIS_2) and, for the Wavepacket, `pulse_init` (PULSE_INIT) and
+        `plateau`; `pulse_duration` > 0 gives PULSE_DURATION directly.  Each face holds its own
+        pulse; see picgb_set_incident_field."""
+        profiles = {"GaussianPulse": 0, "PlaneWave": 1, "Wavepacket": 2, "Polynom": 3}
         if profile not in profiles:
-            raise ValueError(f"unknown incident profile {profile!r}: 'GaussianPulse' or 'PlaneWave'")
+            raise ValueError(f"unknown incident profile {profile!r}: one of {sorted(profiles)}")
         cells = (self.grid.nx, self.grid.ny, self.grid.nz)
         t1, t2 = [d for d in range(3) if d != axis] if axis in (0, 1, 2) else (0, 2)
         c1, c2 = center if center is not None else (cells[t1] / 2.0, cells[t2] / 2.0)
@@ -327,7 +330,8 @@ class Simulation:
                             float(time_delay), len(laguerre_modes or ()),
                             (ctypes.c_float * 8)(*(laguerre_modes or ())),
                             (ctypes.c_float * 8)(*(laguerre_phases or ())), profiles[profile], float(ramp_init),
-                            float(plateau))
+                            float(plateau), float(pulse_duration), (ctypes.c_float * 2)(*(waist_axis or (0.0, 0.0))),
+                            float(pulse_init))
         L.call("picgb_set_incident_field", self.handle, ctypes.byref(f))
 
     def clear_incident_field(self, axis: int | None = None, direction: int = 1) -> None:

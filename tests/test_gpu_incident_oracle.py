@@ -11,7 +11,7 @@ dot products, updated[comp2] += base * inc[comp1], updated[comp1] -= base * inc[
 Contract: E and B agree within 2e-6 of the amplitude E0 = a0 omega (measured on GB300: 2e-7
 to 3e-7), for faces on all three axes, both directions and both polarisations, for two faces
 at once, at oblique incidence (s and p polarised), with circular polarisation, with a sum of
-Laguerre-Gauss modes and TIME_DELAY, and for the PlaneWave profile (profiles/PlaneWave.hpp); the rest is float rounding of the carrier's argument (up to about 40 rad) and
+Laguerre-Gauss modes and TIME_DELAY, and for the PlaneWave, Wavepacket and Polynom profiles; the rest is float rounding of the carrier's argument (up to about 40 rad) and
 the GPU's fused multiply-adds.  A structural difference (a quarter cell in the origin, a sign,
 a staggering) shows at 1e-2 E0 or more.
 """
@@ -39,7 +39,8 @@ def dims(axis):
 
 
 def oracle_face(gd, axis, direction, surface, pol, center, prop=None, polvec=None, circular=False, delay=0.0,
-                modes=None, phases=None, profile="GaussianPulse", ramp_init=0.0, plateau=0.0):
+                modes=None, phases=None, profile="GaussianPulse", ramp_init=0.0, plateau=0.0, pulse_duration=0.0,
+                waist_axis=None, pulse_init=0.0):
     """The face in the reference's parameters: the origin is the beam axis on the Huygens plane (a
     quarter cell before the first or last total E plane) at the transverse centre, the focus lies
     `focus` face-axis cells from it along the propagation."""
@@ -52,13 +53,15 @@ def oracle_face(gd, axis, direction, surface, pol, center, prop=None, polvec=Non
     origin[t2] = center[1] * cell[t2]
     origin[axis] = (surface - 0.25 * direction) * cell[axis]
     focus = [origin[a] + BEAM["focus"] * cell[axis] * d[a] for a in range(3)]
-    tau = BEAM["duration_fwhm"] / (2 * math.sqrt(2 * math.log(2)))  # rms duration of the intensity
+    # PULSE_DURATION: given, or the rms duration of the intensity from its FWHM
+    tau = pulse_duration if pulse_duration > 0 else BEAM["duration_fwhm"] / (2 * math.sqrt(2 * math.log(2)))
     pv = [float(np.float32(v)) for v in polvec] if polvec is not None else None
     return orc.incident_face(gd, axis, direction, surface, pol, BEAM["a0"], BEAM["wavelength"], BEAM["waist"], tau,
                              -BEAM["t_center"], BEAM["phase"], focus, propagation=d if prop is not None else None,
                              polarisation_vector=pv, circular=circular, time_delay=delay, laguerre_modes=modes,
-                             laguerre_phases=phases, profile=1 if profile == "PlaneWave" else 0, ramp_init=ramp_init,
-                             plateau=plateau)
+                             laguerre_phases=phases,
+                             profile={"GaussianPulse": 0, "PlaneWave": 1, "Wavepacket": 2, "Polynom": 3}[profile],
+                             ramp_init=ramp_init, plateau=plateau, pulse_init=pulse_init, waist_axis=waist_axis)
 
 
 def run_both(axis, faces):
@@ -71,14 +74,16 @@ def run_both(axis, faces):
                                    circular=f.get("circular", False), time_delay=f.get("delay", 0.0),
                                    laguerre_modes=f.get("modes"), laguerre_phases=f.get("phases"),
                                    profile=f.get("profile", "GaussianPulse"), ramp_init=f.get("ramp_init", 0.0),
-                                   plateau=f.get("plateau", 0.0), **BEAM)
+                                   plateau=f.get("plateau", 0.0), pulse_duration=f.get("pulse_duration", 0.0),
+                                   waist_axis=f.get("waist_axis"), pulse_init=f.get("pulse_init", 0.0), **BEAM)
         sim.run(STEPS)
         Eg, Bg = sim.get_field("E"), sim.get_field("B")
     E = np.zeros_like(Eg)
     B = np.zeros_like(Bg)
     of = [oracle_face(gd, f["axis"], f["dir"], f["surface"], f["pol"], f["center"], f.get("prop"), f.get("polvec"),
                       f.get("circular", False), f.get("delay", 0.0), f.get("modes"), f.get("phases"),
-                      f.get("profile", "GaussianPulse"), f.get("ramp_init", 0.0), f.get("plateau", 0.0)) for f in faces]
+                      f.get("profile", "GaussianPulse"), f.get("ramp_init", 0.0), f.get("plateau", 0.0),
+                      f.get("pulse_duration", 0.0), f.get("waist_axis"), f.get("pulse_init", 0.0)) for f in faces]
     dt = np.float32(g.dt)
     for s in range(STEPS):
         # the times of the field stages: step dt, step dt + dt/2, (step + 1) dt, in float
@@ -150,12 +155,18 @@ OBLIQUE = [
     dict(axis=2, dir=-1, surface=LONG - 1 - 16, pol=0, center=(13.0, 18.5), profile="PlaneWave", ramp_init=3.0,
          plateau=10.0, prop=unit((0.2, 0.3, -0.9)), polvec=unit(np.cross(unit((0.2, 0.3, -0.9)), (0.0, 1.0, 0.0))),
          circular=True, delay=2.0),
+    # Wavepacket: separate transverse waists, PULSE_INIT, a plateau; circular and oblique
+    dict(axis=1, dir=1, surface=16, pol=0, center=(13.0, 18.5), profile="Wavepacket", waist_axis=(5.0, 8.0),
+         pulse_init=4.0, plateau=6.0, prop=(math.sin(TH), math.cos(TH), 0.0), polvec=(0.0, 0.0, 1.0), circular=True),
+    # Polynom with an explicit PULSE_DURATION, through the low x face
+    dict(axis=0, dir=1, surface=16, pol=1, center=(13.0, 18.5), profile="Polynom", waist_axis=(6.0, 4.0),
+         pulse_duration=30.0),
 ]
 
 
 @pytest.mark.parametrize("face", OBLIQUE, ids=["s-pol", "p-pol", "x-high", "circular", "oblique-circular",
                                                "laguerre-delay", "laguerre-circular-oblique", "plane-wave",
-                                               "plane-wave-circular-oblique"])
+                                               "plane-wave-circular-oblique", "wavepacket", "polynom"])
 def test_oblique_and_circular_faces_match_the_oracle(face):
     Eg, Bg, E, B = run_both(face["axis"], [face])
     scale = max(np.abs(E).max(), np.abs(B).max())
