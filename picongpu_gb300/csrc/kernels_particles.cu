@@ -777,30 +777,46 @@ namespace picgb
         float* a[7];
     };
 
-    // Host-to-device copy by the SMs: segment blockIdx.y, four 16-byte loads per thread and round
-    // in flight when both ends are 16-byte aligned (the rest byte by byte).
+    // Copy of `n` units of type T by the whole grid, four loads per thread and round in flight.
+    template<typename T>
+    __device__ __forceinline__ void copyUnits(T* __restrict__ d, T const* __restrict__ s, size_t n)
+    {
+        size_t const stride = size_t(gridDim.x) * blockDim.x;
+        size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        for(; i + 3 * stride < n; i += 4 * stride)
+        {
+            T const a = s[i], b = s[i + stride], c = s[i + 2 * stride], e = s[i + 3 * stride];
+            d[i] = a;
+            d[i + stride] = b;
+            d[i + 2 * stride] = c;
+            d[i + 3 * stride] = e;
+        }
+        for(; i < n; i += stride)
+            d[i] = s[i];
+    }
+
+    // Host-to-device copy by the SMs: segment blockIdx.y in 16-byte units when both ends are
+    // 16-byte aligned, else in 4-byte units when both are 4-byte aligned (an array offset by one
+    // float), the rest byte by byte.
     __global__ void __launch_bounds__(256) kCopyIn(CopyJobs jobs)
     {
         CopySeg const sg = jobs.s[blockIdx.y];
         char* const d = static_cast<char*>(sg.dst);
         char const* const src = static_cast<char const*>(sg.src);
-        bool const aligned = ((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0;
-        size_t const n16 = aligned ? sg.bytes / 16 : 0;
-        uint4* const d16 = reinterpret_cast<uint4*>(d);
-        uint4 const* const s16 = reinterpret_cast<uint4 const*>(src);
-        size_t const stride = size_t(gridDim.x) * blockDim.x;
-        size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-        for(; i + 3 * stride < n16; i += 4 * stride)
+        uintptr_t const misalign = reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(src);
+        size_t done = 0;
+        if((misalign & 15u) == 0)
         {
-            uint4 const a = s16[i], b = s16[i + stride], c = s16[i + 2 * stride], e = s16[i + 3 * stride];
-            d16[i] = a;
-            d16[i + stride] = b;
-            d16[i + 2 * stride] = c;
-            d16[i + 3 * stride] = e;
+            done = sg.bytes / 16 * 16;
+            copyUnits(reinterpret_cast<uint4*>(d), reinterpret_cast<uint4 const*>(src), sg.bytes / 16);
         }
-        for(; i < n16; i += stride)
-            d16[i] = s16[i];
-        for(size_t j = n16 * 16 + size_t(blockIdx.x) * blockDim.x + threadIdx.x; j < sg.bytes; j += stride)
+        else if((misalign & 3u) == 0)
+        {
+            done = sg.bytes / 4 * 4;
+            copyUnits(reinterpret_cast<uint32_t*>(d), reinterpret_cast<uint32_t const*>(src), sg.bytes / 4);
+        }
+        size_t const stride = size_t(gridDim.x) * blockDim.x;
+        for(size_t j = done + size_t(blockIdx.x) * blockDim.x + threadIdx.x; j < sg.bytes; j += stride)
             d[j] = src[j];
     }
 
