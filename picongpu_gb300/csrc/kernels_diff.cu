@@ -144,7 +144,10 @@ namespace picgb::diff
     // on entry and dL/d(state before the step) on exit; dL/dE, dL/dB of the gather are
     // added to lamE, lamB.  lamJ = dL/dJ of this step.
     template<int SHAPE, typename T>
-    __global__ void __launch_bounds__(kDiffThreads) kDiffAdjoint(
+#ifndef PICGB_ADJOINT_MIN_BLOCKS
+#    define PICGB_ADJOINT_MIN_BLOCKS 3 // resident blocks of 128 threads the adjoint's register budget is sized for
+#endif
+    __global__ void __launch_bounds__(kDiffThreads, PICGB_ADJOINT_MIN_BLOCKS) kDiffAdjoint(
         DiffParticles<T> sp,
         T const* __restrict__ E,
         T const* __restrict__ B,
