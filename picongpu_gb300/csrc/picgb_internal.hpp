@@ -97,12 +97,8 @@ namespace picgb
         JFixed jf; // fixed-point format of the J tile (used when built with PICGB_J_FIXED)
     };
 
-    // Incident Gaussian pulse entering through the total-field/scattered-field surface
-    // y = j0 (fields/incidentField/Solver.hpp:500-533, profiles/GaussianPulse.hpp): the
-    // field at (x, y, z, t) is E0 exp(-r^2 / w0^2) exp(-(tau - tc)^2 / (2 sigma^2))
-    // sin(omega (tau - tc) + phase), tau = t - (y - j0 dy) / c, r the distance from the
-    // axis (cx, cz), polarised along x (pol 0) or z (pol 1), travelling along +y.
-    // One face of the total-field/scattered-field box and its pulse, in the vector form of
+    // One face of the total-field/scattered-field box and its pulse (fields/incidentField/
+    // Solver.hpp:500-533, the profiles of fields/incidentField/profiles/), in the vector form of
     // fields/incidentField/Functors.hpp (BaseFunctorE): propagation direction d, polarisation
     // vectors, origin on the face's Huygens plane.
     struct IncidentParams
