@@ -394,7 +394,7 @@ def run_ensemble(args, local_rank):
         species = [pg.Species("e", -1.0, 1.0, shape=shape), pg.Species("i", 1.0, MASS_P, shape=shape)]
         g = pg.Grid(8, 8, 4, dt=DT, device=local_rank)
         if args.no_ensemble_tune:
-            sc, th, rates = (8, 8, 4), 256, {}
+            sc, th, rates = (8, 8, 4), args.ensemble_threads, {}
         else:
             sc, th, rates = pg.autotune(dims[:ntune], species,
                                         ensemble_inits(pg, ppc[:ntune], u_th[:ntune], dens[:ntune]), grid=g,
@@ -683,7 +683,10 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-boxes", type=int, default=512)
     ap.add_argument("--ensemble-steps", type=int, default=200)
-    ap.add_argument("--no-ensemble-tune", action="store_true", help="8x8x4 supercells, 256 threads, no autotuning")
+    ap.add_argument("--no-ensemble-tune", action="store_true",
+                    help="8x8x4 supercells and --ensemble-threads threads per supercell, no autotuning")
+    ap.add_argument("--ensemble-threads", type=int, default=256, choices=(128, 256, 512),
+                    help="threads per supercell of the batched push with --no-ensemble-tune")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-laser", action="store_true")
     ap.add_argument("--laser-steps", type=int, default=40)

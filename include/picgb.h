@@ -444,7 +444,9 @@ extern "C"
     /* picgb_species_init_plasma on every box with its own parameters: per_box[nbox]. */
     int picgb_ensemble_init_plasma(picgb_ensemble* ens, int32_t species, const picgb_plasma_init* per_box);
     /* nsteps batched steps; one graph launch per step, then a status check (an overflowing
-     * supercell is re-laid out before the next step, as in picgb_step). */
+     * supercell is re-laid out before the next step, as in picgb_step).  The boxes are
+     * periodic and carry no incident field: picgb_set_boundaries and
+     * picgb_set_incident_field refuse a box of an ensemble (PICGB_ERR_UNSUPPORTED). */
     int picgb_ensemble_run(picgb_ensemble* ens, uint32_t nsteps);
     /* picgb_set_sort_interval for every box and for the batched step (one batched reorder per
      * species after every `steps`-th batched step); default 20, 0 = never. */

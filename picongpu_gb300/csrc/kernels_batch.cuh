@@ -3,6 +3,16 @@
 // items (box, supercell) from a global counter, so large and small boxes share
 // the GPU without a launch per box; each item runs the same supercell push as
 // the single-box kernel (kernels_push.cuh) on that box's fields and particles.
+//
+// The grid and push parameters that every box of the launch shares (cell size, time
+// step, speed of light, the species' charge, mass and pusher) are kernel arguments, as
+// in the single-box kernel: the compiler uses them as constant-bank operands.  Only
+// what differs between boxes comes from the work item's descriptor in shared memory:
+// the box's extent, its storage and field pointers and the fixed-point format of its J
+// tile.  With the whole GridParams and PushParams taken from the shared descriptor, the
+// 512-thread kernel held those values in registers and spilled 104 bytes per thread
+// inside the particle loop (2.3 GB of local-memory loads per launch on one 128^3
+// two-stream box, 17 % slower than the single-box kernel on the same box).
 #pragma once
 
 #include "kernels_push.cuh"
@@ -29,7 +39,9 @@ namespace picgb
         uint32_t const* __restrict__ items,
         uint32_t nitems,
         uint32_t* __restrict__ counter,
-        unsigned* __restrict__ status)
+        unsigned* __restrict__ status,
+        GridParams const g0,
+        PushParams const pp0)
     {
         extern __shared__ __align__(16) float smem[];
         __shared__ unsigned s_nhole;
@@ -50,13 +62,22 @@ namespace picgb
             for(int i = threadIdx.x; i < kWords; i += THREADS)
                 reinterpret_cast<uint32_t*>(&s_box)[i] = __ldg(src + i);
             __syncthreads();
+            GridParams g = g0; // the box's extent over the shared grid parameters
+            g.nx = s_box.g.nx;
+            g.ny = s_box.g.ny;
+            g.nz = s_box.g.nz;
+            g.nscx = s_box.g.nscx;
+            g.nscy = s_box.g.nscy;
+            g.nscz = s_box.g.nscz;
+            PushParams pp = pp0; // the box's J-tile format over the species' parameters
+            pp.jf = s_box.pp.jf;
             pushSupercell<SHAPE, SX, SY, SZ, THREADS, ALT, EMZ>(
                 s_box.sp,
                 s_box.E,
                 s_box.B,
                 s_box.J,
-                s_box.g,
-                s_box.pp,
+                g,
+                pp,
                 status,
                 int(batchSc(v)),
                 smem,
@@ -72,6 +93,8 @@ namespace picgb
         uint32_t nitems,
         uint32_t* counter,
         unsigned* status,
+        GridParams const& g0,
+        PushParams const& pp0,
         cudaStream_t stream)
     {
         using TG = TileGeom<Shape<SHAPE>, SuperCell<SX, SY, SZ>, THREADS>;
@@ -92,7 +115,7 @@ namespace picgb
         uint32_t const blocks = std::min<uint32_t>(uint32_t(occ) * uint32_t(nsm), nitems);
         if(blocks == 0)
             return cudaSuccess;
-        k<<<blocks, THREADS, smem, stream>>>(table, items, nitems, counter, status);
+        k<<<blocks, THREADS, smem, stream>>>(table, items, nitems, counter, status, g0, pp0);
         return cudaGetLastError();
     }
 
@@ -132,11 +155,13 @@ namespace picgb
         uint32_t nitems,                                                                                              \
         uint32_t* counter,                                                                                            \
         unsigned* status,                                                                                             \
+        GridParams const& g0,                                                                                         \
+        PushParams const& pp0,                                                                                        \
         cudaStream_t stream)                                                                                          \
     {                                                                                                                 \
         if(threads != 128 && threads != 256 && threads != 512)                                                        \
             return cudaErrorInvalidValue;                                                                             \
-        PICGB_BATCH_CASES(launchPushBatchT, SHAPE, ALT, EMZ, table, items, nitems, counter, status, stream)           \
+        PICGB_BATCH_CASES(launchPushBatchT, SHAPE, ALT, EMZ, table, items, nitems, counter, status, g0, pp0, stream)\
         return cudaErrorInvalidValue;                                                                                 \
     }
 } // namespace picgb

@@ -11,7 +11,7 @@ namespace picgb
 {
 #define PICGB_DECL_BATCH(NAME)                                                                                        \
     cudaError_t launchPushBatch##NAME(int, int, BatchSpecies const*, uint32_t const*, uint32_t, uint32_t*, unsigned*, \
-                                      cudaStream_t);
+                                      GridParams const&, PushParams const&, cudaStream_t);
 #define PICGB_DECL_BATCH_SHAPE(NAME)                                                                                  \
     PICGB_DECL_BATCH(NAME)                                                                                            \
     PICGB_DECL_BATCH(NAME##Alt)                                                                                       \
@@ -108,15 +108,17 @@ namespace picgb
         uint32_t nitems,
         uint32_t* counter,
         unsigned* status,
+        GridParams const& g0,
+        PushParams const& pp0,
         cudaStream_t stream)
     {
         bool const alt = pusher == kPusherHigueraCary || pusher == kPusherVay;
         bool const emz = current == kCurrentEmZ;
 #define PICGB_BATCH_DISPATCH(NAME)                                                                                    \
-    return emz ? (alt ? launchPushBatch##NAME##AltEmZ(scId, threads, table, items, nitems, counter, status, stream)    \
-                      : launchPushBatch##NAME##EmZ(scId, threads, table, items, nitems, counter, status, stream))      \
-               : (alt ? launchPushBatch##NAME##Alt(scId, threads, table, items, nitems, counter, status, stream)       \
-                      : launchPushBatch##NAME(scId, threads, table, items, nitems, counter, status, stream));
+    return emz ? (alt ? launchPushBatch##NAME##AltEmZ(scId, threads, table, items, nitems, counter, status, g0, pp0, stream)    \
+                      : launchPushBatch##NAME##EmZ(scId, threads, table, items, nitems, counter, status, g0, pp0, stream))      \
+               : (alt ? launchPushBatch##NAME##Alt(scId, threads, table, items, nitems, counter, status, g0, pp0, stream)       \
+                      : launchPushBatch##NAME(scId, threads, table, items, nitems, counter, status, g0, pp0, stream));
         switch(shape)
         {
         case 1:

@@ -1239,6 +1239,8 @@ extern "C"
             s->inc[face] = IncidentParams{};
             return PICGB_OK;
         }
+        if(s->inEnsemble)
+            return fail(PICGB_ERR_UNSUPPORTED, "the batched step of an ensemble has no incident field");
         int const cells[3] = {s->cfg.nx, s->cfg.ny, s->cfg.nz};
         int const n = cells[f->axis];
         int const lo = dir > 0 ? 1 : 0, hi = n - 1; // the scattered-side B plane exists: surface - 1 or surface

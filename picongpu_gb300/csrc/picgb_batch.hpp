@@ -41,7 +41,10 @@ namespace picgb
     __host__ __device__ inline uint32_t batchSc(uint32_t it) { return it & (kBatchMaxSc - 1u); }
 
     // Persistent push over every work item (one launch per species): `gridBlocks`
-    // blocks take items from `*counter` (zero at launch) until all are done.
+    // blocks take items from `*counter` (zero at launch) until all are done.  g0 and pp0
+    // hold what every box shares (cell size, time step, c, eps0, the open-axis bits; the
+    // species' charge, mass, pusher and current); the table supplies each box's extent,
+    // storage, fields and J-tile format.
     cudaError_t launchPushBatch(
         int shape,
         int scId,
@@ -53,6 +56,8 @@ namespace picgb
         uint32_t nitems,
         uint32_t* counter,
         unsigned* status,
+        GridParams const& g0,
+        PushParams const& pp0,
         cudaStream_t stream);
     // kReorder over every work item; maxCap = the largest slots per supercell of any box.
     cudaError_t launchReorderBatch(

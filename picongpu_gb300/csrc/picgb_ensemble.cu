@@ -234,7 +234,10 @@ namespace
         for(size_t k = 0; k < nspec; ++k)
             if(pushed[k])
             {
-                auto const& cfg = e->boxes[0]->species[k]->cfg;
+                picgb_sim const* b0 = e->boxes[0];
+                auto const& cfg = b0->species[k]->cfg;
+                // what every box shares, as kernel arguments; the table entries hold the rest
+                PushParams const pp0 = hs[k * nbox].pp;
                 launch(launchPushBatch(
                     cfg.shape,
                     scId,
@@ -246,6 +249,8 @@ namespace
                     e->nitems,
                     e->dCounters + k,
                     e->dStatus,
+                    b0->g,
+                    pp0,
                     e->stream));
                 ++kernels;
             }

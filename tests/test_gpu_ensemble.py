@@ -9,7 +9,9 @@ Contract:
 * over 10 steps the FP64 energies of every box agree within 1e-5 relative;
 * an overflowing supercell inside a batched step is re-laid out and no
   particle is lost;
-* the autotuner times every candidate and returns the fastest.
+* the autotuner times every candidate and returns the fastest;
+* the boxes stay periodic and without incident field (the batched field kernels have
+  neither): a box's handle refuses open boundaries and an incident pulse.
 """
 import numpy as np
 import pytest
@@ -157,3 +159,18 @@ def test_batched_higuera_cary_and_vay_match_single_box(pusher):
                 pa, pb = sorted_by_id(a.box(i).get_particles(name)), sorted_by_id(b.box(i).get_particles(name))
                 for k in ("pos", "mom", "sc", "lcell"):
                     assert np.array_equal(pa[k], pb[k]), (pusher, i, name, k)
+
+
+def test_ensemble_boxes_refuse_open_boundaries_and_incident_fields():
+    dims = [(16, 32, 16), (16, 32, 16)]
+    pulse = dict(a0=1.0, wavelength=16.0, waist=4.0, duration_fwhm=5.0, t_center=10.0, axis=1, surface=8)
+    with pg.Ensemble(dims) as ens:
+        ens.add_species(pg.Species("e", -1.0, 1.0, shape="TSC"))
+        ens.init_plasma("e", [pg.plasma_init(2, 0.02, 0.01, seed=b) for b in range(len(dims))])
+        with pytest.raises(pg.PicError):
+            ens.box(1).set_boundaries(open_axes=(False, True, False), thickness=((0, 0), (4, 4), (0, 0)))
+        with pytest.raises(pg.PicError):
+            ens.box(1).set_incident_field(**pulse)
+        ens.box(1).clear_incident_field()
+        ens.box(1).clear_incident_field(axis=1)
+        ens.run(1)
