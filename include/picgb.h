@@ -422,7 +422,7 @@ extern "C"
      * MPI domain); this form has no counterpart there.  Every box is a complete simulation
      * handle (picgb_ensemble_box) that the single-box API reads and writes as usual; the
      * ensemble adds the batched step: each kernel of picgb_step runs once over all boxes (the
-     * push as one persistent launch over every supercell of every box), and the whole step
+     * push as one launch per species over every supercell of every box), and the whole step
      * is one CUDA graph launch.  Results per box equal those of picgb_step on that box (the
      * same per-particle and per-cell arithmetic; J sums in another atomic order).  All boxes
      * enqueue on the ensemble's stream. */

@@ -280,6 +280,13 @@ namespace picgb
             Esirkepov<SH>::template run<true>(Tile{smem + jOff, qo, jf}, q0, q1, qs, qc, g, invVdt);
     }
 
+    // The hook pushSupercell runs after the block has loaded its tiles (or found its supercell
+    // empty): nothing in the single-box kernel.
+    struct NoHook
+    {
+        __device__ void operator()() const {}
+    };
+
     // Push of the particles of supercell `sc` by one block of THREADS threads.
     // Each thread pushes one particle per round; then the warp deposits at once
     // the lanes whose particle stays in its assignment cell along every axis
@@ -292,7 +299,9 @@ namespace picgb
     // the other variant serves Boris and Free, so neither carries the other's code.
     // EMZ: the EmZ deposit (each particle's first virtual particle at once, the second,
     // for the particles that change cell, through the warp's queue) instead of Esirkepov.
-    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT, bool EMZ>
+    // Every thread calls hook() once: after the tile loads and their barrier, or at once
+    // when the supercell is empty (the batched kernel fetches its next work item there).
+    template<int SHAPE, int SX, int SY, int SZ, int THREADS, bool ALT, bool EMZ, typename Hook = NoHook>
     __device__ __forceinline__ void pushSupercell(
         SpeciesDev const& sp,
         float const* __restrict__ E,
@@ -303,7 +312,8 @@ namespace picgb
         unsigned* __restrict__ status,
         int const sc,
         float* const smem,
-        unsigned& s_nhole)
+        unsigned& s_nhole,
+        Hook const& hook = Hook{})
     {
         using SH = Shape<SHAPE>;
         using SC = SuperCell<SX, SY, SZ>;
@@ -324,6 +334,7 @@ namespace picgb
         {
             if(threadIdx.x == 0)
                 sp.nhole[sc] = 0u;
+            hook();
             return;
         }
         int scx, scy, scz;
@@ -342,6 +353,7 @@ namespace picgb
             for(int t = threadIdx.x; t < TG::JWords; t += blockDim.x)
                 Js[t] = 0.0f;
         __syncthreads();
+        hook();
 
         size_t const base = size_t(sc) * sp.cap;
         int queued = 0; // jobs in this warp's queue (warp-uniform)

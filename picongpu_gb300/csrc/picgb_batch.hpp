@@ -40,8 +40,9 @@ namespace picgb
     __host__ __device__ inline uint32_t batchBox(uint32_t it) { return it >> kBatchScBits; }
     __host__ __device__ inline uint32_t batchSc(uint32_t it) { return it & (kBatchMaxSc - 1u); }
 
-    // Persistent push over every work item (one launch per species): `gridBlocks`
-    // blocks take items from `*counter` (zero at launch) until all are done.  g0 and pp0
+    // Push over every work item, one launch per species: one block per item, or (built with
+    // PICGB_BATCH_PERSISTENT=1) resident blocks taking items from `*counter`, which is zero
+    // at launch.  g0 and pp0
     // hold what every box shares (cell size, time step, c, eps0, the open-axis bits; the
     // species' charge, mass, pusher and current); the table supplies each box's extent,
     // storage, fields and J-tile format.

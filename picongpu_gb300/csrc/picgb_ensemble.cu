@@ -5,7 +5,7 @@
 // points.  The ensemble adds device tables that describe every box (fields,
 // species storage, push parameters) and a batched step in which each kernel
 // of the single-box step runs once over all boxes:
-//   J = 0 (all boxes) -> persistent push over all (box, supercell) items per
+//   J = 0 (all boxes) -> one push launch over all (box, supercell) items per
 //   species -> compaction per species -> B half, E (+J), B half (all boxes).
 // The step is captured once as a CUDA graph and replayed; after every replay
 // the status word is read so that an overflowing supercell is re-laid out
@@ -143,7 +143,7 @@ namespace
             blockBox.insert(blockBox.end(), nb, uint32_t(i));
         }
         // push work items: the boxes with the most particle slots per supercell first, so that
-        // the persistent blocks finish together
+        // the blocks finish together
         std::vector<uint64_t> work(nbox, 0);
         uint32_t maxCap = 32;
         for(size_t i = 0; i < nbox; ++i)

@@ -4,7 +4,7 @@ Each box is a complete single-box simulation (``box(i)`` returns a
 ``Simulation`` view of it, so particles, fields and diagnostics are read and
 written as usual).  ``run(n)`` advances every box with the batched step: each
 kernel of Simulation::runOneStep runs once over all boxes, the push as one
-persistent launch over every supercell of every box, and the step is one CUDA
+launch per species over every supercell of every box, and the step is one CUDA
 graph launch.  ``run_sequential(n)`` advances the boxes one after the other
 through the single-box path instead.  ``autotune`` picks the supercell size
 and the threads per supercell of the batched push by timing each candidate.

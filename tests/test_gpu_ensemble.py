@@ -1,4 +1,4 @@
-"""Batched ensemble (one persistent push over every box, the step as one CUDA
+"""Batched ensemble (one push launch per species over every box, the step as one CUDA
 graph) against the single-box path on the same boxes.
 
 Contract:
