@@ -681,7 +681,7 @@ namespace picgb
     {
         if(n == 0)
             return cudaSuccess;
-        int const blocks = int(std::min<uint64_t>((n + 255) / 256, 152 * 16));
+        int const blocks = int(std::min<uint64_t>((n + 255) / 256, uint64_t(smCount()) * 16));
         kMaxAbsBits<<<blocks, 256, 0, stream>>>(n, w, bits);
         return cudaGetLastError();
     }
@@ -700,7 +700,7 @@ namespace picgb
         int const vol = scId == 0 ? 256 : (scId == 1 ? 64 : 512);
         if(n == 0)
             return cudaSuccess;
-        int const blocks = int(std::min<uint64_t>((n + 255) / 256, 152 * 64));
+        int const blocks = int(std::min<uint64_t>((n + 255) / 256, uint64_t(smCount()) * 64));
         float const* px = pos ? pos[0] : nullptr;
         float const* py = pos ? pos[1] : nullptr;
         float const* pz = pos ? pos[2] : nullptr;
@@ -768,7 +768,7 @@ namespace picgb
         Attr7 a;
         for(int i = 0; i < 7; ++i)
             a.a[i] = attr[i];
-        int const blocks = int(std::min<uint64_t>((n + 255) / 256, 152 * 64));
+        int const blocks = int(std::min<uint64_t>((n + 255) / 256, uint64_t(smCount()) * 64));
         kScatter<<<blocks, 256, 0, stream>>>(n, a, sc, lcell, id, sp, status);
         return cudaGetLastError();
     }
@@ -826,10 +826,7 @@ namespace picgb
     {
         if(jobs.n <= 0)
             return cudaSuccess;
-        int sms = 0, dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        dim3 const grid(unsigned((sms > 0 ? sms : 152) * 2), unsigned(jobs.n));
+        dim3 const grid(unsigned(smCount() * 2), unsigned(jobs.n));
         kCopyIn<<<grid, 256, 0, stream>>>(jobs);
         return cudaGetLastError();
     }
@@ -894,10 +891,7 @@ namespace picgb
         OutAttr o;
         for(int i = 0; i < 7; ++i)
             o.a[i] = attr[i];
-        int sms = 0, dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        uint64_t const blocks = std::min<uint64_t>((total + 255) / 256, uint64_t(sms > 0 ? sms : 152) * 16);
+        uint64_t const blocks = std::min<uint64_t>((total + 255) / 256, uint64_t(smCount()) * 16);
         kGatherOut<<<unsigned(blocks), 256, 0, stream>>>(sp, offsets, nsc, total, o, sc, lcell, id);
         return cudaGetLastError();
     }
@@ -926,66 +920,71 @@ namespace picgb
     }
 
     // KinEnergy (algorithms/KinEnergy.hpp:43-66) per macro particle in float,
-    // summed in FP64.
-    __global__ void kKineticEnergy(SpeciesDev sp, float mass0, float c, double* out)
+    // summed in FP64.  A grid of resident blocks walks the supercells (one FP64 atomic per
+    // block at the end instead of one per supercell).
+    __global__ void kKineticEnergy(SpeciesDev sp, int nsc, float mass0, float c, double* out)
     {
-        int const sc = blockIdx.x;
-        uint32_t const n = sp.count[sc];
-        size_t const base = size_t(sc) * sp.cap;
         float const c2 = fm(c, c);
-        // per thread a compensated float sum (Neumaier's improved Kahan-Babuska summation:
-        // the rounding error of every addition is collected in `comp`), as the reference sums
-        // per thread in float_X; FP64 from the thread sums on.  An FP64 add per particle runs
-        // on this GPU's narrow FP64 pipe.
+        // per thread and supercell a compensated float sum (compensatedAdd), as the reference
+        // sums per thread in float_X, carried into an FP64 sum per thread after each supercell.
+        // An FP64 add per particle runs on this GPU's narrow FP64 pipe.
         // The loads of kBatch particles are issued before their arithmetic, so a thread waits
         // for memory once per batch; the particles are summed in the same order as one at a time.
         constexpr int kBatch = 8;
-        float sum = 0.0f, comp = 0.0f;
-        for(uint32_t k0 = threadIdx.x; k0 < n; k0 += kBatch * blockDim.x)
+        double acc = 0.0;
+        for(int sc = blockIdx.x; sc < nsc; sc += gridDim.x)
         {
-            float wv[kBatch], uxv[kBatch], uyv[kBatch], uzv[kBatch];
-#pragma unroll
-            for(int b = 0; b < kBatch; ++b)
+            uint32_t const n = sp.count[sc];
+            size_t const base = size_t(sc) * sp.cap;
+            float sum = 0.0f, comp = 0.0f;
+            for(uint32_t k0 = threadIdx.x; k0 < n; k0 += kBatch * blockDim.x)
             {
-                uint32_t const k = k0 + b * blockDim.x;
-                size_t const s = base + (k < n ? k : 0u);
-                wv[b] = sp.w[s];
-                uxv[b] = sp.ux[s];
-                uyv[b] = sp.uy[s];
-                uzv[b] = sp.uz[s];
-            }
+                float wv[kBatch], uxv[kBatch], uyv[kBatch], uzv[kBatch];
 #pragma unroll
-            for(int b = 0; b < kBatch; ++b)
-            {
-                if(k0 + b * blockDim.x >= n)
-                    break;
-                float const m = fm(mass0, wv[b]);
-                float const mom2 = l2n2(uxv[b], uyv[b], uzv[b]);
-                float e;
-                if(m == 0.0f)
-                    e = fm(c, fsq(mom2));
-                else
+                for(int b = 0; b < kBatch; ++b)
                 {
-                    float const r = fdv(1.0f, fm(fm(m, m), c2));
-                    float const gamma = fsq(fa(1.0f, fm(mom2, r)));
-                    if(gamma < 1.005f)
-                        e = fdv(mom2, fm(2.0f, m));
-                    else
-                        e = fm(fm(fs(gamma, 1.0f), m), c2);
+                    uint32_t const k = k0 + b * blockDim.x;
+                    size_t const s = base + (k < n ? k : 0u);
+                    wv[b] = sp.w[s];
+                    uxv[b] = sp.ux[s];
+                    uyv[b] = sp.uy[s];
+                    uzv[b] = sp.uz[s];
                 }
-                float const t = fa(sum, e);
-                comp = fa(comp, fabsf(sum) >= fabsf(e) ? fa(fs(sum, t), e) : fa(fs(e, t), sum));
-                sum = t;
+#pragma unroll
+                for(int b = 0; b < kBatch; ++b)
+                {
+                    if(k0 + b * blockDim.x >= n)
+                        break;
+                    float const m = fm(mass0, wv[b]);
+                    float const mom2 = l2n2(uxv[b], uyv[b], uzv[b]);
+                    float e;
+                    if(m == 0.0f)
+                        e = fm(c, fsq(mom2));
+                    else
+                    {
+                        float const r = fdv(1.0f, fm(fm(m, m), c2));
+                        float const gamma = fsq(fa(1.0f, fm(mom2, r)));
+                        if(gamma < 1.005f)
+                            e = fdv(mom2, fm(2.0f, m));
+                        else
+                            e = fm(fm(fs(gamma, 1.0f), m), c2);
+                    }
+                    compensatedAdd(sum, comp, e);
+                }
             }
+            acc += double(sum) + double(comp);
         }
-        double const s = blockSumD(double(sum) + double(comp));
+        double const s = blockSumD(acc);
         if(threadIdx.x == 0 && s != 0.0)
             atomicAdd(out, s);
     }
 
     cudaError_t launchKineticEnergy(SpeciesDev const& sp, int nsc, float mass, float c, double* out, cudaStream_t stream)
     {
-        kKineticEnergy<<<nsc, 256, 0, stream>>>(sp, mass, c, out);
+        if(nsc <= 0)
+            return cudaSuccess;
+        int const blocks = std::min(nsc, smCount() * 8);
+        kKineticEnergy<<<blocks, 256, 0, stream>>>(sp, nsc, mass, c, out);
         return cudaGetLastError();
     }
 } // namespace picgb

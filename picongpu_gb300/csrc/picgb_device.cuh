@@ -24,6 +24,17 @@ namespace picgb
     __device__ __forceinline__ float fdv(float a, float b) { return __fdiv_rn(a, b); }
     __device__ __forceinline__ float fsq(float a) { return __fsqrt_rn(a); }
 
+    // One step of Neumaier's compensated summation (the improved Kahan-Babuska sum): e is
+    // added to sum, and the rounding error of that addition is collected in comp.  The pair
+    // (sum, comp), carried into FP64 as double(sum) + double(comp), holds the float sum with
+    // an error of order n 2^-48 of the sum of |e|.
+    __device__ __forceinline__ void compensatedAdd(float& sum, float& comp, float e)
+    {
+        float const t = fa(sum, e);
+        comp = fa(comp, fabsf(sum) >= fabsf(e) ? fa(fs(sum, t), e) : fa(fs(e, t), sum));
+        sum = t;
+    }
+
     // ------------------------------------------------------------ shapes
     // particles/shapes/{NGP,CIC,TSC,PQS,PCS}.hpp; SHAPE = assignment order, support = SHAPE + 1.
     template<int SHAPE>

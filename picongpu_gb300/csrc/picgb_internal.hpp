@@ -9,6 +9,24 @@ namespace picgb
 {
     struct GridParams; // picgb_device.cuh
 
+    // Multiprocessors of the current device, for sizing grid-stride launches (queried once
+    // per device; 152, the GB300's count, if the query fails).
+    inline int smCount()
+    {
+        static int cache[64] = {};
+        int dev = 0;
+        if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+            return 152;
+        if(cache[dev] == 0)
+        {
+            int n = 0;
+            if(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+                n = 152;
+            cache[dev] = n;
+        }
+        return cache[dev];
+    }
+
 #ifndef PICGB_J_FIXED
     // 1: the shared-memory J tile holds 32-bit fixed-point high and low parts
     // added with native fire-and-forget integer atomics; 0: floats added with
