@@ -394,17 +394,27 @@ namespace picgb
         __host__ __device__ static int rank(int vol) { return starts(vol) + kReorderRounds + 1; } // uint16 [cap]
         __host__ __device__ static int inv(int vol, uint32_t cap) { return rank(vol) + int((cap + 1) / 2); } // uint16 [cap]
         __host__ __device__ static int buf(int vol, uint32_t cap) { return inv(vol, cap) + int((cap + 1) / 2); } // uint32 [cap]
-        __host__ __device__ static size_t bytes(int vol, uint32_t cap) { return sizeof(uint32_t) * (size_t(buf(vol, cap)) + cap); }
+        // bitmap of the vacated slots (the compacting form)
+        __host__ __device__ static int holes(int vol, uint32_t cap) { return buf(vol, cap) + int(cap); } // uint32 [cap / 32]
+        __host__ __device__ static size_t bytes(int vol, uint32_t cap)
+        {
+            return sizeof(uint32_t) * (size_t(holes(vol, cap)) + (cap + 31) / 32);
+        }
     };
 
     // Loads per thread issued before the first shared-memory store of a staging pass, so
     // that a pass costs one memory latency instead of one per loop iteration.
     constexpr int kReorderLoads = 8;
 
-    // a[j] = a_old[inv[j]] for j < n, staged through buf.  The bits of a 32-bit or 16-bit
-    // attribute pass through buf unchanged.
+    // a[j] = a_old[inv[j]] for j < nOut, staged through buf (slots [0, n) are read).  The bits
+    // of a 32-bit or 16-bit attribute pass through buf unchanged.
     template<typename T>
-    __device__ __forceinline__ void permuteInPlace(T* __restrict__ a, uint32_t n, uint32_t* buf, uint16_t const* inv)
+    __device__ __forceinline__ void permuteInPlace(
+        T* __restrict__ a,
+        uint32_t n,
+        uint32_t nOut,
+        uint32_t* buf,
+        uint16_t const* inv)
     {
         static_assert(sizeof(T) == 4 || sizeof(T) == 2, "32-bit or 16-bit attributes");
         using Bits = typename std::conditional<sizeof(T) == 4, uint32_t, uint16_t>::type;
@@ -428,17 +438,52 @@ namespace picgb
             }
         }
         __syncthreads();
-        for(uint32_t j = threadIdx.x; j < n; j += blockDim.x)
+        for(uint32_t j = threadIdx.x; j < nOut; j += blockDim.x)
             ab[j] = Bits(buf[inv[j]]);
         __syncthreads();
     }
 
     // Reorder of supercell sc by one block (rsm: ReorderSmem::bytes(vol, sp.cap) of shared memory).
-    __device__ void reorderSupercell(SpeciesDev const& sp, int sc, int vol, uint32_t* rsm, int& s_tooFull)
+    // COMPACT: the supercell as the push left it (slots [0, min(tail, cap)), the vacated slots in
+    // `holes`) is compacted by the same pass, in place of kCompact: the vacated slots are left
+    // out of the sort and the count becomes the particles that remain.  Where the sort cannot
+    // run (a cell of more than kReorderRounds particles) warp 0 compacts the supercell as
+    // kCompact does.  counters (COMPACT, or nullptr): [64][2] sums of the vacated slots and of
+    // the particles after the step, one slot pair per block index mod 64.
+    template<bool COMPACT>
+    __device__ void reorderSupercell(
+        SpeciesDev const& sp,
+        int sc,
+        int vol,
+        uint32_t* rsm,
+        int& s_tooFull,
+        unsigned long long* counters = nullptr)
     {
-        uint32_t const n = sp.count[sc];
-        if(n < 2)
-            return;
+        uint32_t n, h = 0;
+        if constexpr(COMPACT)
+        {
+            uint32_t const tail = sp.tail[sc];
+            n = tail < sp.cap ? tail : sp.cap;
+            h = sp.nhole[sc];
+            if(threadIdx.x == 0 && counters)
+            {
+                atomicAdd(counters + 2 * (blockIdx.x & 63u), (unsigned long long) h);
+                atomicAdd(counters + 2 * (blockIdx.x & 63u) + 1, (unsigned long long) (n - h));
+            }
+            if(n < 2 || h == n)
+            {
+                if(threadIdx.x < 32)
+                    compactSupercell(sp, sc, rsm);
+                return;
+            }
+        }
+        else
+        {
+            n = sp.count[sc];
+            if(n < 2)
+                return;
+        }
+        uint32_t const newc = n - h;
         int const words = vol / 32;
         uint32_t* cnt = rsm + ReorderSmem::cnt(vol);
         uint32_t* bm = rsm + ReorderSmem::bm(vol);
@@ -446,12 +491,26 @@ namespace picgb
         uint16_t* rank = reinterpret_cast<uint16_t*>(rsm + ReorderSmem::rank(vol));
         uint16_t* inv = reinterpret_cast<uint16_t*>(rsm + ReorderSmem::inv(vol, sp.cap));
         uint32_t* buf = rsm + ReorderSmem::buf(vol, sp.cap);
+        uint32_t* hb = rsm + ReorderSmem::holes(vol, sp.cap);
         size_t const base = size_t(sc) * sp.cap;
         for(int i = threadIdx.x; i < ReorderSmem::starts(vol); i += blockDim.x)
             rsm[i] = 0u;
+        if constexpr(COMPACT)
+            for(uint32_t i = threadIdx.x; i < (n + 31) / 32; i += blockDim.x)
+                hb[i] = 0u;
         if(threadIdx.x == 0)
             s_tooFull = 0;
         __syncthreads();
+        if constexpr(COMPACT)
+        {
+            for(uint32_t i = threadIdx.x; i < h; i += blockDim.x)
+            {
+                uint32_t const v = sp.holes[base + i];
+                atomicOr(hb + (v >> 5), 1u << (v & 31u));
+            }
+            __syncthreads();
+        }
+        auto vacated = [&](uint32_t k) { return COMPACT && ((hb[k >> 5] >> (k & 31u)) & 1u); };
         for(uint32_t k0 = threadIdx.x; k0 < n; k0 += blockDim.x * kReorderLoads)
         {
             uint16_t lcs[kReorderLoads];
@@ -469,6 +528,8 @@ namespace picgb
                     break;
                 uint32_t const lc = lcs[u];
                 buf[k] = lc;
+                if(vacated(k))
+                    continue;
                 if(lc >= uint32_t(vol)) // not a cell of this supercell: leave the order alone
                 {
                     s_tooFull = 1;
@@ -483,8 +544,16 @@ namespace picgb
             }
         }
         __syncthreads();
-        if(s_tooFull)
-            return; // uniform: every thread read it after the barrier
+        if(s_tooFull) // uniform: every thread read it after the barrier
+        {
+            if constexpr(COMPACT)
+            {
+                __syncthreads(); // every thread is past its read of s_tooFull before rsm is reused
+                if(threadIdx.x < 32)
+                    compactSupercell(sp, sc, rsm);
+            }
+            return;
+        }
         // first slot of every round: a prefix over the rounds' occupied cells
         if(threadIdx.x < 32)
         {
@@ -512,6 +581,8 @@ namespace picgb
         __syncthreads();
         for(uint32_t k = threadIdx.x; k < n; k += blockDim.x)
         {
+            if(vacated(k))
+                continue;
             uint32_t const lc = buf[k], r = rank[k];
             uint32_t const* row = bm + r * words;
             uint32_t before = 0;
@@ -521,23 +592,37 @@ namespace picgb
             inv[starts[r] + before] = uint16_t(k);
         }
         __syncthreads();
-        permuteInPlace(sp.px + base, n, buf, inv);
-        permuteInPlace(sp.py + base, n, buf, inv);
-        permuteInPlace(sp.pz + base, n, buf, inv);
-        permuteInPlace(sp.ux + base, n, buf, inv);
-        permuteInPlace(sp.uy + base, n, buf, inv);
-        permuteInPlace(sp.uz + base, n, buf, inv);
-        permuteInPlace(sp.w + base, n, buf, inv);
-        permuteInPlace(sp.lcell + base, n, buf, inv);
+        permuteInPlace(sp.px + base, n, newc, buf, inv);
+        permuteInPlace(sp.py + base, n, newc, buf, inv);
+        permuteInPlace(sp.pz + base, n, newc, buf, inv);
+        permuteInPlace(sp.ux + base, n, newc, buf, inv);
+        permuteInPlace(sp.uy + base, n, newc, buf, inv);
+        permuteInPlace(sp.uz + base, n, newc, buf, inv);
+        permuteInPlace(sp.w + base, n, newc, buf, inv);
+        permuteInPlace(sp.lcell + base, n, newc, buf, inv);
         if(sp.id)
-            permuteInPlace(sp.id + base, n, buf, inv);
+            permuteInPlace(sp.id + base, n, newc, buf, inv);
+        if constexpr(COMPACT)
+            if(threadIdx.x == 0)
+            {
+                sp.count[sc] = newc;
+                sp.tail[sc] = newc;
+                sp.nhole[sc] = 0u;
+            }
     }
 
     __global__ void __launch_bounds__(kReorderThreads) kReorder(SpeciesDev sp, int vol)
     {
         extern __shared__ uint32_t rsm[];
         __shared__ int s_tooFull;
-        reorderSupercell(sp, int(blockIdx.x), vol, rsm, s_tooFull);
+        reorderSupercell<false>(sp, int(blockIdx.x), vol, rsm, s_tooFull);
+    }
+
+    __global__ void __launch_bounds__(kReorderThreads) kCompactReorder(SpeciesDev sp, int vol, unsigned long long* counters)
+    {
+        extern __shared__ uint32_t rsm[];
+        __shared__ int s_tooFull;
+        reorderSupercell<true>(sp, int(blockIdx.x), vol, rsm, s_tooFull, counters);
     }
 
     // The reorder over the supercells of every box of an ensemble: block b handles work item b.
@@ -547,7 +632,7 @@ namespace picgb
         extern __shared__ uint32_t rsm[];
         __shared__ int s_tooFull;
         uint32_t const it = items[blockIdx.x];
-        reorderSupercell(boxes[batchBox(it)].sp, int(batchSc(it)), vol, rsm, s_tooFull);
+        reorderSupercell<false>(boxes[batchBox(it)].sp, int(batchSc(it)), vol, rsm, s_tooFull);
     }
 
     size_t reorderSmemBytes(int vol, uint32_t cap) { return ReorderSmem::bytes(vol, cap); }
@@ -562,6 +647,19 @@ namespace picgb
                 return e;
         }
         kReorder<<<nsc, kReorderThreads, smem, stream>>>(sp, vol);
+        return cudaGetLastError();
+    }
+
+    cudaError_t launchCompactReorder(SpeciesDev const& sp, int nsc, int vol, unsigned long long* counters, cudaStream_t stream)
+    {
+        size_t const smem = ReorderSmem::bytes(vol, sp.cap);
+        if(smem > 48 * 1024)
+        {
+            cudaError_t e = cudaFuncSetAttribute(kCompactReorder, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if(e != cudaSuccess)
+                return e;
+        }
+        kCompactReorder<<<nsc, kReorderThreads, smem, stream>>>(sp, vol, counters);
         return cudaGetLastError();
     }
 

@@ -260,6 +260,8 @@ namespace picgb::host
         CUDA_TRY(dalloc(d.sp_lcell, size_t(d.spill_cap)));
         CUDA_TRY(dalloc(d.sp_id, size_t(d.spill_cap)));
         CUDA_TRY(dalloc(d.sp_count, 1));
+        CUDA_TRY(dalloc(sp.leaveCount, size_t(128)));
+        CUDA_TRY(cudaMemsetAsync(sp.leaveCount, 0, sizeof(unsigned long long) * 128, s->stream));
         CUDA_TRY(cudaMemsetAsync(d.count, 0, sizeof(uint32_t) * s->nsc, s->stream));
         CUDA_TRY(cudaMemsetAsync(d.tail, 0, sizeof(uint32_t) * s->nsc, s->stream));
         CUDA_TRY(cudaMemsetAsync(d.nhole, 0, sizeof(uint32_t) * s->nsc, s->stream));
@@ -447,6 +449,35 @@ namespace picgb::host
         return PICGB_OK;
     }
 
+    // Fraction of a species' particles that left their supercell in a step, above which the
+    // step compacts it with the compacting reorder (kCompactReorder) every step instead of
+    // hole filling (kCompact): hole filling moves each arrival with scattered 4-byte accesses,
+    // and a sort that visits every particle once restores the interleaved order as well.
+    constexpr double kHotLeaveFraction = 0.03;
+
+    // The counters of the compacting reorders of the last step (the stream is synchronised):
+    // the species' leave fraction decides whether the next steps sort it every step.
+    int readLeaveCounts(picgb_sim* s)
+    {
+        for(auto& sp : s->species)
+        {
+            if(!sp->allocated || !sp->counted)
+                continue;
+            unsigned long long c[128];
+            CUDA_TRY(cudaMemcpy(c, sp->leaveCount, sizeof(c), cudaMemcpyDeviceToHost));
+            CUDA_TRY(cudaMemsetAsync(sp->leaveCount, 0, sizeof(c), s->stream));
+            unsigned long long left = 0, kept = 0;
+            for(int i = 0; i < 64; ++i)
+            {
+                left += c[2 * i];
+                kept += c[2 * i + 1];
+            }
+            sp->hot = double(left) > kHotLeaveFraction * double(left + kept);
+            sp->counted = false;
+        }
+        return PICGB_OK;
+    }
+
     // After a step: the profiling events are read and spilled arrivals re-inserted.
     int afterStep(picgb_sim* s)
     {
@@ -454,6 +485,8 @@ namespace picgb::host
         if(int r = readStatus(s, &bits, false))
             return r;
         CUDA_TRY(profFlush(s));
+        if(int r = readLeaveCounts(s))
+            return r;
         return reinsertSpilled(s, bits);
     }
 
@@ -462,6 +495,8 @@ namespace picgb::host
     {
         unsigned bits = 0;
         if(int r = readStatus(s, &bits, false))
+            return r;
+        if(int r = readLeaveCounts(s))
             return r;
         return reinsertSpilled(s, bits);
     }
@@ -485,24 +520,28 @@ namespace picgb::host
                 return launchPush(x.cfg.shape, s->cfg.supercell, x.dev, s->E, s->B, s->J, s->g, pp, s->status, s->stream);
             }));
         }
+        // compaction: every sortInterval steps, and every step for a species that leaves its
+        // supercells often, by the compacting reorder (it also restores the interleaved order);
+        // otherwise by hole filling
+        bool const sortStep = s->sortInterval && ++s->stepsSinceSort >= s->sortInterval;
+        if(sortStep)
+            s->stepsSinceSort = 0;
+        int const vol = s->sc[0] * s->sc[1] * s->sc[2];
         for(auto& sp : s->species)
         {
             if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE)
                 continue;
             Species& x = *sp;
-            CUDA_TRY(timedLaunch(s, PICGB_KERNEL_COMPACT, [&] { return launchCompact(x.dev, s->nsc, s->stream); }));
-        }
-        if(s->sortInterval && ++s->stepsSinceSort >= s->sortInterval)
-        {
-            s->stepsSinceSort = 0;
-            int const vol = s->sc[0] * s->sc[1] * s->sc[2];
-            for(auto& sp : s->species)
+            bool const canSort = s->sortInterval && reorderSmemBytes(vol, x.dev.cap) <= 200 * 1024;
+            if(canSort && (sortStep || x.hot))
             {
-                if(!sp->allocated || sp->cfg.pusher == PICGB_PUSHER_NONE || reorderSmemBytes(vol, sp->dev.cap) > 200 * 1024)
-                    continue;
-                Species& x = *sp;
-                CUDA_TRY(timedLaunch(s, PICGB_KERNEL_REORDER, [&] { return launchReorder(x.dev, s->nsc, vol, s->stream); }));
+                CUDA_TRY(timedLaunch(s, PICGB_KERNEL_REORDER, [&] {
+                    return launchCompactReorder(x.dev, s->nsc, vol, x.leaveCount, s->stream);
+                }));
+                x.counted = true;
             }
+            else
+                CUDA_TRY(timedLaunch(s, PICGB_KERNEL_COMPACT, [&] { return launchCompact(x.dev, s->nsc, s->stream); }));
         }
         return PICGB_OK;
     }

@@ -177,6 +177,15 @@ namespace picgb
     cudaError_t launchCompact(SpeciesDev const& sp, int nsc, cudaStream_t stream);
     // Interleaved cell order restored in every supercell (kReorder); vol = cells per supercell.
     cudaError_t launchReorder(SpeciesDev const& sp, int nsc, int vol, cudaStream_t stream);
+    // Compaction of the push's vacated slots and the interleaved order in one pass per supercell
+    // (in place of launchCompact); counters: [64][2] sums of vacated slots and of the particles
+    // that remain, added to (or nullptr).
+    cudaError_t launchCompactReorder(
+        SpeciesDev const& sp,
+        int nsc,
+        int vol,
+        unsigned long long* counters,
+        cudaStream_t stream);
     // Shared memory kReorder needs for slots of `cap` particles per supercell.
     size_t reorderSmemBytes(int vol, uint32_t cap);
     cudaError_t launchMaxAbsBits(float const* w, uint64_t n, unsigned* bits, cudaStream_t stream);

@@ -70,6 +70,12 @@ namespace picgb::host
         int nsc = 0;
         bool allocated = false;
         float wmax = 0.0f; // largest |weighting| (bounds a single J contribution)
+        // compaction by the compacting reorder: its counters ([64][2] sums of vacated slots and of
+        // remaining particles), whether the last launch wrote them, and whether the species
+        // leaves its supercells often enough to take that path every step
+        unsigned long long* leaveCount = nullptr;
+        bool counted = false;
+        bool hot = false;
 
         void freeAll()
         {
@@ -91,6 +97,8 @@ namespace picgb::host
             dfree(dev.sp_lcell);
             dfree(dev.sp_id);
             dfree(dev.sp_count);
+            dfree(leaveCount);
+            counted = false;
             allocated = false;
         }
     };

@@ -8,6 +8,11 @@
   slots of the first m rounds (m = the smallest count of a cell) hold cell k mod vol.
 * Over 30 steps with a reorder every 7 steps the FP64 energies follow the run without
   reorders within 1e-4 (the deposit sums in another order).
+* The reorder of a step also compacts the slots the push vacated (kCompactReorder in place of
+  kCompact): bit-exact with hole filling after one step, also for a supercell with a cell of
+  more than 64 particles, where the sort gives way to hole filling.
+* A species that leaves its supercells often (more than 3 % of it per step, measured at a
+  reorder) is reordered every step from then on; a cold one only every sort interval.
 """
 import numpy as np
 import pytest
@@ -123,3 +128,53 @@ def test_batched_reorder_moves_particles_only():
                 key[k] = seen[c] * vol + c
                 seen[c] += 1
             assert np.all(np.diff(key) > 0)
+
+
+def crowded(sort_interval):
+    """A 4 ppc plasma plus 120 particles in cell (3, 3, 3), which some of them leave."""
+    g = pg.Grid(32, 32, 16, dt=DT)
+    sim = pg.Simulation(g)
+    sim.add_species(pg.Species("e", -1.0, 1.0, shape="TSC", with_ids=True))
+    sim.init_plasma("e", 4, 0.02, 0.2, seed=11, position_seed=12)
+    p = sim.get_particles("e")
+    rng = np.random.default_rng(13)
+    m = 120
+    extra = dict(pos=rng.random((3, m), dtype=np.float32), mom=(0.3 * rng.standard_normal((3, m))).astype(np.float32),
+                 w=np.full(m, p["w"][0], np.float32), sc=np.zeros(m, np.int32),
+                 lcell=np.full(m, 3 + 8 * (3 + 8 * 3), np.uint16),
+                 id=np.arange(p["id"].max() + 1, p["id"].max() + 1 + m, dtype=np.uint32))
+    sim.set_particles("e", {k: np.concatenate([p[k], extra[k]], axis=-1) for k in p})
+    sim.set_sort_interval(sort_interval)
+    return sim
+
+
+def test_compacting_reorder_falls_back_for_a_crowded_cell():
+    a, b = crowded(1), crowded(0)
+    with a, b:
+        n0 = a.particle_count("e")
+        a.step()
+        b.step()
+        pa, pb = sorted_by_id(a.get_particles("e")), sorted_by_id(b.get_particles("e"))
+        assert pa["id"].size == n0
+        for k in ("id", "pos", "mom", "w", "sc", "lcell"):
+            assert np.array_equal(pa[k], pb[k]), k
+        assert a.device_status() == 0
+
+
+def reorder_launches(u_th, steps):
+    g = pg.Grid(32, 32, 16, dt=DT)
+    with pg.Simulation(g) as sim:
+        sim.add_species(pg.Species("e", -1.0, 1.0, shape="TSC"))
+        sim.init_plasma("e", 4, 0.02, u_th, seed=15, position_seed=16)
+        n0 = sim.particle_count("e")
+        sim.profile(True)
+        sim.run(steps)
+        kt = sim.kernel_times()
+        assert sim.particle_count("e") == n0
+        return kt["reorder"][1], kt["compact"][1]
+
+
+def test_hot_species_is_reordered_every_step():
+    # default interval 20: the reorder of step 20 measures the leave fraction
+    assert reorder_launches(0.001, 25) == (1, 24)  # cold: hole filling between the reorders
+    assert reorder_launches(0.5, 25) == (6, 19)  # hot: every step from step 21 on
