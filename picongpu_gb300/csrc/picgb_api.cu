@@ -262,6 +262,7 @@ namespace picgb::host
         CUDA_TRY(dalloc(d.sp_count, 1));
         CUDA_TRY(dalloc(sp.leaveCount, size_t(128)));
         CUDA_TRY(cudaMemsetAsync(sp.leaveCount, 0, sizeof(unsigned long long) * 128, s->stream));
+        sp.probe = true;
         CUDA_TRY(cudaMemsetAsync(d.count, 0, sizeof(uint32_t) * s->nsc, s->stream));
         CUDA_TRY(cudaMemsetAsync(d.tail, 0, sizeof(uint32_t) * s->nsc, s->stream));
         CUDA_TRY(cudaMemsetAsync(d.nhole, 0, sizeof(uint32_t) * s->nsc, s->stream));
@@ -520,9 +521,9 @@ namespace picgb::host
                 return launchPush(x.cfg.shape, s->cfg.supercell, x.dev, s->E, s->B, s->J, s->g, pp, s->status, s->stream);
             }));
         }
-        // compaction: every sortInterval steps, and every step for a species that leaves its
-        // supercells often, by the compacting reorder (it also restores the interleaved order);
-        // otherwise by hole filling
+        // compaction: every sortInterval steps, every step for a species that leaves its
+        // supercells often, and in the first step after new storage (to measure that), by the
+        // compacting reorder (it also restores the interleaved order); otherwise by hole filling
         bool const sortStep = s->sortInterval && ++s->stepsSinceSort >= s->sortInterval;
         if(sortStep)
             s->stepsSinceSort = 0;
@@ -533,8 +534,9 @@ namespace picgb::host
                 continue;
             Species& x = *sp;
             bool const canSort = s->sortInterval && reorderSmemBytes(vol, x.dev.cap) <= 200 * 1024;
-            if(canSort && (sortStep || x.hot))
+            if(canSort && (sortStep || x.hot || x.probe))
             {
+                x.probe = false;
                 CUDA_TRY(timedLaunch(s, PICGB_KERNEL_REORDER, [&] {
                     return launchCompactReorder(x.dev, s->nsc, vol, x.leaveCount, s->stream);
                 }));

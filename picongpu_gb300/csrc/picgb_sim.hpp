@@ -76,6 +76,7 @@ namespace picgb::host
         unsigned long long* leaveCount = nullptr;
         bool counted = false;
         bool hot = false;
+        bool probe = false; // the next step measures the leave fraction (set for new storage)
 
         void freeAll()
         {

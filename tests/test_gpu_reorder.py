@@ -11,8 +11,9 @@
 * The reorder of a step also compacts the slots the push vacated (kCompactReorder in place of
   kCompact): bit-exact with hole filling after one step, also for a supercell with a cell of
   more than 64 particles, where the sort gives way to hole filling.
-* A species that leaves its supercells often (more than 3 % of it per step, measured at a
-  reorder) is reordered every step from then on; a cold one only every sort interval.
+* A species that leaves its supercells often (more than 3 % of it per step, measured by the
+  reorder of the first step and of every sort step) is reordered every step from then on; a
+  cold one only in its first step and every sort interval.
 """
 import numpy as np
 import pytest
@@ -175,6 +176,6 @@ def reorder_launches(u_th, steps):
 
 
 def test_hot_species_is_reordered_every_step():
-    # default interval 20: the reorder of step 20 measures the leave fraction
-    assert reorder_launches(0.001, 25) == (1, 24)  # cold: hole filling between the reorders
-    assert reorder_launches(0.5, 25) == (6, 19)  # hot: every step from step 21 on
+    # default interval 20: the reorders of steps 1 and 20 measure the leave fraction
+    assert reorder_launches(0.001, 25) == (2, 23)  # cold: hole filling between the reorders
+    assert reorder_launches(0.5, 25) == (25, 0)  # hot: every step from step 2 on
