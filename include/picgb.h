@@ -385,8 +385,12 @@ extern "C"
      * slot while they move between cells, which spreads a warp's particles over the supercell and
      * raises the push kernel's shared-memory bank conflicts (two-stream 256^3: 6 % after 200
      * steps); the reorder moves every particle once (about 3 ms per species there).  The
-     * reference's particle order inside a supercell is not specified either
-     * (pmacc/particles/ParticlesBase.kernel:183-359 fills gaps in arbitrary order). */
+     * reorder also compacts the slots the push vacated, in place of that step's hole filling.
+     * A species that left its supercells at more than 3 % of its particles in a reordered step
+     * (the first step after new particle storage is one) is reordered every step from then
+     * on, as long as steps > 0.  The reference's particle order inside a supercell is not
+     * specified either (pmacc/particles/ParticlesBase.kernel:183-359 fills gaps in arbitrary
+     * order). */
     int picgb_set_sort_interval(picgb_sim* sim, uint32_t steps);
     int picgb_synchronize(picgb_sim* sim);
     /* Device-side kernel launches issued by this handle since creation (own kernels only). */
@@ -401,12 +405,12 @@ extern "C"
     enum picgb_kernel_class
     {
         PICGB_KERNEL_PUSH = 0, /* fused gather/push/move(/deposit)/migration */
-        PICGB_KERNEL_COMPACT = 1, /* hole compaction after the migration */
+        PICGB_KERNEL_COMPACT = 1, /* hole filling after the migration (steps without a reorder) */
         PICGB_KERNEL_YEE_B = 2, /* B half step */
         PICGB_KERNEL_YEE_E = 3, /* E step (+ J) */
         PICGB_KERNEL_DEPOSIT = 4, /* separate deposit (fuse_deposit = 0) */
         PICGB_KERNEL_ADD_CURRENT = 5, /* separate J add (fuse_deposit = 0) */
-        PICGB_KERNEL_REORDER = 6, /* interleaved cell order restored (picgb_set_sort_interval) */
+        PICGB_KERNEL_REORDER = 6, /* compaction with the interleaved cell order restored (picgb_set_sort_interval) */
         PICGB_KERNEL_CLASSES = 7
     };
     int picgb_profile_enable(picgb_sim* sim, int32_t on);
