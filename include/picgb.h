@@ -387,8 +387,8 @@ extern "C"
      * steps); the reorder moves every particle once (about 3 ms per species there).  The
      * reorder also compacts the slots the push vacated, in place of that step's hole filling.
      * A species that left its supercells at more than 3 % of its particles in a reordered step
-     * (the first step after new particle storage is one) is reordered every step from then
-     * on, as long as steps > 0.  The reference's particle order inside a supercell is not
+     * (the first step after picgb_species_init_plasma is one) is reordered every step from
+     * then on, as long as steps > 0.  The reference's particle order inside a supercell is not
      * specified either (pmacc/particles/ParticlesBase.kernel:183-359 fills gaps in arbitrary
      * order). */
     int picgb_set_sort_interval(picgb_sim* sim, uint32_t steps);

@@ -262,7 +262,6 @@ namespace picgb::host
         CUDA_TRY(dalloc(d.sp_count, 1));
         CUDA_TRY(dalloc(sp.leaveCount, size_t(128)));
         CUDA_TRY(cudaMemsetAsync(sp.leaveCount, 0, sizeof(unsigned long long) * 128, s->stream));
-        sp.probe = true;
         CUDA_TRY(cudaMemsetAsync(d.count, 0, sizeof(uint32_t) * s->nsc, s->stream));
         CUDA_TRY(cudaMemsetAsync(d.tail, 0, sizeof(uint32_t) * s->nsc, s->stream));
         CUDA_TRY(cudaMemsetAsync(d.nhole, 0, sizeof(uint32_t) * s->nsc, s->stream));
@@ -522,8 +521,9 @@ namespace picgb::host
             }));
         }
         // compaction: every sortInterval steps, every step for a species that leaves its
-        // supercells often, and in the first step after new storage (to measure that), by the
-        // compacting reorder (it also restores the interleaved order); otherwise by hole filling
+        // supercells often, and in the first step after a device plasma initialisation (to
+        // measure that), by the compacting reorder (it also restores the interleaved order);
+        // otherwise by hole filling
         bool const sortStep = s->sortInterval && ++s->stepsSinceSort >= s->sortInterval;
         if(sortStep)
             s->stepsSinceSort = 0;
@@ -877,6 +877,8 @@ extern "C"
         CUDA_TRY(launchInitPlasma(sp.dev, s->g, ip, s->sc, s->stream));
         ++s->launches;
         CUDA_TRY(cudaStreamSynchronize(s->stream));
+        sp.probe = true; // a new plasma: its first step measures how fast it leaves its supercells
+        sp.hot = false;
         return PICGB_OK;
     }
 

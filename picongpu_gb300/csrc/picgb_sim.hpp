@@ -76,7 +76,7 @@ namespace picgb::host
         unsigned long long* leaveCount = nullptr;
         bool counted = false;
         bool hot = false;
-        bool probe = false; // the next step measures the leave fraction (set for new storage)
+        bool probe = false; // the next step measures the leave fraction (set by the plasma initialisation)
 
         void freeAll()
         {

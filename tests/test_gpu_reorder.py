@@ -12,8 +12,9 @@
   kCompact): bit-exact with hole filling after one step, also for a supercell with a cell of
   more than 64 particles, where the sort gives way to hole filling.
 * A species that leaves its supercells often (more than 3 % of it per step, measured by the
-  reorder of the first step and of every sort step) is reordered every step from then on; a
-  cold one only in its first step and every sort interval.
+  reorder of the first step after its device initialisation and of every sort step) is
+  reordered every step from then on; a cold one only in that first step and every sort
+  interval.
 """
 import numpy as np
 import pytest
